@@ -1,0 +1,337 @@
+"""Benchmark of the GB300 geodesic tracer (one JSON line on rank 0).
+
+Workload (the headline of the reference's own benchmarks, and the scene of
+its 4K x 256 spp Kerr claim): Kerr a/M = 0.94, 3840x2160, 256 samples per
+pixel with Halton(2,3) jitter, observer at r = 40 M, inclination 75 deg
+(elevation 0.261799 rad), vertical FOV 30 deg, disc from the prograde ISCO to
+30 M, peak temperature 1e4 K, reference defaults otherwise.  One bench step is
+one progressive pass of 16 samples per pixel over the full frame
+(132,710,400 rays); 16 steps make the 256-spp frame.
+
+  value   Mrays/s, device time (CUDA events on the launching stream) over the
+          K timed steps, inputs resident; max over ranks.
+  e2e     the same metric through the public C ABI with host buffers: per
+          step a full 16-spp frame (uniforms host->device, RGBA8 frame
+          device->host into pinned memory), wall clock.
+  roofline  the trace kernel against the device's measured FP32 FMA ceiling:
+          algorithmic FLOPs (the reference formulas' operation count per
+          integrator step, counted by the CPU oracle, times the steps the GPU
+          took) / the kernel's event-timed duration.
+  cpu_baseline  the CPU oracle (a restatement of the reference kernel,
+          bit-exact with it on the host) on all host cores, on a bounded
+          sample of the same workload.
+
+`--impl reference` times the reference algorithm on the host cores (the CPU
+oracle; the reference's own sources are not present on the GPU host) on the
+same workload and prints the same line with "impl": "reference".
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WIDTH, HEIGHT, SPP, SPP_PER_STEP = 3840, 2160, 256, 16
+METRIC = "Kerr geodesic Mrays/s at 4K x 256spp"
+
+
+def workload_uniforms(S, spp=SPP):
+    isco = S.kerr_isco_prograde(1.0, 0.94)
+    scene = S.Scene(spin_a_over_M=0.94, disc_inner_M=isco, disc_outer_M=30.0, disc_peak_T_K=1e4,
+                    render_supersample=spp)
+    cam = S.build_orbital_camera(40.0, 0.261799, 0.0, 30.0)
+    return S.pack_uniforms(scene, cam, WIDTH, HEIGHT, 0.0)
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, reasons)."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = threading.Thread(target=self._run, daemon=True)
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self) -> dict:
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if "Active" in s[3 + i]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def cpu_baseline(S, O, u, seconds: float = 12.0, seed: int = 0) -> dict:
+    """The CPU oracle on a random pixel subset with the step's 16 samples."""
+    threads = os.cpu_count() or 1
+    rng = np.random.default_rng(seed)
+    npix = u.width * u.height
+
+    def run(n):
+        pix = rng.choice(npix, n, replace=False).astype(np.uint32)
+        gx = np.repeat(pix % u.width, SPP_PER_STEP)
+        gy = np.repeat(pix // u.width, SPP_PER_STEP)
+        s = np.tile(np.arange(SPP_PER_STEP, dtype=np.uint32), n)
+        t0 = time.perf_counter()
+        O.trace(u, gx, gy, s, threads=threads)
+        return gx.size, time.perf_counter() - t0
+
+    rays, dt = run(256)
+    n = int(max(256, min(200_000, 256 * seconds / max(dt, 1e-3))))
+    rays, dt = run(n)
+    return {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+            "sample": f"{n} random pixels x {SPP_PER_STEP} Halton samples of the workload ({rays} rays, "
+                      f"{dt:.1f} s), FP32 oracle"}
+
+
+def ops_per_step(S, O, u, n: int = 1024, seed: int = 1) -> tuple[float, float]:
+    """Reference-formula FP32 ops per integrator step (ratio estimator over a
+    random sample of the workload's rays) and mean steps per ray."""
+    rng = np.random.default_rng(seed)
+    gx = rng.integers(0, u.width, n).astype(np.uint32)
+    gy = rng.integers(0, u.height, n).astype(np.uint32)
+    s = rng.integers(0, SPP, n).astype(np.uint32)
+    ops, steps, _ = O.count_ops(u, gx, gy, s)
+    return float(ops.sum()) / max(1.0, float(steps.sum())), float(steps.mean())
+
+
+def run_reference(args, rank: int) -> None:
+    if rank != 0:
+        return
+    import singularity_gb300 as S
+    from oracle import pyoracle as O
+    O.build(ref=False)
+    u = workload_uniforms(S)
+    threads = os.cpu_count() or 1
+    rng = np.random.default_rng(0)
+    npix = u.width * u.height
+    n_pix = 2048  # bounded sample per step: 2048 pixels x 16 samples
+
+    def step():
+        pix = rng.choice(npix, n_pix, replace=False).astype(np.uint32)
+        gx = np.repeat(pix % u.width, SPP_PER_STEP)
+        gy = np.repeat(pix // u.width, SPP_PER_STEP)
+        s = np.tile(np.arange(SPP_PER_STEP, dtype=np.uint32), n_pix)
+        O.trace(u, gx, gy, s, threads=threads)
+        return gx.size
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    rays = sum(step() for _ in range(args.steps))
+    dt = time.perf_counter() - t0
+    v = rays / dt / 1e6
+    line = {"metric": METRIC, "value": v, "unit": "Mrays/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": {"workload": "kerr_a0.94_r40_i75_fov30_3840x2160_256spp_fixed_h0.4",
+                       "sample_per_step": f"{n_pix} random pixels x {SPP_PER_STEP} samples"},
+            "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                             "sample": f"{n_pix} random pixels x {SPP_PER_STEP} Halton samples per step"},
+            "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=16)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--e2e-steps", type=int, default=4)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--rhs-form", type=int, default=0)
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import torch
+    import torch.distributed as dist
+
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+
+    import singularity_gb300 as S
+    from singularity_gb300 import _native as N
+
+    lib = N.load()
+    u = workload_uniforms(S)
+    # Weak scaling: each rank renders its own view (camera azimuth offset per rank).
+    if world > 1:
+        cam = S.build_orbital_camera(40.0, 0.261799, 2 * np.pi * rank / world, 30.0)
+        isco = S.kerr_isco_prograde(1.0, 0.94)
+        u = S.pack_uniforms(S.Scene(spin_a_over_M=0.94, disc_inner_M=isco, disc_outer_M=30.0, disc_peak_T_K=1e4,
+                                    render_supersample=SPP), cam, WIDTH, HEIGHT, 0.0)
+    npix = u.width * u.height
+    r = S.Renderer(local)
+    stream = torch.cuda.Stream()
+    d_out = torch.empty(npix * 4, dtype=torch.uint8, device="cuda")
+    opts = S.default_opts(sample_count=SPP_PER_STEP, rhs_form=args.rhs_form)
+    passes = SPP // SPP_PER_STEP
+    step_idx = [0]
+    stats_acc = {"steps": 0, "rays": 0, "trace_ms": [], "budget": 0}
+
+    def step(record=True):
+        k = step_idx[0] % passes
+        opts.sample_begin = k * SPP_PER_STEP
+        st = lib.sgx_render_device(r.handle, C.byref(u), C.byref(opts), C.c_void_p(d_out.data_ptr()),
+                                   N.FORMAT_RGBA8_SRGB, C.c_void_p(stream.cuda_stream))
+        if st != 0:
+            raise RuntimeError(lib.sgx_last_error(r.handle).decode())
+        step_idx[0] += 1
+        if record:
+            s = r.stats()
+            stats_acc["steps"] += s.steps
+            stats_acc["rays"] += s.rays
+            stats_acc["budget"] += s.budget_hits
+            stats_acc["trace_ms"].append(s.trace_ms)
+
+    for _ in range(args.warmup):
+        step(record=False)
+    step_idx[0] = 0  # timed region starts a fresh 256-spp frame
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    rays_total = stats_acc["rays"] * world
+    value = rays_total / (ms / 1e3) / 1e6
+
+    # --- e2e through the public API with host buffers ---
+    e2e = None
+    if args.e2e_steps > 0:
+        u16 = u.copy()
+        u16.supersample = SPP_PER_STEP
+        host = torch.empty(npix * 4, dtype=torch.uint8, pin_memory=True)
+        ref_opts = S.default_opts(rhs_form=args.rhs_form)
+
+        def e2e_step():
+            st = lib.sgx_render(r.handle, C.byref(u16), C.byref(ref_opts))
+            if st != 0:
+                raise RuntimeError(lib.sgx_last_error(r.handle).decode())
+            st = lib.sgx_capture(r.handle, C.c_void_p(host.data_ptr()), host.numel(), N.FORMAT_RGBA8_SRGB)
+            if st != 0:
+                raise RuntimeError(lib.sgx_last_error(r.handle).decode())
+        e2e_step()
+        if world > 1:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            e2e_step()
+        dt = time.perf_counter() - t0
+        if world > 1:
+            t = torch.tensor([dt], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dt = float(t.item())
+        e2e = {"value": npix * SPP_PER_STEP * args.e2e_steps * world / dt / 1e6, "unit": "Mrays/s",
+               "h2d_bytes_per_step": C.sizeof(N.Uniforms), "d2h_bytes_per_step": npix * 4,
+               "note": "sgx_render (full 16-spp frame) + sgx_capture RGBA8 into pinned host memory, wall clock"}
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+
+    # --- roofline of the trace kernel ---
+    from oracle import pyoracle as O
+    O.build(ref=False)
+    ops_step, mean_steps_cpu = ops_per_step(S, O, u)
+    trace_ms = np.array(stats_acc["trace_ms"])
+    per_launch_ms = float(trace_ms.mean())
+    steps_per_launch = stats_acc["steps"] / max(1, len(trace_ms))
+    achieved = ops_step * steps_per_launch / (per_launch_ms * 1e-3) / 1e12
+    peak = C.c_double(0)
+    lib.sgx_measure_fp32_peak(local, 20000, C.byref(peak))
+    traffic = None
+    tp = ROOT / "profiles" / "trace_kernel_traffic.json"
+    if tp.exists():
+        t = json.loads(tp.read_text())
+        traffic = t.get("bytes_per_ray", 0) * npix * SPP_PER_STEP if "bytes_per_ray" in t else None
+    roof = {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
+            "frac": achieved / peak.value if peak.value else None, "traffic": traffic,
+            "peak_source": "measured: register-resident FMA ceiling (sgx_measure_fp32_peak) on this GPU",
+            "ops_per_step": ops_step, "kernel_ms_per_launch": per_launch_ms,
+            "gpu_steps_per_ray": stats_acc["steps"] / max(1, stats_acc["rays"]),
+            "cpu_oracle_steps_per_ray": mean_steps_cpu}
+
+    cpu = None if args.no_cpu_baseline else cpu_baseline(S, O, u)
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": value / 13.1, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "kerr_a0.94_r40_i75_fov30_isco-30M_T1e4_3840x2160_256spp_fixed_h0.4_max2500",
+                   "spp_per_step": SPP_PER_STEP, "rays_per_step": npix * SPP_PER_STEP,
+                   "integrator": "fixed-step RK4 (reference algorithm)", "rhs_form": args.rhs_form,
+                   "l2": "each step writes a 2.1 GB per-sample buffer (> 129 MB L2); no extra flush",
+                   "vs_baseline_basis": "13.1 Mrays/s: 4K Kerr a/M=0.94 256 spp in 162 s on an RTX 3090 "
+                                        "(README.md:39,130), wall clock incl. PNG"},
+        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+        "gpu_launches": 3 * args.steps,
+        "budget_exhausted_rays": stats_acc["budget"],
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,222 @@
+/*
+ * sgx.h — C ABI of the GB300 geodesic tracer (the drop-in boundary).
+ *
+ * Plain C: pointers, sizes, status codes; no CUDA or torch types.  Every entry
+ * point below names the reference interface it replaces.  The reference's
+ * boundary is the C++ class CudaBackend
+ * (render/cuda/cuda_backend.hpp:17-46, render/include/render_backend.hpp:107-132)
+ * and below it the kernel `singularity_geodesic_kernel(uint8_t*, Uniforms)`
+ * (render/cuda/kernels/geodesic_kernel.cu:462).  The C++ shim
+ * singularity_gb300/csrc/cuda_backend.hpp re-creates that class on top of
+ * these functions, so the reference's cuda_cli relinks unchanged.
+ *
+ * Error behaviour: the reference prints CUDA errors and carries on
+ * (cuda_backend.cu:38-43); here every call returns an sgx_status and the
+ * context keeps the last message for sgx_last_error().
+ *
+ * Threading: a context is used by one host thread at a time; all its GPU
+ * work runs on the context's own stream.
+ */
+#ifndef SGX_H
+#define SGX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "sgx_uniforms.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SGX_ABI_VERSION 1
+
+typedef enum sgx_status {
+    SGX_OK = 0,
+    SGX_ERR_INVALID_ARGUMENT = 1,
+    SGX_ERR_CUDA = 2,
+    SGX_ERR_OUT_OF_MEMORY = 3,
+    SGX_ERR_NOT_RENDERED = 4,
+    SGX_ERR_UNSUPPORTED = 5
+} sgx_status;
+
+/* Output encodings of a rendered frame. */
+typedef enum sgx_format {
+    SGX_FORMAT_RGBA8_SRGB = 0, /* reference output: ACES per sample, mean, sRGB, u8 */
+    SGX_FORMAT_RGBA32F = 1,    /* the same mean before sRGB/quantisation, float, alpha 1 */
+    SGX_FORMAT_RGBA16F_HDR = 2 /* mean scene-referred HDR (x exposure), half, alpha 1 */
+} sgx_format;
+
+/* Arithmetic of the integration. */
+typedef enum sgx_precision {
+    SGX_PRECISION_FP32 = 0,  /* bulk FP32 */
+    SGX_PRECISION_MIXED = 1, /* FP32 bulk, FP64 constants of motion and FP64 step control
+                                near the photon orbit and the horizon */
+    SGX_PRECISION_FP64 = 2   /* FP64 throughout */
+} sgx_precision;
+
+typedef enum sgx_integrator {
+    SGX_INTEGRATOR_FIXED = 0,   /* the reference: fixed-step RK4, h = u.h_step */
+    SGX_INTEGRATOR_ADAPTIVE = 1 /* error-controlled RK4 with FSAL third-order estimate (Kerr) */
+} sgx_integrator;
+
+/* Per-render options.  sgx_render_opts_default() gives the reference's
+ * behaviour: FP32, fixed step, every sample, RGBA8 sRGB. */
+typedef struct sgx_render_opts {
+    uint32_t struct_size;    /* sizeof(sgx_render_opts) */
+    uint32_t precision;      /* sgx_precision */
+    uint32_t integrator;     /* sgx_integrator */
+    uint32_t format;         /* sgx_format kept by sgx_capture's default */
+    float tolerance;         /* adaptive: error tolerance (default 1e-6) */
+    float h_init_frac;       /* adaptive: first step = h_init_frac * r_camera (default 0.02) */
+    float h_max_frac;        /* adaptive: step ceiling = h_max_frac * r (default 0.1) */
+    float fp64_zone;         /* mixed: FP64 control band half-width in M (default 0.05) */
+    uint32_t sample_begin;   /* first Halton sample of this pass (default 0) */
+    uint32_t sample_count;   /* samples in this pass; 0 = all remaining (default 0) */
+    uint32_t block_threads;  /* launch shape: threads per block; 0 = tuned default */
+    uint32_t blocks_per_sm;  /* launch shape: resident blocks per SM; 0 = occupancy limit */
+    uint32_t refill_interval;/* steps between warp refills of finished rays; 0 = tuned */
+    uint32_t rhs_form;       /* Kerr right-hand side: 0 = shared-reciprocal form (default),
+                                1 = the reference's division-for-division form */
+    uint32_t reserved[2];
+} sgx_render_opts;
+
+/* Counters of the last render (summed over its passes). */
+typedef struct sgx_render_stats {
+    uint64_t rays;        /* camera samples traced */
+    uint64_t steps;       /* integrator steps taken (accepted + rejected) */
+    uint64_t rejected;    /* adaptive: rejected attempts */
+    uint64_t zone_steps;  /* mixed: steps taken with FP64 control */
+    uint64_t budget_hits; /* rays that exhausted max_steps */
+    float trace_ms;       /* device time of the trace kernel(s) of the last pass */
+    float total_ms;       /* device time of the last pass, all kernels */
+} sgx_render_stats;
+
+/* The reference's Scene (render_backend.hpp:46-82), as C. */
+typedef struct sgx_scene {
+    uint32_t metric; /* SGX_METRIC_* */
+    float mass_solar;
+    float spin_a_over_M;
+    float disc_inner_M;
+    float disc_outer_M;
+    uint32_t disc_doppler_on;
+    uint32_t disc_redshift_on;
+    uint32_t disc_texture_on;
+    uint32_t show_overlay;
+    uint32_t render_supersample;
+    float exposure;
+    float bloom_threshold;
+    float bloom_strength;
+    float disc_turbulence;
+    float disc_peak_T_K;
+    uint32_t max_steps;
+    float h_step;
+    uint32_t adaptive_step_on;
+} sgx_scene;
+
+/* The reference's CameraState (render_backend.hpp:84-99). */
+typedef struct sgx_camera {
+    float position[3];
+    float basis[9]; /* row-major rows: right, up, -forward */
+    float fov_y_radians;
+} sgx_camera;
+
+/* The reference's SceneConfig (core/include/scene/scene_config.hpp:39-58). */
+typedef struct sgx_scene_config {
+    float mass;
+    float spin;
+    float disc_r_inner;
+    float disc_r_outer;
+    uint32_t disc_doppler_on;
+    uint32_t disc_redshift_on;
+    float camera_fov_deg;
+    float camera_distance;
+    float camera_elevation;
+    float h_step;
+    int32_t max_steps;
+} sgx_scene_config;
+
+/* SceneLoadStatus (scene_config.hpp:60-65). */
+typedef enum sgx_scene_status {
+    SGX_SCENE_OK = 0,
+    SGX_SCENE_FILE_NOT_FOUND = 1,
+    SGX_SCENE_PARSE_ERROR = 2,
+    SGX_SCENE_UNKNOWN_KEY = 3
+} sgx_scene_status;
+
+typedef struct sgx_context sgx_context;
+
+/* ---- library ---------------------------------------------------------- */
+int sgx_abi_version(void);
+const char* sgx_status_string(sgx_status s);
+void sgx_render_opts_default(sgx_render_opts* opts);
+
+/* ---- host helpers (no GPU needed) ------------------------------------- */
+/* Scene{} defaults (render_backend.hpp:46-82). */
+void sgx_scene_default(sgx_scene* out);
+/* build_orbital_camera (cuda_cli/main.cpp:68-109). */
+void sgx_build_orbital_camera(sgx_camera* cam, float distance_M, float elevation_rad, float azimuth_rad,
+                              float fov_y_deg);
+/* pack_uniforms_cuda (render/cuda/cuda_backend.cu:45-101). */
+void sgx_pack_uniforms(const sgx_scene* scene, const sgx_camera* cam, uint32_t width, uint32_t height,
+                       float time_sec, sgx_uniforms* out);
+/* SceneConfig defaults and load_scene_config_from_file / _from_stream
+ * (scene_config.hpp:134-199).  On failure *line gets the 1-based line and
+ * errbuf the offending line (or key, or path), as SceneLoadResult does. */
+void sgx_scene_config_default(sgx_scene_config* out);
+sgx_scene_status sgx_scene_config_load_file(const char* path, sgx_scene_config* out, int* line, char* errbuf,
+                                            size_t errbuf_len);
+sgx_scene_status sgx_scene_config_load_string(const char* text, sgx_scene_config* out, int* line,
+                                              char* errbuf, size_t errbuf_len);
+/* kerr_isco_prograde (core/include/physics/kerr.hpp:97-121). */
+float sgx_kerr_isco_prograde(float mass, float spin);
+
+/* ---- context: CudaBackend lifecycle ----------------------------------- */
+/* CudaBackend() + the device it runs on.  device < 0 -> the current device. */
+sgx_status sgx_create(int device, sgx_context** out);
+/* ~CudaBackend / shutdown() (cuda_backend.cu:107-127). */
+void sgx_destroy(sgx_context* ctx);
+/* initialize(RenderConfig) / resize() (cuda_backend.cu:111-138): sizes the
+ * context's device image.  Rendering at another size resizes implicitly. */
+sgx_status sgx_resize(sgx_context* ctx, uint32_t width, uint32_t height);
+/* render_frame (cuda_backend.cu:140-152): traces u into the context's image.
+ * opts may be NULL (reference behaviour).  With opts->sample_count set, one
+ * call renders one progressive pass [sample_begin, sample_begin+count); the
+ * image is final after the pass that reaches u->supersample. */
+sgx_status sgx_render(sgx_context* ctx, const sgx_uniforms* u, const sgx_render_opts* opts);
+/* capture_frame (cuda_backend.cu:154-166): copies the last image to host
+ * memory in `format`; bytes must be width*height*(4 | 16 | 8). */
+sgx_status sgx_capture(sgx_context* ctx, void* host_out, size_t bytes, uint32_t format);
+/* Counters of the last sgx_render. */
+sgx_status sgx_get_stats(const sgx_context* ctx, sgx_render_stats* out);
+/* Message of the last failed call on ctx (never NULL). */
+const char* sgx_last_error(const sgx_context* ctx);
+
+/* Kernel-level entry: the work of singularity_geodesic_kernel<<<>>>
+ * (geodesic_kernel.cu:462) into a caller-owned device buffer d_out (format as
+ * given), on the caller's cudaStream_t (passed as void*; NULL = the context's
+ * stream).  Scratch memory comes from the context. */
+sgx_status sgx_render_device(sgx_context* ctx, const sgx_uniforms* u, const sgx_render_opts* opts, void* d_out,
+                             uint32_t format, void* stream);
+
+/* Parity probe: trace n individual samples (pixel gx, gy, Halton index s) and
+ * return their HDR colour (before exposure and tone map), integrator steps and
+ * termination kind (0 horizon, 1 escape, 2 disc, 3 budget, 4 cold disc,
+ * 5 no root) — the per-sample values of geodesic_kernel.cu:483-501.  Host
+ * arrays; any output may be NULL. */
+sgx_status sgx_trace_samples(sgx_context* ctx, const sgx_uniforms* u, const sgx_render_opts* opts, uint64_t n,
+                             const uint32_t* gx, const uint32_t* gy, const uint32_t* s, float* hdr3,
+                             uint32_t* steps, uint32_t* term);
+
+/* ---- measurement --------------------------------------------------------- */
+/* No counterpart in the reference: the device's FP32 FMA issue ceiling in
+ * TFLOP/s (2 flops per FMA), measured with a register-resident FMA kernel of
+ * `iters` iterations on `device` (< 0: current).  The roofline denominator of
+ * the tracer, whose work is FP32 SIMT arithmetic. */
+sgx_status sgx_measure_fp32_peak(int device, int iters, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SGX_H */

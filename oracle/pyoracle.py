@@ -1,0 +1,179 @@
+"""TEST INFRASTRUCTURE — ctypes front end of the CPU oracle.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg import
+this module, and only as the checker.  It loads:
+
+* ``oracle/_build/liboracle.so`` — the restatement (geodesic_oracle.hpp,
+  adaptive_oracle.hpp), built by ``make -C oracle``;
+* ``oracle/_ref/libref_host.so`` — the reference's own kernel source compiled
+  for the host CPU (``make -C oracle ref``), present only where the reference
+  tree is.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "liboracle.so"
+REF_LIB = HERE / "_ref" / "libref_host.so"
+REFERENCE_ROOT = Path(os.environ.get("SGX_REFERENCE_ROOT", "/root/reference"))
+
+
+class AdaptiveOpts(C.Structure):
+    _fields_ = [("tol", C.c_float), ("h_init_frac", C.c_float), ("h_max_frac", C.c_float), ("zone", C.c_float),
+                ("max_steps", C.c_uint32), ("mixed", C.c_uint32), ("kahan", C.c_uint32), ("pad", C.c_uint32)]
+
+
+class RayDiag(C.Structure):
+    _fields_ = [("E", C.c_double), ("L", C.c_double), ("Q0", C.c_double), ("Q_end", C.c_double),
+                ("H2_end", C.c_double), ("norm_Q", C.c_double), ("accepted", C.c_uint32),
+                ("rejected", C.c_uint32), ("zone_steps", C.c_uint32), ("pad", C.c_uint32)]
+
+
+def build(ref: bool = True) -> None:
+    """Compile the oracle (and the reference host build when its sources exist)."""
+    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    if ref and (REFERENCE_ROOT / "render" / "cuda" / "kernels" / "geodesic_kernel.cu").exists():
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REFERENCE_ROOT={REFERENCE_ROOT}"], check=True)
+
+
+_lib = None
+_ref = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            build(ref=False)
+        _lib = C.CDLL(str(LIB))
+    return _lib
+
+
+def ref_available() -> bool:
+    return REF_LIB.exists()
+
+
+def ref_lib() -> C.CDLL:
+    global _ref
+    if _ref is None:
+        _ref = C.CDLL(str(REF_LIB))
+    return _ref
+
+
+def _p(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _u(u) -> C.c_void_p:
+    return C.cast(C.pointer(u), C.c_void_p)
+
+
+def default_threads() -> int:
+    return os.cpu_count() or 1
+
+
+def render(u, precision: str = "f32", pixels: np.ndarray | None = None, threads: int | None = None,
+           adaptive: AdaptiveOpts | None = None):
+    """RGBA8 image (or the listed pixels) and the LDR mean, as the reference kernel computes them."""
+    threads = threads or default_threads()
+    npix = u.width * u.height if pixels is None else len(pixels)
+    rgba = np.zeros((npix, 4), dtype=np.uint8)
+    dt = np.float32 if precision == "f32" else np.float64
+    ldr = np.zeros((npix, 3), dtype=dt)
+    pix = None if pixels is None else np.ascontiguousarray(pixels, dtype=np.uint32)
+    L = lib()
+    if adaptive is None:
+        fn = L.oracle_render_f32 if precision == "f32" else L.oracle_render_f64
+        rc = fn(_u(u), C.c_int64(npix), _p(pix), _p(rgba), _p(ldr), C.c_int(threads))
+    else:
+        fn = L.oracle_render_adaptive_f32 if precision == "f32" else L.oracle_render_adaptive_f64
+        rc = fn(_u(u), C.byref(adaptive), C.c_int64(npix), _p(pix), _p(rgba), _p(ldr), C.c_int(threads))
+    if rc != 0:
+        raise RuntimeError(f"oracle render failed ({rc})")
+    if pixels is None:
+        return rgba.reshape(u.height, u.width, 4), ldr.reshape(u.height, u.width, 3)
+    return rgba, ldr
+
+
+def trace(u, gx, gy, s, precision: str = "f32", threads: int | None = None, adaptive: AdaptiveOpts | None = None,
+          diag: bool = False):
+    """Per-sample HDR colour, steps and termination kind."""
+    threads = threads or default_threads()
+    gx = np.ascontiguousarray(gx, dtype=np.uint32)
+    gy = np.ascontiguousarray(gy, dtype=np.uint32)
+    s = np.ascontiguousarray(s, dtype=np.uint32)
+    n = gx.size
+    dt = np.float32 if precision == "f32" else np.float64
+    hdr = np.zeros((n, 3), dtype=dt)
+    steps = np.zeros(n, dtype=np.uint32)
+    term = np.zeros(n, dtype=np.uint32)
+    L = lib()
+    if adaptive is None:
+        fn = L.oracle_trace_f32 if precision == "f32" else L.oracle_trace_f64
+        rc = fn(_u(u), C.c_int64(n), _p(gx), _p(gy), _p(s), _p(hdr), _p(steps), _p(term), C.c_int(threads))
+        d = None
+    else:
+        d = (RayDiag * n)() if diag else None
+        fn = L.oracle_trace_adaptive_f32 if precision == "f32" else L.oracle_trace_adaptive_f64
+        rc = fn(_u(u), C.byref(adaptive), C.c_int64(n), _p(gx), _p(gy), _p(s), _p(hdr), _p(steps), _p(term),
+                d, C.c_int(threads))
+    if rc != 0:
+        raise RuntimeError(f"oracle trace failed ({rc})")
+    if diag:
+        return hdr, steps, term, d
+    return hdr, steps, term
+
+
+def count_ops(u, gx, gy, s, adaptive: AdaptiveOpts | None = None):
+    """Per-sample algorithmic FP32 operation counts of the reference formulas."""
+    gx = np.ascontiguousarray(gx, dtype=np.uint32)
+    gy = np.ascontiguousarray(gy, dtype=np.uint32)
+    s = np.ascontiguousarray(s, dtype=np.uint32)
+    n = gx.size
+    ops = np.zeros(n, dtype=np.uint64)
+    steps = np.zeros(n, dtype=np.uint32)
+    term = np.zeros(n, dtype=np.uint32)
+    rc = lib().oracle_count_ops(_u(u), C.c_int64(n), _p(gx), _p(gy), _p(s), _p(ops), _p(steps), _p(term),
+                                C.byref(adaptive) if adaptive is not None else None)
+    if rc != 0:
+        raise RuntimeError("oracle count failed")
+    return ops, steps, term
+
+
+# ---- the reference itself, compiled for the host (present only here) ----
+def ref_render(u, threads: int | None = None) -> np.ndarray:
+    threads = threads or default_threads()
+    out = np.zeros((u.height, u.width, 4), dtype=np.uint8)
+    ref_lib().ref_render_rgba8(_u(u), _p(out), C.c_int(threads))
+    return out
+
+
+def ref_trace(u, gx, gy, s, threads: int | None = None) -> np.ndarray:
+    threads = threads or default_threads()
+    gx = np.ascontiguousarray(gx, dtype=np.uint32)
+    gy = np.ascontiguousarray(gy, dtype=np.uint32)
+    s = np.ascontiguousarray(s, dtype=np.uint32)
+    hdr = np.zeros((gx.size, 3), dtype=np.float32)
+    ref_lib().ref_trace_hdr(_u(u), C.c_int64(gx.size), _p(gx), _p(gy), _p(s), _p(hdr), C.c_int(threads))
+    return hdr
+
+
+def ref_orbital_camera(distance, elevation, azimuth, fov_deg) -> np.ndarray:
+    out = np.zeros(13, dtype=np.float32)
+    ref_lib().ref_build_orbital_camera(C.c_float(distance), C.c_float(elevation), C.c_float(azimuth),
+                                       C.c_float(fov_deg), _p(out))
+    return out
+
+
+def ref_load_scene_text(text: str):
+    out = np.zeros(11, dtype=np.float32)
+    line = C.c_int(0)
+    st = ref_lib().ref_load_scene_text(text.encode(), _p(out), C.byref(line))
+    return st, out, line.value

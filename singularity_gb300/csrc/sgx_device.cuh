@@ -1,0 +1,609 @@
+// singularity_gb300/csrc/sgx_device.cuh
+//
+// Device-side physics of the tracer, templated on the arithmetic type T
+// (float for the FP32 and mixed forms, double for the FP64 form).
+//
+// The formulas are the reference's (cited per function); the structure is
+// this library's own:
+//   * everything that depends only on the view (camera spherical position and
+//     its orthonormal frame, the Kerr metric at the camera, horizon radius,
+//     f(r_cam)) is evaluated once per view by `make_view` instead of once per
+//     sample, with the same float expressions, so the values are the ones the
+//     reference recomputes for every sample;
+//   * the per-ray state is the minimum the output depends on: the reference
+//     also integrates t, which nothing reads, so it is dropped;
+//   * the Kerr right-hand side comes in two algebraically equal forms: REF
+//     keeps the reference's fourteen IEEE divisions (kerr_hamilton.h:97-155);
+//     FAST shares three reciprocals 1/Sigma, 1/Delta, 1/sin^2 and folds the
+//     per-ray products E^2, 4MaEL, a^2 L^2 into constants.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "sgx_uniforms.h"
+
+namespace sgxd {
+
+// ---------------------------------------------------------------------------
+// Scalar traits
+// ---------------------------------------------------------------------------
+template <class T> struct DM;
+template <> struct DM<float> {
+    static __device__ __forceinline__ float lit(float f, double) { return f; }
+    static __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
+    static __device__ __forceinline__ float sin_(float x) { return sinf(x); }
+    static __device__ __forceinline__ float cos_(float x) { return cosf(x); }
+    static __device__ __forceinline__ void sincos_(float x, float* s, float* c) { sincosf(x, s, c); }
+    static __device__ __forceinline__ float acos_(float x) { return acosf(x); }
+    static __device__ __forceinline__ float atan2_(float y, float x) { return atan2f(y, x); }
+    static __device__ __forceinline__ float pow_(float x, float y) { return powf(x, y); }
+    static __device__ __forceinline__ float log_(float x) { return logf(x); }
+    static __device__ __forceinline__ float fmin_(float a, float b) { return fminf(a, b); }
+    static __device__ __forceinline__ float fmax_(float a, float b) { return fmaxf(a, b); }
+    static __device__ __forceinline__ float rcp_(float x) { return 1.0f / x; }
+};
+template <> struct DM<double> {
+    static __device__ __forceinline__ double lit(float, double d) { return d; }
+    static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
+    static __device__ __forceinline__ double sin_(double x) { return sin(x); }
+    static __device__ __forceinline__ double cos_(double x) { return cos(x); }
+    static __device__ __forceinline__ void sincos_(double x, double* s, double* c) { sincos(x, s, c); }
+    static __device__ __forceinline__ double acos_(double x) { return acos(x); }
+    static __device__ __forceinline__ double atan2_(double y, double x) { return atan2(y, x); }
+    static __device__ __forceinline__ double pow_(double x, double y) { return pow(x, y); }
+    static __device__ __forceinline__ double log_(double x) { return log(x); }
+    static __device__ __forceinline__ double fmin_(double a, double b) { return fmin(a, b); }
+    static __device__ __forceinline__ double fmax_(double a, double b) { return fmax(a, b); }
+    static __device__ __forceinline__ double rcp_(double x) { return 1.0 / x; }
+};
+
+#define DLIT(x) (::sgxd::DM<T>::lit(x##f, x))
+
+template <class T> __device__ __forceinline__ T clampv(T x, T lo, T hi) {
+    return DM<T>::fmin_(DM<T>::fmax_(x, lo), hi);
+}
+
+template <class T> struct V3 {
+    T x, y, z;
+};
+template <class T> __device__ __forceinline__ V3<T> mk3(T x, T y, T z) { return V3<T>{x, y, z}; }
+template <class T> __device__ __forceinline__ T dot3(V3<T> a, V3<T> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+// How a ray ended (diagnostic; the image only sees the colour).
+enum : std::uint32_t {
+    TERM_HORIZON = 0,
+    TERM_ESCAPE = 1,
+    TERM_DISC = 2,
+    TERM_BUDGET = 3,
+    TERM_DISC_COLD = 4,
+    TERM_NO_ROOT = 5,
+};
+
+// ---------------------------------------------------------------------------
+// Per-view constants
+// ---------------------------------------------------------------------------
+template <class T> struct View {
+    // camera frame (build_camera_ray_subpixel, geodesic_kernel.cu:188-223)
+    V3<T> fwd, right, up;
+    V3<T> rhat, that, phat;
+    T aspect, tan_half_fov, width_f, height_f;
+    T cam_r, cam_theta, cam_phi, sin_th, cos_th;
+    T uphi_den;  // cam_r * max(sin_th, 1e-6)
+    // scene
+    T M, a, a2, rs, r_in, r_out, peak_T, h, escape_r, time_sec, exposure, turbulence;
+    T hcut;   // capture radius: 1.02 r_+ (Kerr) or u.horizon_cut (Schwarzschild)
+    T f_cam;  // Schwarzschild 1 - rs/r_cam
+    T f_obs;  // Kerr shading 1 - 2M/r_cam
+    // Kerr metric at the camera (geodesic_kernel.cu:310-319)
+    T g_tt, g_tp, g_rr, g_thth, g_pp, s2_c;
+    std::uint32_t width, height, flags, max_steps, spp, metric;
+};
+
+template <class T> __device__ inline View<T> make_view(const sgx_uniforms& u) {
+    View<T> v;
+    v.fwd = mk3(T(u.cam_fwd.x), T(u.cam_fwd.y), T(u.cam_fwd.z));
+    v.right = mk3(T(u.cam_right.x), T(u.cam_right.y), T(u.cam_right.z));
+    v.up = mk3(T(u.cam_up.x), T(u.cam_up.y), T(u.cam_up.z));
+    v.aspect = T(u.aspect);
+    v.tan_half_fov = T(u.tan_half_fov);
+    v.width_f = T(float(u.width));
+    v.height_f = T(float(u.height));
+    const V3<T> p = mk3(T(u.cam_pos.x), T(u.cam_pos.y), T(u.cam_pos.z));
+    v.cam_r = DM<T>::sqrt_(dot3(p, p));
+    v.cam_theta = DM<T>::acos_(clampv(p.z / DM<T>::fmax_(v.cam_r, DLIT(1e-6)), DLIT(-1.0), DLIT(1.0)));
+    v.cam_phi = DM<T>::atan2_(p.y, p.x);
+    v.sin_th = DM<T>::sin_(v.cam_theta);
+    v.cos_th = DM<T>::cos_(v.cam_theta);
+    const T cos_phi = DM<T>::cos_(v.cam_phi);
+    const T sin_phi = DM<T>::sin_(v.cam_phi);
+    v.rhat = mk3(v.sin_th * cos_phi, v.sin_th * sin_phi, v.cos_th);
+    v.that = mk3(v.cos_th * cos_phi, v.cos_th * sin_phi, -v.sin_th);
+    v.phat = mk3(-sin_phi, cos_phi, DLIT(0.0));
+    v.uphi_den = v.cam_r * DM<T>::fmax_(v.sin_th, DLIT(1e-6));
+
+    v.M = T(u.mass_M);
+    v.a = T(u.spin_a);
+    v.a2 = v.a * v.a;
+    v.rs = T(u.rs);
+    v.r_in = T(u.disc_r_inner);
+    v.r_out = T(u.disc_r_outer);
+    v.peak_T = T(u.disc_peak_T);
+    v.h = T(u.h_step);
+    v.escape_r = T(u.escape_r);
+    v.time_sec = T(u.time_sec);
+    v.exposure = T(u.exposure);
+    v.turbulence = T(u.disc_turbulence);
+    v.width = u.width;
+    v.height = u.height;
+    v.flags = u.flags;
+    v.max_steps = u.max_steps;
+    v.spp = u.supersample < 1u ? 1u : (u.supersample > 1024u ? 1024u : u.supersample);
+    v.metric = u.metric_type;
+
+    v.f_cam = DLIT(1.0) - v.rs / v.cam_r;
+    v.f_obs = DLIT(1.0) - DLIT(2.0) * v.M / v.cam_r;
+    const T r = v.cam_r, a = v.a, Mm = v.M;
+    const T Sigma_c = r * r + a * a * v.cos_th * v.cos_th;
+    const T Delta_c = r * r - DLIT(2.0) * Mm * r + a * a;
+    v.s2_c = v.sin_th * v.sin_th;
+    v.g_tt = -(DLIT(1.0) - DLIT(2.0) * Mm * r / Sigma_c);
+    v.g_tp = DLIT(-2.0) * Mm * r * a * v.s2_c / Sigma_c;
+    v.g_rr = Sigma_c / Delta_c;
+    v.g_thth = Sigma_c;
+    v.g_pp = v.s2_c * ((r * r + a * a) * (r * r + a * a) - a * a * Delta_c * v.s2_c) / Sigma_c;
+    if (v.metric == SGX_METRIC_KERR) {
+        v.hcut = DLIT(1.02) * (Mm + DM<T>::sqrt_(DM<T>::fmax_(Mm * Mm - a * a, DLIT(0.0))));
+    } else {
+        v.hcut = T(u.horizon_cut);
+    }
+    return v;
+}
+
+// ---------------------------------------------------------------------------
+// Camera sample (geodesic_kernel.cu:188-223, 442-451, 483-501)
+// ---------------------------------------------------------------------------
+template <class T> __device__ __forceinline__ T halton(std::uint32_t i, std::uint32_t base) {
+    T f = DLIT(1.0);
+    T r = DLIT(0.0);
+    const T b = T(float(base));
+    while (i > 0u) {
+        f = f / b;
+        r = r + f * T(float(i % base));
+        i /= base;
+    }
+    return r;
+}
+
+template <class T> struct CamDir {
+    T ur, utheta, uphi;
+};
+
+template <class T>
+__device__ __forceinline__ CamDir<T> camera_dir(const View<T>& v, std::uint32_t gx, std::uint32_t gy,
+                                                std::uint32_t s) {
+    T ox, oy;
+    if (v.spp == 1u) {
+        ox = DLIT(0.5);
+        oy = DLIT(0.5);
+    } else {
+        ox = halton<T>(s + 1u, 2u);
+        oy = halton<T>(s + 1u, 3u);
+    }
+    const T fx = T(float(gx)) + ox;
+    const T fy = T(float(gy)) + oy;
+    const T u_ndc = (DLIT(2.0) * fx / v.width_f - DLIT(1.0)) * v.aspect * v.tan_half_fov;
+    const T v_ndc = -(DLIT(2.0) * fy / v.height_f - DLIT(1.0)) * v.tan_half_fov;
+    V3<T> d = mk3(v.fwd.x + (v.right.x * u_ndc + v.up.x * v_ndc), v.fwd.y + (v.right.y * u_ndc + v.up.y * v_ndc),
+                  v.fwd.z + (v.right.z * u_ndc + v.up.z * v_ndc));
+    const T len = DM<T>::fmax_(DM<T>::sqrt_(dot3(d, d)), DLIT(1e-20));
+    const T ik = DLIT(1.0) / len;
+    d = mk3(d.x * ik, d.y * ik, d.z * ik);
+    CamDir<T> c;
+    c.ur = dot3(d, v.rhat);
+    c.utheta = dot3(d, v.that) / v.cam_r;
+    c.uphi = dot3(d, v.phat) / v.uphi_den;
+    return c;
+}
+
+// ---------------------------------------------------------------------------
+// Shading (geodesic_kernel.cu:77-171), evaluated once per terminated ray.
+// ---------------------------------------------------------------------------
+template <class T> __device__ inline V3<T> blackbody_srgb(T temp) {
+    temp = clampv(temp, DLIT(1000.0), DLIT(40000.0)) * DLIT(0.01);
+    T r, g, b;
+    if (temp <= DLIT(66.0)) {
+        r = DLIT(1.0);
+        g = clampv(DLIT(0.39008157876901960784) * DM<T>::log_(temp) - DLIT(0.63184144378862745098), DLIT(0.0),
+                   DLIT(1.0));
+    } else {
+        const T t1 = temp - DLIT(60.0);
+        r = clampv(DLIT(1.29293618606274509804) * DM<T>::pow_(t1, DLIT(-0.1332047592)), DLIT(0.0), DLIT(1.0));
+        g = clampv(DLIT(1.12989086089529411765) * DM<T>::pow_(t1, DLIT(-0.0755148492)), DLIT(0.0), DLIT(1.0));
+    }
+    if (temp >= DLIT(66.0)) {
+        b = DLIT(1.0);
+    } else if (temp <= DLIT(19.0)) {
+        b = DLIT(0.0);
+    } else {
+        const T t1 = temp - DLIT(10.0);
+        b = clampv(DLIT(0.54320678911019607843) * DM<T>::log_(t1) - DLIT(1.19625408914), DLIT(0.0), DLIT(1.0));
+    }
+    return mk3(r, g, b);
+}
+
+template <class T> __device__ __forceinline__ T disc_temperature(T r_cross, T r_inner, T peak_T) {
+    if (r_cross < r_inner) return DLIT(0.0);
+    const T ratio = r_inner / r_cross;
+    const T q = DM<T>::pow_(ratio, DLIT(0.75));
+    const T edge = DLIT(1.0) - DM<T>::sqrt_(ratio);
+    const T raw = q * DM<T>::fmax_(edge, DLIT(0.0));
+    return peak_T * raw / DLIT(0.186);
+}
+
+template <class T> __device__ inline T disc_band_mask(T r_cross, T phi_cross, T r_inner, T turbulence, T time_sec) {
+    const T rho = DM<T>::log_(DM<T>::fmax_(r_cross / r_inner, DLIT(0.1)));
+    const T shear = DLIT(4.0) / DM<T>::fmax_(DM<T>::pow_(r_cross / r_inner, DLIT(1.5)), DLIT(0.25));
+    const T omega = DM<T>::pow_(DM<T>::fmax_(r_cross / r_inner, DLIT(0.1)), DLIT(-1.5));
+    const T phi_anim = phi_cross - DLIT(0.8) * time_sec * omega;
+    const T band1 = DLIT(0.5) + DLIT(0.5) * DM<T>::cos_(DLIT(10.0) * rho + DLIT(3.0) * phi_anim + shear);
+    const T band2 = DLIT(0.5) + DLIT(0.5) * DM<T>::cos_(DLIT(22.0) * rho - DLIT(1.7) * phi_anim);
+    const T combined = DLIT(0.8) + turbulence * (band1 * band1 * band2 - DLIT(0.8));
+    return clampv(DLIT(0.65) + DLIT(0.55) * combined, DLIT(0.0), DLIT(1.3));
+}
+
+__device__ __forceinline__ std::uint32_t star_hash(std::uint32_t ix, std::uint32_t iy) {
+    std::uint32_t x = ix * 0x9E3779B9u + iy;
+    x ^= x << 13;
+    x ^= x >> 17;
+    x ^= x << 5;
+    return x;
+}
+
+// Sky colour for an escaped ray at (theta, phi): the starfield of
+// geodesic_kernel.cu:135-171 applied to the direction at the last state.
+template <class T> __device__ inline V3<T> sky_color(T theta, T phi) {
+    const T st = DM<T>::sin_(theta), ct = DM<T>::cos_(theta);
+    const V3<T> dir = mk3(st * DM<T>::cos_(phi), st * DM<T>::sin_(phi), ct);
+    const T len = DM<T>::sqrt_(dot3(dir, dir));
+    if (len < DLIT(1e-6)) return mk3(DLIT(0.0), DLIT(0.0), DLIT(0.005));
+    const T ik = DLIT(1.0) / len;
+    const V3<T> n = mk3(dir.x * ik, dir.y * ik, dir.z * ik);
+    const T pi = DLIT(3.14159265358979323846);
+    const T th = DM<T>::acos_(clampv(n.z, DLIT(-1.0), DLIT(1.0)));
+    const T ph = DM<T>::atan2_(n.y, n.x) + pi;
+    int ix = int(ph / (DLIT(2.0) * pi) * T(768.0f)) % 768;
+    int iy = int(th / pi * T(384.0f)) % 384;
+    if (ix < 0) ix += 768;
+    if (iy < 0) iy += 384;
+    const std::uint32_t seed = star_hash(std::uint32_t(ix), std::uint32_t(iy));
+    T r = DLIT(0.0015), g = DLIT(0.002), b = DLIT(0.005);
+    if ((seed & 0xFFu) < 4u) {
+        const T bright_raw = T(float((seed >> 8) & 0xFFu)) / DLIT(255.0);
+        const T brightness = DM<T>::pow_(bright_raw, DLIT(4.0));
+        const T hue = T(float((seed >> 16) & 0xFFu)) / DLIT(255.0);
+        const T star_r = DLIT(1.0) - DLIT(0.5) * hue;
+        const T star_g = DLIT(0.8) + DLIT(0.2) * hue * (DLIT(1.0) - hue) * DLIT(4.0);
+        const T star_b = DLIT(0.4) + DLIT(0.6) * hue;
+        r = DM<T>::fmin_(DLIT(1.0), r + brightness * star_r);
+        g = DM<T>::fmin_(DLIT(1.0), g + brightness * star_g);
+        b = DM<T>::fmin_(DLIT(1.0), b + brightness * star_b);
+    }
+    return mk3(r * DLIT(0.6), g * DLIT(0.6), b * DLIT(0.6));
+}
+
+template <class T>
+__device__ __forceinline__ V3<T> disc_shade(const View<T>& v, T r_cross, T phi_cross, T T_local, T g) {
+    const V3<T> col = blackbody_srgb(g * T_local);
+    const T flux = clampv(DM<T>::pow_(v.r_in / r_cross, DLIT(3.0)), DLIT(0.05), DLIT(1.5));
+    const T bands = disc_band_mask(r_cross, phi_cross, v.r_in, v.turbulence, v.time_sec);
+    const T g2 = g * g;
+    const T k = flux * bands * g2 * g2;
+    return mk3(col.x * k, col.y * k, col.z * k);
+}
+
+// Kerr disc colour (geodesic_kernel.cu:368-393).
+template <class T> __device__ inline V3<T> kerr_disc(const View<T>& v, T L, T r_cross, T phi_cross, T T_local) {
+    const T f_emit = DLIT(1.0) - DLIT(2.0) * v.M / r_cross;
+    const T g_grav = (v.flags & SGX_FLAG_REDSHIFT_ON)
+                         ? DM<T>::sqrt_(DM<T>::fmax_(f_emit, DLIT(1e-6)) / DM<T>::fmax_(v.f_obs, DLIT(1e-6)))
+                         : DLIT(1.0);
+    T g_dop = DLIT(1.0);
+    if (v.flags & SGX_FLAG_DOPPLER_ON) {
+        const T om0 = DM<T>::sqrt_(v.M / (r_cross * r_cross * r_cross));
+        const T omega_K = om0 / (DLIT(1.0) + v.a * om0);
+        const T vel = r_cross * omega_K / DM<T>::sqrt_(DM<T>::fmax_(f_emit, DLIT(1e-6)));
+        const T cos_psi = clampv(L / r_cross, DLIT(-1.0), DLIT(1.0));
+        g_dop = DM<T>::sqrt_(DM<T>::fmax_(DLIT(1.0) - vel * vel, DLIT(0.0)))
+                / DM<T>::fmax_(DLIT(1.0) - vel * cos_psi, DLIT(1e-4));
+    }
+    return disc_shade(v, r_cross, phi_cross, T_local, g_grav * g_dop);
+}
+
+// Schwarzschild disc colour (geodesic_kernel.cu:266-287).
+template <class T> __device__ inline V3<T> schw_disc(const View<T>& v, T uphi_cross, T r_cross, T phi, T T_local) {
+    const T f_emit = DLIT(1.0) - v.rs / r_cross;
+    const T g_grav = (v.flags & SGX_FLAG_REDSHIFT_ON) ? DM<T>::sqrt_(DM<T>::fmax_(f_emit / v.f_cam, DLIT(0.0)))
+                                                      : DLIT(1.0);
+    T g_dop = DLIT(1.0);
+    if (v.flags & SGX_FLAG_DOPPLER_ON) {
+        const T omega = DM<T>::sqrt_(v.M / (r_cross * r_cross * r_cross));
+        const T vel = r_cross * omega / DM<T>::sqrt_(DM<T>::fmax_(f_emit, DLIT(1e-6)));
+        const T cos_psi = clampv(-uphi_cross * r_cross, DLIT(-1.0), DLIT(1.0));
+        g_dop = DM<T>::sqrt_(DM<T>::fmax_(DLIT(1.0) - vel * vel, DLIT(0.0)))
+                / DM<T>::fmax_(DLIT(1.0) - vel * cos_psi, DLIT(1e-4));
+    }
+    return disc_shade(v, r_cross, phi, T_local, g_grav * g_dop);
+}
+
+// ACES (Narkowicz) of hdr * exposure (geodesic_kernel.cu:413-422).
+template <class T> __device__ __forceinline__ T aces1(T x) {
+    return clampv((x * (DLIT(2.51) * x + DLIT(0.03))) / (x * (DLIT(2.43) * x + DLIT(0.59)) + DLIT(0.14)), DLIT(0.0),
+                  DLIT(1.0));
+}
+
+__device__ __forceinline__ float linear_to_srgb(float c) {
+    c = fminf(fmaxf(c, 0.0f), 1.0f);
+    return c <= 0.0031308f ? 12.92f * c : 1.055f * powf(c, 1.0f / 2.4f) - 0.055f;
+}
+__device__ __forceinline__ std::uint8_t to_u8(float c) {
+    return (std::uint8_t)fminf(fmaxf(linear_to_srgb(c) * 255.0f + 0.5f, 0.0f), 255.0f);
+}
+
+// ---------------------------------------------------------------------------
+// Kerr Hamiltonian right-hand side (kerr_hamilton.h:97-155), t dropped.
+// ---------------------------------------------------------------------------
+template <class T> struct KS {
+    T r, th, ph, pr, pth;
+};
+
+// Per-ray constants of motion and the products the FAST form folds.
+template <class T> struct KC {
+    T E, L;
+    T E2, L2, cEL, aL2;  // E^2, L^2, 4 M a E L, a^2 L^2
+    T twoMaE, twoMaL;    // 2 M a E, 2 M a L
+};
+
+template <class T> __device__ __forceinline__ KC<T> make_kc(const View<T>& v, T E, T L) {
+    KC<T> c;
+    c.E = E;
+    c.L = L;
+    c.E2 = E * E;
+    c.L2 = L * L;
+    c.cEL = DLIT(4.0) * v.M * v.a * E * L;
+    c.aL2 = v.a2 * c.L2;
+    c.twoMaE = DLIT(2.0) * v.M * v.a * E;
+    c.twoMaL = DLIT(2.0) * v.M * v.a * L;
+    return c;
+}
+
+// The reference's expression, division for division.
+template <class T> __device__ __forceinline__ KS<T> kerr_rhs_ref(const KS<T>& s, const View<T>& v, const KC<T>& c) {
+    T st, ct;
+    DM<T>::sincos_(s.th, &st, &ct);
+    const T r = s.r;
+    const T s2 = st * st;
+    const T safe_s2 = (s2 < DLIT(1e-10)) ? DLIT(1e-10) : s2;
+    const T c2 = ct * ct;
+    const T r2 = r * r;
+    const T a = v.a, Mm = v.M, a2 = v.a2;
+    const T Sigma = r2 + a2 * c2;
+    const T Delta = r2 - DLIT(2.0) * Mm * r + a2;
+    const T A = (r2 + a2) * (r2 + a2) - a2 * Delta * s2;
+    const T SD = Sigma * Delta;
+    const T E = c.E, L = c.L, L2 = L * L;
+    KS<T> d;
+    d.ph = (DLIT(2.0) * Mm * r * a * E * s2 + (Delta - a2 * s2) * L) / (SD * safe_s2);
+    d.r = Delta * s.pr / Sigma;
+    d.th = s.pth / Sigma;
+    const T B = -A * E * E + DLIT(4.0) * Mm * r * a * E * L - a2 * L2;
+    const T Sig_r = DLIT(2.0) * r;
+    const T Del_r = DLIT(2.0) * r - DLIT(2.0) * Mm;
+    const T A_r = DLIT(4.0) * r * (r2 + a2) - a2 * Del_r * s2;
+    const T B_r = -A_r * E * E + DLIT(4.0) * Mm * a * E * L;
+    const T sin2t = DLIT(2.0) * st * ct;
+    const T Sig_t = -a2 * sin2t;
+    const T B_t = a2 * Delta * sin2t * E * E;
+    const T Sigma2 = Sigma * Sigma;
+    const T Dp2 = Delta * s.pr * s.pr + s.pth * s.pth;
+    const T dH_dr = B_r / SD - B * (Sig_r * Delta + Sigma * Del_r) / (SD * SD) - L2 * Sig_r / (Sigma2 * safe_s2)
+                    + Del_r * s.pr * s.pr / Sigma - Dp2 * Sig_r / Sigma2;
+    const T dH_dth = B_t / SD - B * Sig_t / (Sigma2 * Delta)
+                     - L2 * (Sig_t * safe_s2 + Sigma * sin2t) / (Sigma2 * safe_s2 * safe_s2) - Dp2 * Sig_t / Sigma2;
+    d.pr = DLIT(-0.5) * dH_dr;
+    d.pth = DLIT(-0.5) * dH_dth;
+    return d;
+}
+
+// Same function, three reciprocals and folded constants.
+//   dphi   = (2Mra E s2 + (Delta - a2 s2) L) / (Sigma Delta s2)
+//   dr     = Delta p_r / Sigma,     dth = p_th / Sigma
+//   -2 dp_r  = B_r/(SD) - B (2r Delta + Sigma Del_r)/(SD)^2 - 2r L^2/(Sigma^2 s2)
+//              + Del_r p_r^2 / Sigma - 2r Dp2 / Sigma^2
+//   -2 dp_th = B_t/(SD) - B Sig_t/(Sigma^2 Delta)
+//              - L^2 (Sig_t s2 + Sigma sin2t)/(Sigma^2 s2^2) - Dp2 Sig_t / Sigma^2
+template <class T> __device__ __forceinline__ KS<T> kerr_rhs_fast(const KS<T>& s, const View<T>& v, const KC<T>& c) {
+    T st, ct;
+    DM<T>::sincos_(s.th, &st, &ct);
+    const T r = s.r;
+    const T a2 = v.a2;
+    const T s2 = st * st;
+    const T safe_s2 = DM<T>::fmax_(s2, DLIT(1e-10));
+    const T c2 = ct * ct;
+    const T r2 = r * r;
+    const T r2a2 = r2 + a2;
+    const T Sigma = r2 + a2 * c2;
+    const T Del_r = DLIT(2.0) * (r - v.M);
+    const T Delta = r * (r - DLIT(2.0) * v.M) + a2;
+    const T a2s2 = a2 * s2;
+    const T A = r2a2 * r2a2 - a2s2 * Delta;
+    const T iS = DM<T>::rcp_(Sigma);
+    const T iD = DM<T>::rcp_(Delta);
+    const T is2 = DM<T>::rcp_(safe_s2);
+    const T iSD = iS * iD;
+    const T iS2 = iS * iS;
+    KS<T> d;
+    d.ph = (c.twoMaE * r * s2 + (Delta - a2s2) * c.L) * iSD * is2;
+    d.r = Delta * s.pr * iS;
+    d.th = s.pth * iS;
+    const T B = (c.cEL * r - A * c.E2) - c.aL2;
+    const T A_r = DLIT(4.0) * r * r2a2 - a2s2 * Del_r;
+    const T B_r = c.cEL - A_r * c.E2;
+    const T sin2t = DLIT(2.0) * st * ct;
+    const T Sig_t = -a2 * sin2t;
+    const T pr2 = s.pr * s.pr;
+    const T Dp2 = Delta * pr2 + s.pth * s.pth;
+    const T two_r = DLIT(2.0) * r;
+    const T dH_dr = iSD * (B_r - B * (two_r * Delta + Sigma * Del_r) * iSD) + Del_r * pr2 * iS
+                    - two_r * iS2 * (c.L2 * is2 + Dp2);
+    const T dH_dth = iSD * (a2 * Delta * sin2t * c.E2) - B * Sig_t * iS2 * iD
+                     - iS2 * (c.L2 * is2 * (Sig_t + Sigma * sin2t * is2) + Dp2 * Sig_t);
+    d.pr = DLIT(-0.5) * dH_dr;
+    d.pth = DLIT(-0.5) * dH_dth;
+    return d;
+}
+
+template <class T, bool FAST>
+__device__ __forceinline__ KS<T> kerr_rhs(const KS<T>& s, const View<T>& v, const KC<T>& c) {
+    if constexpr (FAST) return kerr_rhs_fast(s, v, c);
+    else return kerr_rhs_ref(s, v, c);
+}
+
+template <class T> __device__ __forceinline__ KS<T> ks_axpy(const KS<T>& y, const KS<T>& k, T f) {
+    return KS<T>{y.r + k.r * f, y.th + k.th * f, y.ph + k.ph * f, y.pr + k.pr * f, y.pth + k.pth * f};
+}
+
+// Fixed-step RK4 with the reference's near-pole damping (kerr_hamilton.h:165-178).
+template <class T, bool FAST>
+__device__ __forceinline__ KS<T> kerr_rk4(const KS<T>& y, T h, const View<T>& v, const KC<T>& c) {
+    T st = DM<T>::sin_(y.th);
+    st = (st < DLIT(0.0)) ? -st : st;
+    T ps = st * DLIT(5.0);
+    ps = (ps > DLIT(1.0)) ? DLIT(1.0) : ((ps < DLIT(0.05)) ? DLIT(0.05) : ps);
+    h = h * ps;
+    const T hh = DLIT(0.5) * h;
+    const KS<T> k1 = kerr_rhs<T, FAST>(y, v, c);
+    const KS<T> k2 = kerr_rhs<T, FAST>(ks_axpy(y, k1, hh), v, c);
+    const KS<T> k3 = kerr_rhs<T, FAST>(ks_axpy(y, k2, hh), v, c);
+    const KS<T> k4 = kerr_rhs<T, FAST>(ks_axpy(y, k3, h), v, c);
+    const T h6 = h / DLIT(6.0);
+    KS<T> o;
+    o.r = y.r + ((k1.r + k2.r * DLIT(2.0)) + (k3.r * DLIT(2.0) + k4.r)) * h6;
+    o.th = y.th + ((k1.th + k2.th * DLIT(2.0)) + (k3.th * DLIT(2.0) + k4.th)) * h6;
+    o.ph = y.ph + ((k1.ph + k2.ph * DLIT(2.0)) + (k3.ph * DLIT(2.0) + k4.ph)) * h6;
+    o.pr = y.pr + ((k1.pr + k2.pr * DLIT(2.0)) + (k3.pr * DLIT(2.0) + k4.pr)) * h6;
+    o.pth = y.pth + ((k1.pth + k2.pth * DLIT(2.0)) + (k3.pth * DLIT(2.0) + k4.pth)) * h6;
+    return o;
+}
+
+// Initial canonical state from a camera direction (geodesic_kernel.cu:320-344).
+// Returns false when the u^t quadratic has no real root.
+template <class T>
+__device__ __forceinline__ bool kerr_init(const View<T>& v, const CamDir<T>& cd, KS<T>& y, T& E, T& L) {
+    const T A_q = v.g_tt;
+    const T B_q = DLIT(2.0) * v.g_tp * cd.uphi;
+    const T C_q = v.g_rr * cd.ur * cd.ur + v.g_thth * cd.utheta * cd.utheta + v.g_pp * cd.uphi * cd.uphi;
+    const T disc_q = B_q * B_q - DLIT(4.0) * A_q * C_q;
+    if (disc_q < DLIT(0.0)) return false;
+    const T ut = (-B_q - DM<T>::sqrt_(disc_q)) / (DLIT(2.0) * A_q);
+    E = -(v.g_tt * ut + v.g_tp * cd.uphi);
+    L = v.g_tp * ut + v.g_pp * cd.uphi;
+    y.r = v.cam_r;
+    y.th = v.cam_theta;
+    y.ph = v.cam_phi;
+    y.pr = v.g_rr * cd.ur;
+    y.pth = v.g_thth * cd.utheta;
+    return true;
+}
+
+// FP64 constants of motion from the FP32 camera direction (mixed form).
+__device__ __forceinline__ bool kerr_init_fp64_constants(const View<float>& v, const CamDir<float>& cd, double& E,
+                                                         double& L, double& pr, double& pth) {
+    const double Mm = v.M, a = v.a, r = v.cam_r, ct = v.cos_th, st = v.sin_th;
+    const double Sigma = r * r + a * a * ct * ct, Delta = r * r - 2.0 * Mm * r + a * a, s2 = st * st;
+    const double g_tt = -(1.0 - 2.0 * Mm * r / Sigma);
+    const double g_tp = -2.0 * Mm * r * a * s2 / Sigma;
+    const double g_rr = Sigma / Delta, g_thth = Sigma;
+    const double g_pp = s2 * ((r * r + a * a) * (r * r + a * a) - a * a * Delta * s2) / Sigma;
+    const double ur = cd.ur, uth = cd.utheta, uph = cd.uphi;
+    const double B = 2.0 * g_tp * uph, C = g_rr * ur * ur + g_thth * uth * uth + g_pp * uph * uph;
+    const double disc = B * B - 4.0 * g_tt * C;
+    if (disc < 0.0) return false;
+    const double ut = (-B - sqrt(disc)) / (2.0 * g_tt);
+    E = -(g_tt * ut + g_tp * uph);
+    L = g_tp * ut + g_pp * uph;
+    pr = g_rr * ur;
+    pth = g_thth * uth;
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// Schwarzschild (geodesic_math.h:101-134), t dropped.
+// ---------------------------------------------------------------------------
+template <class T> struct SS {
+    T r, th, ph, ut, ur, uth, uph;
+};
+
+template <class T> __device__ __forceinline__ SS<T> schw_rhs(const SS<T>& s, T rs) {
+    const T f = DLIT(1.0) - rs / s.r;
+    const T r2 = s.r * s.r;
+    T sin_t, cos_t;
+    DM<T>::sincos_(s.th, &sin_t, &cos_t);
+    SS<T> d;
+    d.r = s.ur;
+    d.th = s.uth;
+    d.ph = s.uph;
+    d.ut = -(rs / (r2 * f)) * s.ut * s.ur;
+    d.ur = -(rs * f / (DLIT(2.0) * r2)) * s.ut * s.ut + (rs / (DLIT(2.0) * r2 * f)) * s.ur * s.ur
+           + s.r * f * (s.uth * s.uth + sin_t * sin_t * s.uph * s.uph);
+    d.uth = DLIT(-2.0) * s.ur * s.uth / s.r + sin_t * cos_t * s.uph * s.uph;
+    d.uph = DLIT(-2.0) * s.ur * s.uph / s.r - DLIT(2.0) * (cos_t / sin_t) * s.uth * s.uph;
+    return d;
+}
+
+template <class T> __device__ __forceinline__ SS<T> ss_axpy(const SS<T>& y, const SS<T>& k, T f) {
+    return SS<T>{y.r + k.r * f,   y.th + k.th * f,   y.ph + k.ph * f,  y.ut + k.ut * f,
+                 y.ur + k.ur * f, y.uth + k.uth * f, y.uph + k.uph * f};
+}
+
+template <class T> __device__ __forceinline__ SS<T> schw_rk4(const SS<T>& y, T h, T rs) {
+    const T hh = DLIT(0.5) * h;
+    const SS<T> k1 = schw_rhs(y, rs);
+    const SS<T> k2 = schw_rhs(ss_axpy(y, k1, hh), rs);
+    const SS<T> k3 = schw_rhs(ss_axpy(y, k2, hh), rs);
+    const SS<T> k4 = schw_rhs(ss_axpy(y, k3, h), rs);
+    const T h6 = h / DLIT(6.0);
+    auto comb = [&](T y0, T a1, T a2, T a3, T a4) { return y0 + ((a1 + a2 * DLIT(2.0)) + (a3 * DLIT(2.0) + a4)) * h6; };
+    return SS<T>{comb(y.r, k1.r, k2.r, k3.r, k4.r),         comb(y.th, k1.th, k2.th, k3.th, k4.th),
+                 comb(y.ph, k1.ph, k2.ph, k3.ph, k4.ph),     comb(y.ut, k1.ut, k2.ut, k3.ut, k4.ut),
+                 comb(y.ur, k1.ur, k2.ur, k3.ur, k4.ur),     comb(y.uth, k1.uth, k2.uth, k3.uth, k4.uth),
+                 comb(y.uph, k1.uph, k2.uph, k3.uph, k4.uph)};
+}
+
+template <class T> __device__ __forceinline__ SS<T> schw_init(const View<T>& v, const CamDir<T>& cd) {
+    SS<T> s;
+    s.r = v.cam_r;
+    s.th = v.cam_theta;
+    s.ph = v.cam_phi;
+    s.ur = cd.ur;
+    s.uth = cd.utheta;
+    s.uph = cd.uphi;
+    const T kin = (cd.ur * cd.ur) / v.f_cam + cd.utheta * cd.utheta * v.cam_r * v.cam_r
+                  + cd.uphi * cd.uphi * v.cam_r * v.cam_r * v.sin_th * v.sin_th;
+    s.ut = DM<T>::sqrt_(DM<T>::fmax_(kin / v.f_cam, DLIT(0.0)));
+    return s;
+}
+
+// Equatorial crossing of theta = pi/2 between two samples
+// (disc_intersection.h:30-55); frac only meaningful when crossed.
+template <class T> __device__ __forceinline__ bool crossed_equator(T th_prev, T th_curr, T& frac) {
+    const T mid = DLIT(1.5707963267948966);
+    const T dp = th_prev - mid;
+    const T dc = th_curr - mid;
+    const bool x = (dp * dc) < DLIT(0.0);
+    frac = x ? (mid - th_prev) / (th_curr - th_prev) : DLIT(0.0);
+    return x;
+}
+
+}  // namespace sgxd

@@ -1,0 +1,431 @@
+// singularity_gb300/csrc/sgx_trace.cu
+//
+// Kernels of the geodesic tracer for sm_103a.
+//
+// The reference launches one thread per pixel and traces the pixel's samples
+// one after another (geodesic_kernel.cu:462-510); a warp then runs as long as
+// its slowest ray, and ray lengths span 1 to thousands of steps.  Here the
+// unit of work is one (pixel, sample) ray taken from a global queue by a
+// persistent kernel:
+//   * each warp keeps 32 rays in registers; every `refill` steps the lanes
+//     whose ray has ended are found with a ballot, their results are shaded
+//     and stored, and one atomic per warp hands them the next ray ids;
+//   * ray id = pixel * S + sample, so fresh warps start on neighbouring rays;
+//   * per-sample tone-mapped colours go to a [S][npix] float4 buffer and an
+//     ordered pass sums them per pixel in sample order, exactly the
+//     accumulation order of the reference loop, so results do not depend on
+//     which warp traced which sample;
+//   * view constants live in shared memory, read by every lane.
+// All loops are bounded: a ray ends after max_steps integrator steps, and the
+// queue is a single counter that only grows.
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "sgx_device.cuh"
+#include "sgx_kernels.hpp"
+
+namespace sgxk {
+
+using namespace sgxd;
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+template <class T> __device__ __forceinline__ bool finite_(T x) { return isfinite(x); }
+
+// ---------------------------------------------------------------------------
+// Ray policies: the state each lane keeps and one loop iteration of the
+// reference (checks on the current state, then one step).
+// ---------------------------------------------------------------------------
+
+// Kerr, fixed step (geodesic_kernel.cu:303-403).
+template <class T, bool FAST> struct KerrFixed {
+    KS<T> y;
+    KC<T> c;
+    T prev_th, prev_r;
+    T t0, t1, t2;  // termination data: (r_cross, phi, T_local) or (theta, phi)
+    std::uint32_t steps, term;
+
+    __device__ __forceinline__ bool init(const View<T>& v, const CamDir<T>& cd, const PassDesc&) {
+        steps = 0;
+        T E, L;
+        if (!kerr_init(v, cd, y, E, L)) {
+            term = TERM_NO_ROOT;
+            return false;
+        }
+        c = make_kc(v, E, L);
+        prev_th = y.th;
+        prev_r = y.r;
+        if (v.max_steps == 0u) {
+            term = TERM_BUDGET;
+            return false;
+        }
+        return true;
+    }
+
+    // Returns true when the ray has ended.
+    __device__ __forceinline__ bool step(const View<T>& v, const PassDesc&) {
+        if (!finite_(y.r) || y.r < v.hcut) {
+            term = TERM_HORIZON;
+            return true;
+        }
+        if (y.r > v.escape_r) {
+            term = TERM_ESCAPE;
+            t0 = y.th;
+            t1 = y.ph;
+            return true;
+        }
+        T frac;
+        if ((v.flags & SGX_FLAG_DISC_ON) && crossed_equator(prev_th, y.th, frac)) {
+            const T r_cross = prev_r + frac * (y.r - prev_r);
+            if (r_cross >= v.r_in && r_cross <= v.r_out) {
+                const T T_local = disc_temperature(r_cross, v.r_in, v.peak_T);
+                term = T_local > DLIT(0.0) ? TERM_DISC : TERM_DISC_COLD;
+                t0 = r_cross;
+                t1 = y.ph;
+                t2 = T_local;
+                return true;
+            }
+        }
+        prev_th = y.th;
+        prev_r = y.r;
+        y = kerr_rk4<T, FAST>(y, v.h, v, c);
+        if (++steps >= v.max_steps) {
+            term = TERM_BUDGET;
+            return true;
+        }
+        return false;
+    }
+
+    __device__ __forceinline__ V3<T> shade(const View<T>& v) const {
+        if (term == TERM_ESCAPE && (v.flags & SGX_FLAG_STARFIELD_ON)) return sky_color(t0, t1);
+        if (term == TERM_DISC) return kerr_disc(v, c.L, t0, t1, t2);
+        return mk3(DLIT(0.0), DLIT(0.0), DLIT(0.0));
+    }
+};
+
+// Schwarzschild, fixed step (geodesic_kernel.cu:229-297).
+template <class T, bool FAST> struct SchwFixed {
+    SS<T> y;
+    T prev_th, prev_r, prev_uph;
+    T t0, t1, t2, t3;
+    std::uint32_t steps, term;
+
+    __device__ __forceinline__ bool init(const View<T>& v, const CamDir<T>& cd, const PassDesc&) {
+        steps = 0;
+        y = schw_init(v, cd);
+        prev_th = y.th;
+        prev_r = y.r;
+        prev_uph = y.uph;
+        if (v.max_steps == 0u) {
+            term = TERM_BUDGET;
+            return false;
+        }
+        return true;
+    }
+
+    __device__ __forceinline__ bool step(const View<T>& v, const PassDesc&) {
+        if (!finite_(y.r) || y.r < v.hcut) {
+            term = TERM_HORIZON;
+            return true;
+        }
+        if (y.r > v.escape_r) {
+            term = TERM_ESCAPE;
+            t0 = y.th;
+            t1 = y.ph;
+            return true;
+        }
+        T frac;
+        if ((v.flags & SGX_FLAG_DISC_ON) && crossed_equator(prev_th, y.th, frac)) {
+            const T r_cross = prev_r + frac * (y.r - prev_r);
+            const T uph_cross = prev_uph + frac * (y.uph - prev_uph);
+            if (r_cross >= v.r_in && r_cross <= v.r_out) {
+                const T T_local = disc_temperature(r_cross, v.r_in, v.peak_T);
+                term = T_local > DLIT(0.0) ? TERM_DISC : TERM_DISC_COLD;
+                t0 = r_cross;
+                // phi_cross = lerp(phi, phi, frac) in the reference (geodesic_kernel.cu:282)
+                t1 = y.ph + frac * (y.ph - y.ph);
+                t2 = T_local;
+                t3 = uph_cross;
+                return true;
+            }
+        }
+        prev_th = y.th;
+        prev_r = y.r;
+        prev_uph = y.uph;
+        y = schw_rk4(y, v.h, v.rs);
+        if (++steps >= v.max_steps) {
+            term = TERM_BUDGET;
+            return true;
+        }
+        return false;
+    }
+
+    __device__ __forceinline__ V3<T> shade(const View<T>& v) const {
+        if (term == TERM_ESCAPE && (v.flags & SGX_FLAG_STARFIELD_ON)) return sky_color(t0, t1);
+        if (term == TERM_DISC) return schw_disc(v, t3, t0, t1, t2);
+        return mk3(DLIT(0.0), DLIT(0.0), DLIT(0.0));
+    }
+};
+
+template <class T> __device__ __forceinline__ void load_view(View<T>& dst, const View<T>* src) {
+    // Cooperative copy of the view constants into shared memory.
+    const int words = int(sizeof(View<T>) / 4);
+    const std::uint32_t* s = reinterpret_cast<const std::uint32_t*>(src);
+    std::uint32_t* d = reinterpret_cast<std::uint32_t*>(&dst);
+    for (int i = threadIdx.x; i < words; i += blockDim.x) d[i] = s[i];
+}
+
+template <class T> __device__ __forceinline__ float4 tone(const View<T>& v, V3<T> hdr, std::uint32_t steps) {
+    return make_float4(float(aces1(hdr.x * v.exposure)), float(aces1(hdr.y * v.exposure)),
+                       float(aces1(hdr.z * v.exposure)), __uint_as_float(steps));
+}
+
+// Warp-aggregated add of a per-lane counter.
+__device__ __forceinline__ void warp_add(unsigned long long* dst, unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
+    if ((threadIdx.x & 31) == 0 && v != 0ull) atomicAdd(dst, v);
+}
+
+enum : int { MODE_IDLE = 0, MODE_ACTIVE = 1, MODE_DONE = 2 };
+
+template <class T, class Ray>
+__global__ void __launch_bounds__(256) trace_persistent(const View<T>* __restrict__ g_view, PassDesc pass) {
+    __shared__ View<T> v;
+    load_view(v, g_view);
+    __syncthreads();
+
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    Ray ray;
+    int mode = MODE_IDLE;
+    std::uint64_t id = 0;
+    bool exhausted = false;
+    unsigned long long my_steps = 0, my_budget = 0, my_rays = 0;
+
+    for (;;) {
+        // 1. shade and store rays that ended.
+        if (mode == MODE_DONE) {
+            const std::uint32_t pix = std::uint32_t(id / pass.S);
+            const std::uint32_t sl = std::uint32_t(id - std::uint64_t(pix) * pass.S);
+            pass.results[std::uint64_t(sl) * pass.npix + pix] = tone(v, ray.shade(v), ray.steps);
+            my_steps += ray.steps;
+            my_budget += (ray.term == TERM_BUDGET) ? 1ull : 0ull;
+            my_rays += 1ull;
+            mode = MODE_IDLE;
+        }
+        // 2. refill idle lanes from the queue, one atomic per warp.
+        if (!exhausted) {
+            const unsigned idle = __ballot_sync(kFull, mode == MODE_IDLE);
+            if (idle != 0u) {
+                const unsigned n = __popc(idle);
+                const int leader = __ffs(idle) - 1;
+                unsigned long long base = 0;
+                if (int(lane) == leader) base = atomicAdd(&pass.counters->next_ray, (unsigned long long)n);
+                base = __shfl_sync(kFull, base, leader);
+                if (mode == MODE_IDLE) {
+                    id = base + __popc(idle & lt_mask);
+                    if (id < pass.total_rays) {
+                        const std::uint32_t pix = std::uint32_t(id / pass.S);
+                        const std::uint32_t sl = std::uint32_t(id - std::uint64_t(pix) * pass.S);
+                        const std::uint32_t gy = pix / v.width;
+                        const std::uint32_t gx = pix - gy * v.width;
+                        const CamDir<T> cd = camera_dir(v, gx, gy, pass.s0 + sl);
+                        mode = ray.init(v, cd, pass) ? MODE_ACTIVE : MODE_DONE;
+                    }
+                }
+                if (base + n >= pass.total_rays) exhausted = true;
+            }
+        }
+        if (__ballot_sync(kFull, mode != MODE_IDLE) == 0u) break;
+        // 3. integrate.
+        for (std::uint32_t j = 0; j < pass.refill; ++j) {
+            if (mode == MODE_ACTIVE && ray.step(v, pass)) mode = MODE_DONE;
+            if (__all_sync(kFull, mode != MODE_ACTIVE)) break;
+        }
+    }
+    warp_add(&pass.counters->steps, my_steps);
+    warp_add(&pass.counters->budget_hits, my_budget);
+    warp_add(&pass.counters->rays, my_rays);
+}
+
+template <class T, class Ray>
+__global__ void __launch_bounds__(128) trace_probe(const View<T>* __restrict__ g_view, std::uint64_t n,
+                                                   const std::uint32_t* gx, const std::uint32_t* gy,
+                                                   const std::uint32_t* s, float* hdr3, std::uint32_t* steps,
+                                                   std::uint32_t* term, PassDesc pass) {
+    __shared__ View<T> v;
+    load_view(v, g_view);
+    __syncthreads();
+    const std::uint64_t i = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Ray ray;
+    const CamDir<T> cd = camera_dir(v, gx[i], gy[i], s[i]);
+    if (ray.init(v, cd, pass)) {
+        while (!ray.step(v, pass)) {
+        }
+    }
+    const V3<T> hdr = ray.shade(v);
+    if (hdr3 != nullptr) {
+        hdr3[3 * i + 0] = float(hdr.x);
+        hdr3[3 * i + 1] = float(hdr.y);
+        hdr3[3 * i + 2] = float(hdr.z);
+    }
+    if (steps != nullptr) steps[i] = ray.steps;
+    if (term != nullptr) term[i] = ray.term;
+}
+
+template <class T> __global__ void setup_view(const sgx_uniforms* u, View<T>* out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *out = make_view<T>(*u);
+}
+
+// Ordered per-pixel sum over the pass's samples (the reference's
+// `ldr = ldr + aces(...)` loop, geodesic_kernel.cu:492-501), then the final
+// encode (geodesic_kernel.cu:502-509) on the last pass.
+__device__ __forceinline__ void encode_pixel(float4 sum, float scale, std::uint32_t format, void* out,
+                                             std::uint32_t pix) {
+    const float r = sum.x * scale, g = sum.y * scale, b = sum.z * scale;
+    if (format == SGX_FORMAT_RGBA8_SRGB) {
+        uchar4 o;
+        o.x = to_u8(r);
+        o.y = to_u8(g);
+        o.z = to_u8(b);
+        o.w = 255;
+        static_cast<uchar4*>(out)[pix] = o;
+    } else {
+        static_cast<float4*>(out)[pix] = make_float4(r, g, b, 1.0f);
+    }
+}
+
+__global__ void accumulate_kernel(const float4* __restrict__ results, float4* __restrict__ acc, std::uint32_t npix,
+                                  std::uint32_t S, bool first, bool finalize, float scale, std::uint32_t format,
+                                  void* out) {
+    const std::uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= npix) return;
+    float4 sum = first ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : acc[pix];
+    for (std::uint32_t s = 0; s < S; ++s) {
+        const float4 q = results[std::uint64_t(s) * npix + pix];
+        sum.x = sum.x + q.x;
+        sum.y = sum.y + q.y;
+        sum.z = sum.z + q.z;
+    }
+    acc[pix] = sum;
+    if (finalize) encode_pixel(sum, scale, format, out, pix);
+}
+
+__global__ void encode_kernel(const float4* __restrict__ acc, std::uint32_t npix, float scale, std::uint32_t format,
+                              void* out) {
+    const std::uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= npix) return;
+    encode_pixel(acc[pix], scale, format, out, pix);
+}
+
+// ---------------------------------------------------------------------------
+// Dispatch
+// ---------------------------------------------------------------------------
+template <class T, template <class, bool> class Policy, bool FAST>
+cudaError_t run_persistent(const void* d_view, const PassDesc& pass, LaunchShape shape, cudaStream_t st) {
+    auto kern = trace_persistent<T, Policy<T, FAST>>;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int threads = shape.block_threads > 0 ? shape.block_threads : 256;
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0);
+    if (e != cudaSuccess) return e;
+    if (shape.blocks_per_sm > 0 && shape.blocks_per_sm < per_sm) per_sm = shape.blocks_per_sm;
+    if (per_sm < 1) per_sm = 1;
+    std::uint64_t blocks = std::uint64_t(sms) * per_sm;
+    const std::uint64_t need = (pass.total_rays + threads - 1) / threads;
+    if (need < blocks) blocks = need > 0 ? need : 1;
+    kern<<<unsigned(blocks), threads, 0, st>>>(static_cast<const View<T>*>(d_view), pass);
+    return cudaGetLastError();
+}
+
+template <class T, template <class, bool> class Policy, bool FAST>
+cudaError_t run_probe(const void* d_view, std::uint64_t n, const std::uint32_t* gx, const std::uint32_t* gy,
+                      const std::uint32_t* s, float* hdr3, std::uint32_t* steps, std::uint32_t* term,
+                      const PassDesc& pass, cudaStream_t st) {
+    const unsigned threads = 128;
+    const std::uint64_t blocks = (n + threads - 1) / threads;
+    if (blocks == 0) return cudaSuccess;
+    trace_probe<T, Policy<T, FAST>><<<unsigned(blocks), threads, 0, st>>>(static_cast<const View<T>*>(d_view), n, gx,
+                                                                         gy, s, hdr3, steps, term, pass);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+std::size_t view_bytes() {
+    const std::size_t a = sizeof(View<float>), b = sizeof(View<double>);
+    return ((a > b ? a : b) + 255) / 256 * 256;
+}
+
+cudaError_t launch_setup_view(const sgx_uniforms* d_u, void* d_view, int precision, cudaStream_t st) {
+    if (precision == SGX_PRECISION_FP64) {
+        setup_view<double><<<1, 32, 0, st>>>(d_u, static_cast<View<double>*>(d_view));
+    } else {
+        setup_view<float><<<1, 32, 0, st>>>(d_u, static_cast<View<float>*>(d_view));
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace(const void* d_view, int metric, int precision, int integrator, bool fast_math,
+                         const PassDesc& pass, LaunchShape shape, cudaStream_t st) {
+    if (integrator != SGX_INTEGRATOR_FIXED) return cudaErrorNotSupported;
+    const bool f64 = precision == SGX_PRECISION_FP64;
+    if (metric == SGX_METRIC_KERR) {
+        if (f64) return fast_math ? run_persistent<double, KerrFixed, true>(d_view, pass, shape, st)
+                                  : run_persistent<double, KerrFixed, false>(d_view, pass, shape, st);
+        return fast_math ? run_persistent<float, KerrFixed, true>(d_view, pass, shape, st)
+                         : run_persistent<float, KerrFixed, false>(d_view, pass, shape, st);
+    }
+    if (f64) return run_persistent<double, SchwFixed, false>(d_view, pass, shape, st);
+    return run_persistent<float, SchwFixed, false>(d_view, pass, shape, st);
+}
+
+cudaError_t launch_probe(const void* d_view, int metric, int precision, int integrator, bool fast_math,
+                         std::uint64_t n, const std::uint32_t* gx, const std::uint32_t* gy, const std::uint32_t* s,
+                         float* hdr3, std::uint32_t* steps, std::uint32_t* term, float tol, float h_init_frac,
+                         float h_max_frac, float zone, cudaStream_t st) {
+    if (integrator != SGX_INTEGRATOR_FIXED) return cudaErrorNotSupported;
+    PassDesc pass{};
+    pass.tol = tol;
+    pass.h_init_frac = h_init_frac;
+    pass.h_max_frac = h_max_frac;
+    pass.zone = zone;
+    const bool f64 = precision == SGX_PRECISION_FP64;
+    if (metric == SGX_METRIC_KERR) {
+        if (f64) return fast_math ? run_probe<double, KerrFixed, true>(d_view, n, gx, gy, s, hdr3, steps, term, pass, st)
+                                  : run_probe<double, KerrFixed, false>(d_view, n, gx, gy, s, hdr3, steps, term, pass, st);
+        return fast_math ? run_probe<float, KerrFixed, true>(d_view, n, gx, gy, s, hdr3, steps, term, pass, st)
+                         : run_probe<float, KerrFixed, false>(d_view, n, gx, gy, s, hdr3, steps, term, pass, st);
+    }
+    if (f64) return run_probe<double, SchwFixed, false>(d_view, n, gx, gy, s, hdr3, steps, term, pass, st);
+    return run_probe<float, SchwFixed, false>(d_view, n, gx, gy, s, hdr3, steps, term, pass, st);
+}
+
+cudaError_t launch_accumulate(const float4* results, float4* acc, std::uint32_t npix, std::uint32_t S, bool first,
+                              bool finalize, float scale, std::uint32_t format, void* out, cudaStream_t st) {
+    const unsigned threads = 256;
+    const unsigned blocks = (npix + threads - 1) / threads;
+    accumulate_kernel<<<blocks, threads, 0, st>>>(results, acc, npix, S, first, finalize, scale, format, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_encode(const float4* acc, std::uint32_t npix, float scale, std::uint32_t format, void* out,
+                          cudaStream_t st) {
+    const unsigned threads = 256;
+    const unsigned blocks = (npix + threads - 1) / threads;
+    encode_kernel<<<blocks, threads, 0, st>>>(acc, npix, scale, format, out);
+    return cudaGetLastError();
+}
+
+int max_resident_blocks(int, int, int, bool, int) { return 0; }
+
+}  // namespace sgxk
