@@ -94,7 +94,8 @@ class ClockSampler:
         sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
         mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for s in self.samples for i in range(4) if "Active" in s[3 + i]})
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 3 + i and s[3 + i].strip() == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(self.samples)}
 
@@ -115,7 +116,7 @@ def cpu_baseline(S, O, u, seconds: float = 12.0, seed: int = 0) -> dict:
         return gx.size, time.perf_counter() - t0
 
     rays, dt = run(256)
-    n = int(max(256, min(200_000, 256 * seconds / max(dt, 1e-3))))
+    n = int(max(256, min(2_000_000, 256 * seconds / max(dt, 1e-3))))
     rays, dt = run(n)
     return {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
             "sample": f"{n} random pixels x {SPP_PER_STEP} Halton samples of the workload ({rays} rays, "
