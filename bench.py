@@ -45,6 +45,8 @@ sys.path.insert(0, str(ROOT))
 
 WIDTH, HEIGHT, SPP, SPP_PER_STEP = 3840, 2160, 256, 16
 METRIC = "Kerr geodesic Mrays/s at 4K x 256spp"
+# `--workload small`: the same scene at 1280x720 (profiling captures only).
+SMALL = (1280, 720)
 
 
 def workload_uniforms(S, spp=SPP):
@@ -180,7 +182,11 @@ def main() -> None:
     ap.add_argument("--e2e-steps", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--rhs-form", type=int, default=0)
+    ap.add_argument("--workload", choices=["4k", "small"], default="4k")
     args = ap.parse_args()
+    if args.workload == "small":
+        global WIDTH, HEIGHT
+        WIDTH, HEIGHT = SMALL
     args.warmup = max(3, args.warmup)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

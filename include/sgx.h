@@ -208,6 +208,25 @@ sgx_status sgx_trace_samples(sgx_context* ctx, const sgx_uniforms* u, const sgx_
                              const uint32_t* gx, const uint32_t* gy, const uint32_t* s, float* hdr3,
                              uint32_t* steps, uint32_t* term);
 
+/* ---- allocation-free render ------------------------------------------------- */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory — code issuing work while a stream is captured into a CUDA graph,
+ * hosts whose device memory all belongs to their own pool, frame-paced callers
+ * that cannot take cudaFree's device-wide synchronisation — this renders one
+ * whole frame (all samples, fixed-step integrator, FP32 or FP64) into the
+ * caller's device buffer d_out on the caller's stream without allocating
+ * anything: its scratch is a fixed SGX_NOALLOC_SCRATCH_BYTES array inside the
+ * library, held by every GPU that loads the library until exit.  A frame needs
+ * 16 * width * height * (spp + 1) + 4096 bytes of it; larger frames return
+ * SGX_ERR_INVALID_ARGUMENT with the reason in err (a caller buffer, may be
+ * NULL).  The first call on a device does a one-time set-up (looks up the
+ * array's device address) and should come before any stream capture.  Calls
+ * share the array: calls whose GPU work overlaps race, so issue them on one
+ * stream. */
+#define SGX_NOALLOC_SCRATCH_BYTES (64ull << 20)
+sgx_status sgx_render_noalloc(const sgx_uniforms* u, const sgx_render_opts* opts, void* d_out, uint32_t format,
+                              void* stream, char* err, size_t err_len);
+
 /* ---- measurement --------------------------------------------------------- */
 /* No counterpart in the reference: the device's FP32 FMA issue ceiling in
  * TFLOP/s (2 flops per FMA), measured with a register-resident FMA kernel of

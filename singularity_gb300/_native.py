@@ -23,6 +23,7 @@ SGX_METRIC_SCHWARZSCHILD = 0
 SGX_METRIC_KERR = 1
 
 SGX_OK = 0
+NOALLOC_SCRATCH_BYTES = 64 << 20
 STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory",
                 4: "no frame rendered", 5: "unsupported"}
 
@@ -146,6 +147,8 @@ SIGNATURES = [
     ("sgx_get_stats", C.c_int, [_P, C.POINTER(RenderStats)]),
     ("sgx_last_error", C.c_char_p, [_P]),
     ("sgx_render_device", C.c_int, [_P, C.POINTER(Uniforms), C.POINTER(RenderOpts), _P, C.c_uint32, _P]),
+    ("sgx_render_noalloc", C.c_int, [C.POINTER(Uniforms), C.POINTER(RenderOpts), _P, C.c_uint32, _P, C.c_char_p,
+                                     C.c_size_t]),
     ("sgx_measure_fp32_peak", C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
     ("sgx_trace_samples", C.c_int, [_P, C.POINTER(Uniforms), C.POINTER(RenderOpts), C.c_uint64, _U32P, _U32P,
                                     _U32P, _F32P, _U32P, _U32P]),

@@ -1,0 +1,85 @@
+"""sgx_render_noalloc — the render entry point that allocates nothing.
+
+It exists for callers that cannot allocate device memory: work issued while a
+stream is being captured into a CUDA graph, hosts whose device memory all
+belongs to their own pool, and frame-paced callers that cannot take the
+device-wide synchronisation of cudaFree.  Its scratch is a fixed array inside
+the library, so here it must give the same frame as the allocating entry point
+(sgx_render + sgx_capture) — bit for bit, since the same kernels run — on two
+calls in a row with different scenes and sizes (the array keeps the previous
+call's contents), and it must refuse a frame larger than its scratch with a
+message that says why.
+
+The file name sorts last so a run that stops at the first failure has already
+run every other test.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _noalloc(lib, N, u, fmt, out, stream_ptr, opts=None):
+    err = C.create_string_buffer(512)
+    st = lib.sgx_render_noalloc(C.byref(u), C.byref(opts) if opts is not None else None,
+                                C.c_void_p(out.data_ptr()), fmt, C.c_void_p(stream_ptr), err, len(err))
+    return st, err.value.decode()
+
+
+def test_noalloc_matches_allocating_entry_on_consecutive_calls(sgx):
+    import torch
+    from singularity_gb300 import _native as N
+
+    lib = N.load()
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    r = sgx.Renderer(0)
+
+    isco = sgx.kerr_isco_prograde(1.0, 0.94)
+    scene_a = sgx.Scene(spin_a_over_M=0.94, disc_inner_M=isco, disc_outer_M=30.0, disc_peak_T_K=1e4,
+                        render_supersample=4)
+    u_a = sgx.pack_uniforms(scene_a, sgx.build_orbital_camera(40.0, 0.261799, 0.0, 30.0), 96, 64)
+    scene_b = sgx.Scene(metric=sgx.MetricType.Schwarzschild, spin_a_over_M=0.0, disc_inner_M=6.0,
+                        disc_outer_M=20.0, render_supersample=1, h_step=0.05, max_steps=4000)
+    u_b = sgx.pack_uniforms(scene_b, sgx.build_orbital_camera(30.0, 0.174533, 0.0, 40.0), 80, 48)
+
+    calls = [(u_a, N.FORMAT_RGBA8_SRGB), (u_b, N.FORMAT_RGBA8_SRGB), (u_a, N.FORMAT_RGBA32F)]
+    for u, fmt in calls:
+        npix = u.width * u.height
+        out = torch.zeros(npix * (4 if fmt == N.FORMAT_RGBA8_SRGB else 16), dtype=torch.uint8, device="cuda")
+        st, msg = _noalloc(lib, N, u, fmt, out, stream.cuda_stream)
+        assert st == N.SGX_OK, msg
+        stream.synchronize()
+        got = out.cpu().numpy()
+        want = r.render_image(u, fmt=fmt)
+        if fmt == N.FORMAT_RGBA8_SRGB:
+            got = got.reshape(u.height, u.width, 4)
+        else:
+            got = got.view(np.float32).reshape(u.height, u.width, 4)
+        np.testing.assert_array_equal(got, want)
+    r.close()
+
+
+def test_noalloc_rejects_frames_beyond_its_scratch(sgx):
+    import torch
+    from singularity_gb300 import _native as N
+
+    lib = N.load()
+    u = sgx.pack_uniforms(sgx.Scene(render_supersample=64), sgx.build_orbital_camera(30.0, 0.15, 0.0, 60.0),
+                          512, 512)
+    need = 16 * 512 * 512 * 65 + 4096
+    assert need > N.NOALLOC_SCRATCH_BYTES
+    out = torch.zeros(512 * 512 * 4, dtype=torch.uint8, device="cuda")
+    st, msg = _noalloc(lib, N, u, N.FORMAT_RGBA8_SRGB, out, 0)
+    assert st == 1
+    assert "scratch" in msg and str(need) in msg
+    # progressive passes are not offered by the allocation-free entry point
+    u.supersample = 4
+    opts = sgx.default_opts(sample_begin=2)
+    st, msg = _noalloc(lib, N, u, N.FORMAT_RGBA8_SRGB, out, 0, opts)
+    assert st == 1 and "whole frames" in msg
