@@ -44,6 +44,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 WIDTH, HEIGHT, SPP, SPP_PER_STEP = 3840, 2160, 256, 16
+# Headline integrator (BASELINE configs 2-3): error-controlled RK4, tolerance 1e-6.
 METRIC = "Kerr geodesic Mrays/s at 4K x 256spp"
 # `--workload small`: the same scene at 1280x720 (profiling captures only).
 SMALL = (1280, 720)
@@ -125,14 +126,14 @@ def cpu_baseline(S, O, u, seconds: float = 12.0, seed: int = 0) -> dict:
                       f"{dt:.1f} s), FP32 oracle"}
 
 
-def ops_per_step(S, O, u, n: int = 1024, seed: int = 1) -> tuple[float, float]:
+def ops_per_step(S, O, u, n: int = 1024, seed: int = 1, adaptive=None) -> tuple[float, float]:
     """Reference-formula FP32 ops per integrator step (ratio estimator over a
     random sample of the workload's rays) and mean steps per ray."""
     rng = np.random.default_rng(seed)
     gx = rng.integers(0, u.width, n).astype(np.uint32)
     gy = rng.integers(0, u.height, n).astype(np.uint32)
     s = rng.integers(0, SPP, n).astype(np.uint32)
-    ops, steps, _ = O.count_ops(u, gx, gy, s)
+    ops, steps, _ = O.count_ops(u, gx, gy, s, adaptive=adaptive)
     return float(ops.sum()) / max(1.0, float(steps.sum())), float(steps.mean())
 
 
@@ -173,6 +174,72 @@ def run_reference(args, rank: int) -> None:
     print(json.dumps(line), flush=True)
 
 
+def timed_pass(lib, N, r, u, opts, d_out, stream, torch) -> tuple[float, object]:
+    """One render call on `stream`, device-timed; returns (ms, stats)."""
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    st = lib.sgx_render_device(r.handle, C.byref(u), C.byref(opts), C.c_void_p(d_out.data_ptr()),
+                               N.FORMAT_RGBA8_SRGB, C.c_void_p(stream.cuda_stream))
+    if st != 0:
+        raise RuntimeError(lib.sgx_last_error(r.handle).decode())
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1), r.stats()
+
+
+def precision_study(S, N, O, lib, r, u, d_out, stream, torch, main_opts) -> dict:
+    """BASELINE precision form: FP32 vs FP64 GPU forms at equal tolerance, and
+    errors against the FP64 CPU oracle on 4096 pixels drawn with
+    numpy.random.default_rng(0).choice(W*H, 4096, replace=False)."""
+    out = {}
+    npix = u.width * u.height
+    rays = npix * SPP_PER_STEP
+    # speed of each form on one 16-spp pass
+    for name, prec in (("fp32", N.PRECISION_FP32), ("mixed", N.PRECISION_MIXED), ("fp64", N.PRECISION_FP64)):
+        o = S.default_opts(integrator=N.INTEGRATOR_ADAPTIVE, precision=prec, sample_count=SPP_PER_STEP)
+        timed_pass(lib, N, r, u, o, d_out, stream, torch)  # warm
+        ms, st = timed_pass(lib, N, r, u, o, d_out, stream, torch)
+        out[f"{name}_mrays_s"] = rays / (ms / 1e3) / 1e6
+        out[f"{name}_steps_per_ray"] = st.steps / max(1, st.rays)
+        if name == "mixed":
+            out["mixed_zone_step_frac"] = st.zone_steps / max(1, st.steps)
+    out["fp32_over_fp64"] = out["fp32_mrays_s"] / out["fp64_mrays_s"]
+    # reference algorithm (fixed-step RK4, h = 0.4) through the same kernels
+    o = S.default_opts(sample_count=SPP_PER_STEP)
+    timed_pass(lib, N, r, u, o, d_out, stream, torch)
+    ms, st = timed_pass(lib, N, r, u, o, d_out, stream, torch)
+    out["reference_fixed_step_mrays_s"] = rays / (ms / 1e3) / 1e6
+    out["reference_fixed_step_steps_per_ray"] = st.steps / max(1, st.rays)
+    # accuracy at 4096 seeded pixels, full 256 spp
+    rng = np.random.default_rng(0)
+    pix = rng.choice(npix, 4096, replace=False).astype(np.uint32)
+    imgs = {}
+    for name, prec in (("fp32", N.PRECISION_FP32), ("mixed", N.PRECISION_MIXED)):
+        o = S.default_opts(integrator=N.INTEGRATOR_ADAPTIVE, precision=prec, format=N.FORMAT_RGBA32F)
+        r.render(u, o)
+        imgs[name] = r.capture(N.FORMAT_RGBA32F).reshape(-1, 4)[pix, :3].astype(np.float64)
+    ad64 = O.adaptive_opts()
+    _, ldr64 = O.render(u, "f64", pixels=pix, adaptive=ad64)
+    for name, img in imgs.items():
+        d = np.abs(img - ldr64)
+        out[f"{name}_vs_fp64_oracle_mean_channel_err"] = float(d.mean())
+        out[f"{name}_vs_fp64_oracle_max_channel_err"] = float(d.max())
+    # Carter constant drift of the same integrator (CPU oracle, 1 sample per pixel)
+    gx, gy = (pix % u.width).astype(np.uint32), (pix // u.width).astype(np.uint32)
+    s = np.zeros_like(gx)
+    for prec, key in (("f32", "fp32"), ("f64", "fp64")):
+        _, _, term, d = O.trace(u, gx, gy, s, precision=prec, adaptive=ad64, diag=True)
+        ok = term != 5
+        dq = np.array([abs(x.Q_end - x.Q0) / x.norm_Q for x in d])[ok]
+        out[f"carter_drift_{key}"] = {"median": float(np.median(dq)), "mean": float(dq.mean()),
+                                      "p99": float(np.percentile(dq, 99)), "max": float(dq.max())}
+    out["note"] = ("speeds: one 16-spp 4K pass each; errors: full 256-spp frame, RGBA32F LDR mean, units of "
+                   "full scale; Carter drift |Q_end-Q0|/(|Q0|+L^2+a^2E^2) from the CPU oracle of the same "
+                   "integrator")
+    return out
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -181,7 +248,10 @@ def main() -> None:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--e2e-steps", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-precision-study", action="store_true")
     ap.add_argument("--rhs-form", type=int, default=0)
+    ap.add_argument("--integrator", choices=["adaptive", "fixed"], default="adaptive")
+    ap.add_argument("--precision", choices=["fp32", "mixed", "fp64"], default="fp32")
     ap.add_argument("--workload", choices=["4k", "small"], default="4k")
     args = ap.parse_args()
     if args.workload == "small":
@@ -207,21 +277,21 @@ def main() -> None:
     from singularity_gb300 import _native as N
 
     lib = N.load()
-    u = workload_uniforms(S)
     # Weak scaling: each rank renders its own view (camera azimuth offset per rank).
-    if world > 1:
-        cam = S.build_orbital_camera(40.0, 0.261799, 2 * np.pi * rank / world, 30.0)
-        isco = S.kerr_isco_prograde(1.0, 0.94)
-        u = S.pack_uniforms(S.Scene(spin_a_over_M=0.94, disc_inner_M=isco, disc_outer_M=30.0, disc_peak_T_K=1e4,
-                                    render_supersample=SPP), cam, WIDTH, HEIGHT, 0.0)
+    isco = S.kerr_isco_prograde(1.0, 0.94)
+    cam = S.build_orbital_camera(40.0, 0.261799, 2 * np.pi * rank / world, 30.0)
+    u = S.pack_uniforms(S.Scene(spin_a_over_M=0.94, disc_inner_M=isco, disc_outer_M=30.0, disc_peak_T_K=1e4,
+                                render_supersample=SPP), cam, WIDTH, HEIGHT, 0.0)
     npix = u.width * u.height
     r = S.Renderer(local)
     stream = torch.cuda.Stream()
     d_out = torch.empty(npix * 4, dtype=torch.uint8, device="cuda")
-    opts = S.default_opts(sample_count=SPP_PER_STEP, rhs_form=args.rhs_form)
+    integ = N.INTEGRATOR_ADAPTIVE if args.integrator == "adaptive" else N.INTEGRATOR_FIXED
+    prec = {"fp32": N.PRECISION_FP32, "mixed": N.PRECISION_MIXED, "fp64": N.PRECISION_FP64}[args.precision]
+    opts = S.default_opts(sample_count=SPP_PER_STEP, rhs_form=args.rhs_form, integrator=integ, precision=prec)
     passes = SPP // SPP_PER_STEP
     step_idx = [0]
-    stats_acc = {"steps": 0, "rays": 0, "trace_ms": [], "budget": 0}
+    stats_acc = {"steps": 0, "rays": 0, "trace_ms": [], "budget": 0, "rejected": 0}
 
     def step(record=True):
         k = step_idx[0] % passes
@@ -236,11 +306,12 @@ def main() -> None:
             stats_acc["steps"] += s.steps
             stats_acc["rays"] += s.rays
             stats_acc["budget"] += s.budget_hits
+            stats_acc["rejected"] += s.rejected
             stats_acc["trace_ms"].append(s.trace_ms)
 
     for _ in range(args.warmup):
         step(record=False)
-    step_idx[0] = 0  # timed region starts a fresh 256-spp frame
+    step_idx[0] = 0  # the timed region starts a fresh 256-spp frame
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
@@ -268,10 +339,10 @@ def main() -> None:
         u16 = u.copy()
         u16.supersample = SPP_PER_STEP
         host = torch.empty(npix * 4, dtype=torch.uint8, pin_memory=True)
-        ref_opts = S.default_opts(rhs_form=args.rhs_form)
+        e2e_opts = S.default_opts(rhs_form=args.rhs_form, integrator=integ, precision=prec)
 
         def e2e_step():
-            st = lib.sgx_render(r.handle, C.byref(u16), C.byref(ref_opts))
+            st = lib.sgx_render(r.handle, C.byref(u16), C.byref(e2e_opts))
             if st != 0:
                 raise RuntimeError(lib.sgx_last_error(r.handle).decode())
             st = lib.sgx_capture(r.handle, C.c_void_p(host.data_ptr()), host.numel(), N.FORMAT_RGBA8_SRGB)
@@ -290,7 +361,8 @@ def main() -> None:
             dt = float(t.item())
         e2e = {"value": npix * SPP_PER_STEP * args.e2e_steps * world / dt / 1e6, "unit": "Mrays/s",
                "h2d_bytes_per_step": C.sizeof(N.Uniforms), "d2h_bytes_per_step": npix * 4,
-               "note": "sgx_render (full 16-spp frame) + sgx_capture RGBA8 into pinned host memory, wall clock"}
+               "note": "per step sgx_render (a full 16-spp frame) + sgx_capture RGBA8 into pinned host memory, "
+                       "wall clock"}
 
     if rank != 0:
         if world > 1:
@@ -300,7 +372,8 @@ def main() -> None:
     # --- roofline of the trace kernel ---
     from oracle import pyoracle as O
     O.build(ref=False)
-    ops_step, mean_steps_cpu = ops_per_step(S, O, u)
+    ad = O.adaptive_opts() if integ == N.INTEGRATOR_ADAPTIVE else None
+    ops_step, mean_steps_cpu = ops_per_step(S, O, u, adaptive=ad)
     trace_ms = np.array(stats_acc["trace_ms"])
     per_launch_ms = float(trace_ms.mean())
     steps_per_launch = stats_acc["steps"] / max(1, len(trace_ms))
@@ -311,29 +384,39 @@ def main() -> None:
     tp = ROOT / "profiles" / "trace_kernel_traffic.json"
     if tp.exists():
         t = json.loads(tp.read_text())
-        traffic = t.get("bytes_per_ray", 0) * npix * SPP_PER_STEP if "bytes_per_ray" in t else None
+        key = f"{args.integrator}_bytes_per_ray"
+        traffic = t[key] * npix * SPP_PER_STEP if key in t else None
     roof = {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
             "frac": achieved / peak.value if peak.value else None, "traffic": traffic,
-            "peak_source": "measured: register-resident FMA ceiling (sgx_measure_fp32_peak) on this GPU",
+            "peak_source": "of measured: register-resident FMA ceiling (sgx_measure_fp32_peak) on this GPU; "
+                           "MEASURED_PEAKS.json holds no FP32 SIMT figure",
             "ops_per_step": ops_step, "kernel_ms_per_launch": per_launch_ms,
             "gpu_steps_per_ray": stats_acc["steps"] / max(1, stats_acc["rays"]),
-            "cpu_oracle_steps_per_ray": mean_steps_cpu}
+            "cpu_oracle_steps_per_ray": mean_steps_cpu,
+            "ops_rule": "reference formulas, add/sub/mul/div/sqrt/min/max/transcendental = 1 each"}
 
+    study = None
+    if not args.no_precision_study and args.precision == "fp32" and integ == N.INTEGRATOR_ADAPTIVE:
+        study = precision_study(S, N, O, lib, r, u, d_out, stream, torch, opts)
     cpu = None if args.no_cpu_baseline else cpu_baseline(S, O, u)
     clocks = clk.summary()
+    wl = (f"kerr_a0.94_r40_i75_fov30_isco-30M_T1e4_{WIDTH}x{HEIGHT}_256spp_"
+          + ("adaptive_tol1e-6" if integ == N.INTEGRATOR_ADAPTIVE else "fixed_h0.4_max2500") + f"_{args.precision}")
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": value / 13.1, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "kerr_a0.94_r40_i75_fov30_isco-30M_T1e4_3840x2160_256spp_fixed_h0.4_max2500",
-                   "spp_per_step": SPP_PER_STEP, "rays_per_step": npix * SPP_PER_STEP,
-                   "integrator": "fixed-step RK4 (reference algorithm)", "rhs_form": args.rhs_form,
+        "vs_baseline": value / 13.1, "dtype": "f32" if args.precision != "fp64" else "f64", "data": "synthetic",
+        "config": {"workload": wl, "spp_per_step": SPP_PER_STEP, "rays_per_step": npix * SPP_PER_STEP,
+                   "integrator": ("error-controlled RK4, FSAL 3rd-order estimate, tol 1e-6"
+                                  if integ == N.INTEGRATOR_ADAPTIVE else "fixed-step RK4 (reference algorithm)"),
+                   "precision": args.precision, "rhs_form": args.rhs_form,
                    "l2": "each step writes a 2.1 GB per-sample buffer (> 129 MB L2); no extra flush",
                    "vs_baseline_basis": "13.1 Mrays/s: 4K Kerr a/M=0.94 256 spp in 162 s on an RTX 3090 "
-                                        "(README.md:39,130), wall clock incl. PNG"},
+                                        "(README.md:39,130), wall clock incl. PNG, fixed step h=0.4"},
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
         "gpu_launches": 3 * args.steps,
         "budget_exhausted_rays": stats_acc["budget"],
+        "precision_study": study,
     }
     print(json.dumps(line), flush=True)
     if world > 1:

@@ -50,6 +50,7 @@ struct Counted {
     constexpr Counted(float x) : v(x) {}
     explicit operator int() const { return int(v); }
     explicit operator float() const { return v; }
+    explicit operator double() const { return double(v); }
 };
 inline Counted operator+(Counted a, Counted b) { ++g_ops; return Counted(a.v + b.v); }
 inline Counted operator-(Counted a, Counted b) { ++g_ops; return Counted(a.v - b.v); }

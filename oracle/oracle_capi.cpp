@@ -223,6 +223,6 @@ int oracle_crossing_f32(float th_prev, float th_curr, float* frac) {
 }
 
 // Spherical photon orbit radius for xi = L/E (adaptive_oracle.hpp).
-double oracle_photon_orbit_radius(double a, double M, double xi) { return oracle::photon_orbit_radius(a, M, xi); }
+double oracle_photon_orbit_radius(double a, double M, double xi) { return oracle::photon_orbit_radius<double>(a, M, xi); }
 
 }  // extern "C"

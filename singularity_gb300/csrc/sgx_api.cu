@@ -122,8 +122,10 @@ sgx_status check_opts(sgx_context* c, const sgx_render_opts& o) {
     if (o.format > SGX_FORMAT_RGBA16F_HDR) return fail(c, SGX_ERR_INVALID_ARGUMENT, "unknown format");
     if (o.format == SGX_FORMAT_RGBA16F_HDR) return fail(c, SGX_ERR_UNSUPPORTED, "RGBA16F HDR output is not built");
     if (o.rhs_form > 1) return fail(c, SGX_ERR_INVALID_ARGUMENT, "unknown rhs_form");
-    if (o.integrator == SGX_INTEGRATOR_ADAPTIVE)
-        return fail(c, SGX_ERR_UNSUPPORTED, "adaptive integrator is not built in this library");
+    if (o.integrator == SGX_INTEGRATOR_ADAPTIVE) {
+        if (!(o.tolerance > 0.0f) || !(o.h_init_frac > 0.0f) || !(o.h_max_frac > 0.0f) || !(o.fp64_zone >= 0.0f))
+            return fail(c, SGX_ERR_INVALID_ARGUMENT, "adaptive options must be positive (zone >= 0)");
+    }
     if (o.precision == SGX_PRECISION_MIXED && o.integrator == SGX_INTEGRATOR_FIXED)
         return fail(c, SGX_ERR_INVALID_ARGUMENT, "the mixed precision form applies to the adaptive integrator");
     return SGX_OK;

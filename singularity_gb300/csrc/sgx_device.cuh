@@ -96,6 +96,8 @@ template <class T> struct View {
     T hcut;   // capture radius: 1.02 r_+ (Kerr) or u.horizon_cut (Schwarzschild)
     T f_cam;  // Schwarzschild 1 - rs/r_cam
     T f_obs;  // Kerr shading 1 - 2M/r_cam
+    T r_plus;             // outer horizon M + sqrt(M^2 - a^2)
+    T r_ph_pro, r_ph_ret; // equatorial prograde / retrograde photon orbits
     // Kerr metric at the camera (geodesic_kernel.cu:310-319)
     T g_tt, g_tp, g_rr, g_thth, g_pp, s2_c;
     std::uint32_t width, height, flags, max_steps, spp, metric;
@@ -158,6 +160,9 @@ template <class T> __device__ inline View<T> make_view(const sgx_uniforms& u) {
     } else {
         v.hcut = T(u.horizon_cut);
     }
+    v.r_plus = Mm + DM<T>::sqrt_(DM<T>::fmax_(Mm * Mm - a * a, DLIT(0.0)));
+    v.r_ph_pro = DLIT(2.0) * Mm * (DLIT(1.0) + DM<T>::cos_(DLIT(2.0) / DLIT(3.0) * DM<T>::acos_(-a / Mm)));
+    v.r_ph_ret = DLIT(2.0) * Mm * (DLIT(1.0) + DM<T>::cos_(DLIT(2.0) / DLIT(3.0) * DM<T>::acos_(a / Mm)));
     return v;
 }
 
@@ -604,6 +609,124 @@ template <class T> __device__ __forceinline__ bool crossed_equator(T th_prev, T 
     const bool x = (dp * dc) < DLIT(0.0);
     frac = x ? (mid - th_prev) / (th_curr - th_prev) : DLIT(0.0);
     return x;
+}
+
+// ---------------------------------------------------------------------------
+// Error-controlled Kerr integration (the adaptive extension; the CPU oracle's
+// adaptive_oracle.hpp is its specification, operation for operation).
+// ---------------------------------------------------------------------------
+template <class T> struct KAttempt {
+    KS<T> y4, k4, k5;
+    T h6;
+};
+
+// RK4 stages from y with k1 = f(y) known, plus the first-same-as-last stage.
+template <class T, bool FAST>
+__device__ __forceinline__ KAttempt<T> kerr_attempt(const KS<T>& y, const KS<T>& k1, T h, const View<T>& v,
+                                                    const KC<T>& c) {
+    KAttempt<T> at;
+    const T hh = DLIT(0.5) * h;
+    const KS<T> k2 = kerr_rhs<T, FAST>(ks_axpy(y, k1, hh), v, c);
+    const KS<T> k3 = kerr_rhs<T, FAST>(ks_axpy(y, k2, hh), v, c);
+    at.k4 = kerr_rhs<T, FAST>(ks_axpy(y, k3, h), v, c);
+    at.h6 = h / DLIT(6.0);
+    at.y4.r = y.r + ((k1.r + k2.r * DLIT(2.0)) + (k3.r * DLIT(2.0) + at.k4.r)) * at.h6;
+    at.y4.th = y.th + ((k1.th + k2.th * DLIT(2.0)) + (k3.th * DLIT(2.0) + at.k4.th)) * at.h6;
+    at.y4.ph = y.ph + ((k1.ph + k2.ph * DLIT(2.0)) + (k3.ph * DLIT(2.0) + at.k4.ph)) * at.h6;
+    at.y4.pr = y.pr + ((k1.pr + k2.pr * DLIT(2.0)) + (k3.pr * DLIT(2.0) + at.k4.pr)) * at.h6;
+    at.y4.pth = y.pth + ((k1.pth + k2.pth * DLIT(2.0)) + (k3.pth * DLIT(2.0) + at.k4.pth)) * at.h6;
+    at.k5 = kerr_rhs<T, FAST>(at.y4, v, c);
+    return at;
+}
+
+template <class C> __device__ __forceinline__ C absv(C x) { return x < C(0.0f) ? -x : x; }
+
+// max_i |h/6 (k4_i - k5_i)| / (tol (1 + max(|y_i|, |y4_i|))) over r, theta,
+// phi, p_r, p_theta, evaluated in C; NaN/overflow -> 1e30.
+template <class C, class T>
+__device__ __forceinline__ C error_norm(const KS<T>& y, const KAttempt<T>& a, float tol_f) {
+    const C tol = C(tol_f);
+    const C h6 = C(a.h6);
+    auto one = [&](T yv, T y4v, T k4v, T k5v) {
+        const C ya = absv(C(yv)), yb = absv(C(y4v));
+        const C sc = tol * (C(1.0f) + (ya > yb ? ya : yb));
+        return absv(h6 * (C(k4v) - C(k5v))) / sc;
+    };
+    C e = one(y.r, a.y4.r, a.k4.r, a.k5.r);
+    C t;
+    t = one(y.th, a.y4.th, a.k4.th, a.k5.th);
+    e = t > e ? t : e;
+    t = one(y.ph, a.y4.ph, a.k4.ph, a.k5.ph);
+    e = t > e ? t : e;
+    t = one(y.pr, a.y4.pr, a.k4.pr, a.k5.pr);
+    e = t > e ? t : e;
+    t = one(y.pth, a.y4.pth, a.k4.pth, a.k5.pth);
+    e = t > e ? t : e;
+    if (!(e <= C(1e30f))) e = C(1e30f);
+    return e;
+}
+
+// h *= clamp(0.9 / err^(1/4), 0.2, 4) with IEEE sqrt and division only.
+template <class C> __device__ __forceinline__ C step_factor(C e) {
+    if (e <= C(1e-30f)) return C(4.0f);
+    C f = C(0.9f) / sqrt(sqrt(e));
+    f = f < C(0.2f) ? C(0.2f) : f;
+    f = f > C(4.0f) ? C(4.0f) : f;
+    return f;
+}
+
+template <class T> __device__ __forceinline__ T hermite(T y0, T y1, T d0, T d1, T h, T s) {
+    const T s2 = s * s, s3 = s2 * s;
+    const T h00 = DLIT(2.0) * s3 - DLIT(3.0) * s2 + DLIT(1.0);
+    const T h10 = s3 - DLIT(2.0) * s2 + s;
+    const T h01 = DLIT(3.0) * s2 - DLIT(2.0) * s3;
+    const T h11 = s3 - s2;
+    return h00 * y0 + h10 * h * d0 + h01 * y1 + h11 * h * d1;
+}
+template <class T> __device__ __forceinline__ T hermite_d(T y0, T y1, T d0, T d1, T h, T s) {
+    const T s2 = s * s;
+    const T h00 = DLIT(6.0) * s2 - DLIT(6.0) * s;
+    const T h10 = DLIT(3.0) * s2 - DLIT(4.0) * s + DLIT(1.0);
+    const T h01 = DLIT(6.0) * s - DLIT(6.0) * s2;
+    const T h11 = DLIT(3.0) * s2 - DLIT(2.0) * s;
+    return h00 * y0 + h10 * h * d0 + h01 * y1 + h11 * h * d1;
+}
+
+// theta = pi/2 inside an accepted step: three Newton steps on the Hermite
+// interpolant from the linear estimate, clamped to [0, 1].
+template <class T> __device__ __forceinline__ T crossing_fraction(T th0, T th1, T d0, T d1, T h) {
+    const T mid = DLIT(1.5707963267948966);
+    T s = (mid - th0) / (th1 - th0);
+#pragma unroll 1
+    for (int it = 0; it < 3; ++it) {
+        const T f = hermite(th0, th1, d0, d1, h, s) - mid;
+        const T fp = hermite_d(th0, th1, d0, d1, h, s);
+        if (!(absv(fp) > DLIT(1e-30))) break;
+        T sn = s - f / fp;
+        sn = sn < DLIT(0.0) ? DLIT(0.0) : (sn > DLIT(1.0) ? DLIT(1.0) : sn);
+        s = sn;
+    }
+    return s;
+}
+
+// Spherical photon orbit with the ray's xi = L/E (Bardeen 1973, Teo 2003):
+// 24 bisections inside [r_ph,pro, r_ph,ret]; 3M for a = 0; NaN outside.
+template <class T> __device__ __forceinline__ T photon_orbit_radius(const View<T>& v, T xi) {
+    const T a = v.a, Mm = v.M;
+    if (!(a > DLIT(1e-7)) && !(a < DLIT(-1e-7))) return DLIT(3.0) * Mm;
+    auto xi_of = [&](T r) { return (r * r * (DLIT(3.0) * Mm - r) - a * a * (r + Mm)) / (a * (r - Mm)); };
+    T lo = v.r_ph_pro, hi = v.r_ph_ret;
+    const T flo = xi_of(lo) - xi, fhi = xi_of(hi) - xi;
+    if (!(flo * fhi <= DLIT(0.0))) return T(NAN);
+    const bool lo_neg = flo <= DLIT(0.0);
+#pragma unroll 1
+    for (int i = 0; i < 24; ++i) {
+        const T mid = DLIT(0.5) * (lo + hi);
+        const T fm = xi_of(mid) - xi;
+        if ((fm <= DLIT(0.0)) == lo_neg) lo = mid;
+        else hi = mid;
+    }
+    return DLIT(0.5) * (lo + hi);
 }
 
 }  // namespace sgxd

@@ -41,13 +41,19 @@ template <class T> __device__ __forceinline__ bool finite_(T x) { return isfinit
 // reference (checks on the current state, then one step).
 // ---------------------------------------------------------------------------
 
+// Policy flags: bit 0 = shared-reciprocal Kerr RHS, bit 1 = mixed precision.
+constexpr int FL_FAST = 1;
+constexpr int FL_MIXED = 2;
+
 // Kerr, fixed step (geodesic_kernel.cu:303-403).
-template <class T, bool FAST> struct KerrFixed {
+template <class T, int FL> struct KerrFixed {
+    static constexpr bool FAST = (FL & FL_FAST) != 0;
     KS<T> y;
     KC<T> c;
     T prev_th, prev_r;
     T t0, t1, t2;  // termination data: (r_cross, phi, T_local) or (theta, phi)
     std::uint32_t steps, term;
+    static constexpr std::uint32_t rej = 0, zone = 0;
 
     __device__ __forceinline__ bool init(const View<T>& v, const CamDir<T>& cd, const PassDesc&) {
         steps = 0;
@@ -108,11 +114,12 @@ template <class T, bool FAST> struct KerrFixed {
 };
 
 // Schwarzschild, fixed step (geodesic_kernel.cu:229-297).
-template <class T, bool FAST> struct SchwFixed {
+template <class T, int FL> struct SchwFixed {
     SS<T> y;
     T prev_th, prev_r, prev_uph;
     T t0, t1, t2, t3;
     std::uint32_t steps, term;
+    static constexpr std::uint32_t rej = 0, zone = 0;
 
     __device__ __forceinline__ bool init(const View<T>& v, const CamDir<T>& cd, const PassDesc&) {
         steps = 0;
@@ -171,6 +178,115 @@ template <class T, bool FAST> struct SchwFixed {
     }
 };
 
+// Kerr, error-controlled RK4 with the FSAL third-order estimate (the adaptive
+// extension; oracle/adaptive_oracle.hpp is its specification).  One call of
+// step() is one attempt; max_steps bounds the attempts.
+template <class T, int FL> struct KerrAdaptive {
+    static constexpr bool FAST = (FL & FL_FAST) != 0;
+    static constexpr bool MIXED = (FL & FL_MIXED) != 0;
+    KS<T> y, k1;
+    KC<T> c;
+    T h, r_c;
+    T t0, t1, t2;
+    std::uint32_t steps, term, rej, zone;
+
+    __device__ __forceinline__ bool init(const View<T>& v, const CamDir<T>& cd, const PassDesc& pass) {
+        steps = rej = zone = 0;
+        T E, L;
+        if (!kerr_init(v, cd, y, E, L)) {
+            term = TERM_NO_ROOT;
+            return false;
+        }
+        if constexpr (MIXED) {
+            double Ed, Ld, prd, pthd;
+            if (!kerr_init_fp64_constants(v, cd, Ed, Ld, prd, pthd)) {
+                term = TERM_NO_ROOT;
+                return false;
+            }
+            E = float(Ed);
+            L = float(Ld);
+            y.pr = float(prd);
+            y.pth = float(pthd);
+            r_c = photon_orbit_radius(v, L / E);
+        } else {
+            r_c = DLIT(0.0);
+        }
+        c = make_kc(v, E, L);
+        h = T(pass.h_init_frac) * y.r;
+        k1 = kerr_rhs<T, FAST>(y, v, c);
+        if (v.max_steps == 0u) {
+            term = TERM_BUDGET;
+            return false;
+        }
+        return true;
+    }
+
+    __device__ __forceinline__ bool step(const View<T>& v, const PassDesc& pass) {
+        if (!finite_(y.r) || y.r < v.hcut) {
+            term = TERM_HORIZON;
+            return true;
+        }
+        if (y.r > v.escape_r) {
+            term = TERM_ESCAPE;
+            t0 = y.th;
+            t1 = y.ph;
+            return true;
+        }
+        const T hmax = T(pass.h_max_frac) * y.r;
+        h = h > hmax ? hmax : h;
+        const KAttempt<T> at = kerr_attempt<T, FAST>(y, k1, h, v, c);
+        ++steps;
+        bool accept;
+        bool in_zone = false;
+        if constexpr (MIXED) {
+            const T zw = T(pass.zone);
+            in_zone = (absv(y.r - r_c) < zw) || (y.r - v.r_plus < zw);
+        }
+        if (in_zone) {
+            ++zone;
+            const double e = error_norm<double>(y, at, pass.tol);
+            accept = e <= 1.0;
+            h = T(float(double(float(h)) * step_factor<double>(e)));
+        } else {
+            const T e = error_norm<T>(y, at, pass.tol);
+            accept = e <= DLIT(1.0);
+            h = h * step_factor<T>(e);
+        }
+        if (!accept) {
+            ++rej;
+        } else {
+            T frac;
+            if ((v.flags & SGX_FLAG_DISC_ON) && crossed_equator(y.th, at.y4.th, frac)) {
+                const T hs = at.h6 * DLIT(6.0);
+                const T sfr = crossing_fraction(y.th, at.y4.th, k1.th, at.k5.th, hs);
+                const T r_cross = hermite(y.r, at.y4.r, k1.r, at.k5.r, hs, sfr);
+                if (r_cross >= v.r_in && r_cross <= v.r_out) {
+                    const T T_local = disc_temperature(r_cross, v.r_in, v.peak_T);
+                    term = T_local > DLIT(0.0) ? TERM_DISC : TERM_DISC_COLD;
+                    t0 = r_cross;
+                    t1 = hermite(y.ph, at.y4.ph, k1.ph, at.k5.ph, hs, sfr);
+                    t2 = T_local;
+                    y = at.y4;
+                    return true;
+                }
+            }
+            y = at.y4;
+            k1 = at.k5;
+        }
+        if (steps >= v.max_steps) {
+            term = TERM_BUDGET;
+            return true;
+        }
+        return false;
+    }
+
+    __device__ __forceinline__ V3<T> shade(const View<T>& v) const {
+        if (term == TERM_ESCAPE && (v.flags & SGX_FLAG_STARFIELD_ON)) return sky_color(t0, t1);
+        if (term == TERM_DISC) return kerr_disc(v, c.L, t0, t1, t2);
+        return mk3(DLIT(0.0), DLIT(0.0), DLIT(0.0));
+    }
+};
+
 template <class T> __device__ __forceinline__ void load_view(View<T>& dst, const View<T>* src) {
     // Cooperative copy of the view constants into shared memory.
     const int words = int(sizeof(View<T>) / 4);
@@ -205,7 +321,7 @@ __global__ void __launch_bounds__(256) trace_persistent(const View<T>* __restric
     int mode = MODE_IDLE;
     std::uint64_t id = 0;
     bool exhausted = false;
-    unsigned long long my_steps = 0, my_budget = 0, my_rays = 0;
+    unsigned long long my_steps = 0, my_budget = 0, my_rays = 0, my_rej = 0, my_zone = 0;
 
     for (;;) {
         // 1. shade and store rays that ended.
@@ -214,6 +330,8 @@ __global__ void __launch_bounds__(256) trace_persistent(const View<T>* __restric
             const std::uint32_t sl = std::uint32_t(id - std::uint64_t(pix) * pass.S);
             pass.results[std::uint64_t(sl) * pass.npix + pix] = tone(v, ray.shade(v), ray.steps);
             my_steps += ray.steps;
+            my_rej += ray.rej;
+            my_zone += ray.zone;
             my_budget += (ray.term == TERM_BUDGET) ? 1ull : 0ull;
             my_rays += 1ull;
             mode = MODE_IDLE;
@@ -249,6 +367,8 @@ __global__ void __launch_bounds__(256) trace_persistent(const View<T>* __restric
         }
     }
     warp_add(&pass.counters->steps, my_steps);
+    warp_add(&pass.counters->rejected, my_rej);
+    warp_add(&pass.counters->zone_steps, my_zone);
     warp_add(&pass.counters->budget_hits, my_budget);
     warp_add(&pass.counters->rays, my_rays);
 }
@@ -327,9 +447,9 @@ __global__ void encode_kernel(const float4* __restrict__ acc, std::uint32_t npix
 // ---------------------------------------------------------------------------
 // Dispatch
 // ---------------------------------------------------------------------------
-template <class T, template <class, bool> class Policy, bool FAST>
+template <class T, template <class, int> class Policy, int FL>
 cudaError_t run_persistent(const void* d_view, const PassDesc& pass, LaunchShape shape, cudaStream_t st) {
-    auto kern = trace_persistent<T, Policy<T, FAST>>;
+    auto kern = trace_persistent<T, Policy<T, FL>>;
     int dev = 0;
     cudaGetDevice(&dev);
     int sms = 0;
@@ -347,16 +467,43 @@ cudaError_t run_persistent(const void* d_view, const PassDesc& pass, LaunchShape
     return cudaGetLastError();
 }
 
-template <class T, template <class, bool> class Policy, bool FAST>
+template <class T, template <class, int> class Policy, int FL>
 cudaError_t run_probe(const void* d_view, std::uint64_t n, const std::uint32_t* gx, const std::uint32_t* gy,
                       const std::uint32_t* s, float* hdr3, std::uint32_t* steps, std::uint32_t* term,
                       const PassDesc& pass, cudaStream_t st) {
     const unsigned threads = 128;
     const std::uint64_t blocks = (n + threads - 1) / threads;
     if (blocks == 0) return cudaSuccess;
-    trace_probe<T, Policy<T, FAST>><<<unsigned(blocks), threads, 0, st>>>(static_cast<const View<T>*>(d_view), n, gx,
-                                                                         gy, s, hdr3, steps, term, pass);
+    trace_probe<T, Policy<T, FL>><<<unsigned(blocks), threads, 0, st>>>(static_cast<const View<T>*>(d_view), n, gx, gy,
+                                                                       s, hdr3, steps, term, pass);
     return cudaGetLastError();
+}
+
+// One call site per (metric, precision, integrator, RHS form): F is invoked
+// with the chosen <T, Policy, FL> as a generic lambda's template arguments.
+template <class F>
+cudaError_t dispatch(int metric, int precision, int integrator, bool fast, F&& f) {
+    const bool adaptive = integrator == SGX_INTEGRATOR_ADAPTIVE;
+    if (metric == SGX_METRIC_KERR && adaptive) {
+        if (precision == SGX_PRECISION_FP64)
+            return fast ? f.template operator()<double, KerrAdaptive, FL_FAST>()
+                        : f.template operator()<double, KerrAdaptive, 0>();
+        if (precision == SGX_PRECISION_MIXED)
+            return fast ? f.template operator()<float, KerrAdaptive, FL_FAST | FL_MIXED>()
+                        : f.template operator()<float, KerrAdaptive, FL_MIXED>();
+        return fast ? f.template operator()<float, KerrAdaptive, FL_FAST>()
+                    : f.template operator()<float, KerrAdaptive, 0>();
+    }
+    if (metric == SGX_METRIC_KERR) {
+        if (precision == SGX_PRECISION_FP64)
+            return fast ? f.template operator()<double, KerrFixed, FL_FAST>()
+                        : f.template operator()<double, KerrFixed, 0>();
+        return fast ? f.template operator()<float, KerrFixed, FL_FAST>()
+                    : f.template operator()<float, KerrFixed, 0>();
+    }
+    // Schwarzschild: the reference's fixed-step integrator for every form.
+    if (precision == SGX_PRECISION_FP64) return f.template operator()<double, SchwFixed, 0>();
+    return f.template operator()<float, SchwFixed, 0>();
 }
 
 }  // namespace
@@ -377,37 +524,25 @@ cudaError_t launch_setup_view(const sgx_uniforms* d_u, void* d_view, int precisi
 
 cudaError_t launch_trace(const void* d_view, int metric, int precision, int integrator, bool fast_math,
                          const PassDesc& pass, LaunchShape shape, cudaStream_t st) {
-    if (integrator != SGX_INTEGRATOR_FIXED) return cudaErrorNotSupported;
-    const bool f64 = precision == SGX_PRECISION_FP64;
-    if (metric == SGX_METRIC_KERR) {
-        if (f64) return fast_math ? run_persistent<double, KerrFixed, true>(d_view, pass, shape, st)
-                                  : run_persistent<double, KerrFixed, false>(d_view, pass, shape, st);
-        return fast_math ? run_persistent<float, KerrFixed, true>(d_view, pass, shape, st)
-                         : run_persistent<float, KerrFixed, false>(d_view, pass, shape, st);
-    }
-    if (f64) return run_persistent<double, SchwFixed, false>(d_view, pass, shape, st);
-    return run_persistent<float, SchwFixed, false>(d_view, pass, shape, st);
+    return dispatch(metric, precision, integrator, fast_math,
+                    [&]<class T, template <class, int> class Policy, int FL>() {
+                        return run_persistent<T, Policy, FL>(d_view, pass, shape, st);
+                    });
 }
 
 cudaError_t launch_probe(const void* d_view, int metric, int precision, int integrator, bool fast_math,
                          std::uint64_t n, const std::uint32_t* gx, const std::uint32_t* gy, const std::uint32_t* s,
                          float* hdr3, std::uint32_t* steps, std::uint32_t* term, float tol, float h_init_frac,
                          float h_max_frac, float zone, cudaStream_t st) {
-    if (integrator != SGX_INTEGRATOR_FIXED) return cudaErrorNotSupported;
     PassDesc pass{};
     pass.tol = tol;
     pass.h_init_frac = h_init_frac;
     pass.h_max_frac = h_max_frac;
     pass.zone = zone;
-    const bool f64 = precision == SGX_PRECISION_FP64;
-    if (metric == SGX_METRIC_KERR) {
-        if (f64) return fast_math ? run_probe<double, KerrFixed, true>(d_view, n, gx, gy, s, hdr3, steps, term, pass, st)
-                                  : run_probe<double, KerrFixed, false>(d_view, n, gx, gy, s, hdr3, steps, term, pass, st);
-        return fast_math ? run_probe<float, KerrFixed, true>(d_view, n, gx, gy, s, hdr3, steps, term, pass, st)
-                         : run_probe<float, KerrFixed, false>(d_view, n, gx, gy, s, hdr3, steps, term, pass, st);
-    }
-    if (f64) return run_probe<double, SchwFixed, false>(d_view, n, gx, gy, s, hdr3, steps, term, pass, st);
-    return run_probe<float, SchwFixed, false>(d_view, n, gx, gy, s, hdr3, steps, term, pass, st);
+    return dispatch(metric, precision, integrator, fast_math,
+                    [&]<class T, template <class, int> class Policy, int FL>() {
+                        return run_probe<T, Policy, FL>(d_view, n, gx, gy, s, hdr3, steps, term, pass, st);
+                    });
 }
 
 cudaError_t launch_accumulate(const float4* results, float4* acc, std::uint32_t npix, std::uint32_t S, bool first,
