@@ -217,7 +217,8 @@ sgx_status sgx_trace_samples(sgx_context* ctx, const sgx_uniforms* u, const sgx_
  * caller's device buffer d_out on the caller's stream without allocating
  * anything: its scratch is a fixed SGX_NOALLOC_SCRATCH_BYTES array inside the
  * library, held by every GPU that loads the library until exit.  A frame needs
- * 16 * width * height * (spp + 1) + 4096 bytes of it; larger frames return
+ * 16 * width * height * (spp + 1) + 4096 bytes of it (FP64:
+ * 16 * width * height * (2 * spp + 1) + 4096); larger frames return
  * SGX_ERR_INVALID_ARGUMENT with the reason in err (a caller buffer, may be
  * NULL).  The first call on a device does a one-time set-up (looks up the
  * array's device address) and should come before any stream capture.  Calls

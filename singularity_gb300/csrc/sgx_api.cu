@@ -26,7 +26,7 @@ struct sgx_context {
     std::uint32_t width = 0, height = 0;
     void* d_image = nullptr;       // npix * 16 bytes
     float4* d_acc = nullptr;       // npix
-    float4* d_results = nullptr;   // results_cap bytes
+    void* d_results = nullptr;     // results_cap bytes (hit records)
     std::size_t results_cap = 0;
     void* d_view = nullptr;
     sgx_uniforms* d_u = nullptr;
@@ -89,7 +89,7 @@ sgx_status ensure_results(sgx_context* c, std::size_t bytes) {
     if (c->d_results) cudaFree(c->d_results);
     c->d_results = nullptr;
     c->results_cap = 0;
-    SGX_CUDA(c, cudaMalloc(reinterpret_cast<void**>(&c->d_results), bytes));
+    SGX_CUDA(c, cudaMalloc(&c->d_results, bytes));
     c->results_cap = bytes;
     return SGX_OK;
 }
@@ -149,8 +149,9 @@ sgx_status render_impl(sgx_context* c, const sgx_uniforms* u, const sgx_render_o
     std::size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
     std::size_t budget = std::min(c->workspace_budget, free_b / 2 + c->results_cap);
-    std::uint64_t per_sample = std::uint64_t(npix) * sizeof(float4);
+    std::uint64_t per_sample = std::uint64_t(npix) * sgxk::record_bytes(int(o.precision));
     std::uint32_t S = std::uint32_t(std::max<std::uint64_t>(1, std::min<std::uint64_t>(count, budget / per_sample)));
+    S = std::min(S, sgxk::kMaxPassSamplesHost);
     sgx_status s = ensure_results(c, std::size_t(S) * per_sample);
     if (s != SGX_OK) return s;
 
@@ -183,8 +184,8 @@ sgx_status render_impl(sgx_context* c, const sgx_uniforms* u, const sgx_render_o
         const bool first = (s0 == 0);
         const bool finalize = (s0 + n == spp);
         const float scale = 1.0f / float(spp);
-        SGX_CUDA(c, sgxk::launch_accumulate(c->d_results, c->d_acc, npix, n, first, finalize, scale, format, out,
-                                            st));
+        SGX_CUDA(c, sgxk::launch_accumulate(c->d_view, int(o.precision), c->d_results, c->d_acc, npix, n, first,
+                                            finalize, scale, format, out, st));
         SGX_CUDA(c, cudaMemcpyAsync(c->h_counters, c->d_counters, sizeof(sgxk::PassCounters),
                                     cudaMemcpyDeviceToHost, st));
         SGX_CUDA(c, cudaEventRecord(c->ev_end, st));

@@ -43,6 +43,12 @@ template <> struct DM<float> {
     static __device__ __forceinline__ float fmin_(float a, float b) { return fminf(a, b); }
     static __device__ __forceinline__ float fmax_(float a, float b) { return fmaxf(a, b); }
     static __device__ __forceinline__ float rcp_(float x) { return 1.0f / x; }
+    // PTX rcp.approx.ftz.f32: one MUFU op, at most 1 ulp from 1/x.
+    static __device__ __forceinline__ float rcp_fast(float x) {
+        float r;
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+        return r;
+    }
 };
 template <> struct DM<double> {
     static __device__ __forceinline__ double lit(float, double d) { return d; }
@@ -57,6 +63,7 @@ template <> struct DM<double> {
     static __device__ __forceinline__ double fmin_(double a, double b) { return fmin(a, b); }
     static __device__ __forceinline__ double fmax_(double a, double b) { return fmax(a, b); }
     static __device__ __forceinline__ double rcp_(double x) { return 1.0 / x; }
+    static __device__ __forceinline__ double rcp_fast(double x) { return 1.0 / x; }
 };
 
 #define DLIT(x) (::sgxd::DM<T>::lit(x##f, x))
@@ -185,17 +192,22 @@ template <class T> struct CamDir {
     T ur, utheta, uphi;
 };
 
-template <class T>
-__device__ __forceinline__ CamDir<T> camera_dir(const View<T>& v, std::uint32_t gx, std::uint32_t gy,
-                                                std::uint32_t s) {
-    T ox, oy;
-    if (v.spp == 1u) {
+// Sub-pixel offset of sample s (geodesic_kernel.cu:483-497): the pixel centre
+// for spp == 1, else Halton(s + 1) in bases 2 and 3.
+template <class T> __device__ __forceinline__ void sample_offset(std::uint32_t spp, std::uint32_t s, T& ox, T& oy) {
+    if (spp == 1u) {
         ox = DLIT(0.5);
         oy = DLIT(0.5);
     } else {
         ox = halton<T>(s + 1u, 2u);
         oy = halton<T>(s + 1u, 3u);
     }
+}
+
+// Camera direction for pixel (gx, gy) and sub-pixel offset (ox, oy): the
+// per-sample part of build_camera_ray_subpixel (geodesic_kernel.cu:188-223).
+template <class T>
+__device__ __forceinline__ CamDir<T> camera_dir(const View<T>& v, std::uint32_t gx, std::uint32_t gy, T ox, T oy) {
     const T fx = T(float(gx)) + ox;
     const T fy = T(float(gy)) + oy;
     const T u_ndc = (DLIT(2.0) * fx / v.width_f - DLIT(1.0)) * v.aspect * v.tan_half_fov;
@@ -428,9 +440,8 @@ template <class T> __device__ __forceinline__ KS<T> kerr_rhs_ref(const KS<T>& s,
 //              + Del_r p_r^2 / Sigma - 2r Dp2 / Sigma^2
 //   -2 dp_th = B_t/(SD) - B Sig_t/(Sigma^2 Delta)
 //              - L^2 (Sig_t s2 + Sigma sin2t)/(Sigma^2 s2^2) - Dp2 Sig_t / Sigma^2
-template <class T> __device__ __forceinline__ KS<T> kerr_rhs_fast(const KS<T>& s, const View<T>& v, const KC<T>& c) {
-    T st, ct;
-    DM<T>::sincos_(s.th, &st, &ct);
+template <class T>
+__device__ __forceinline__ KS<T> kerr_rhs_fast_sc(const KS<T>& s, T st, T ct, const View<T>& v, const KC<T>& c) {
     const T r = s.r;
     const T a2 = v.a2;
     const T s2 = st * st;
@@ -443,9 +454,9 @@ template <class T> __device__ __forceinline__ KS<T> kerr_rhs_fast(const KS<T>& s
     const T Delta = r * (r - DLIT(2.0) * v.M) + a2;
     const T a2s2 = a2 * s2;
     const T A = r2a2 * r2a2 - a2s2 * Delta;
-    const T iS = DM<T>::rcp_(Sigma);
-    const T iD = DM<T>::rcp_(Delta);
-    const T is2 = DM<T>::rcp_(safe_s2);
+    const T iS = DM<T>::rcp_fast(Sigma);
+    const T iD = DM<T>::rcp_fast(Delta);
+    const T is2 = DM<T>::rcp_fast(safe_s2);
     const T iSD = iS * iD;
     const T iS2 = iS * iS;
     KS<T> d;
@@ -469,6 +480,12 @@ template <class T> __device__ __forceinline__ KS<T> kerr_rhs_fast(const KS<T>& s
     return d;
 }
 
+template <class T> __device__ __forceinline__ KS<T> kerr_rhs_fast(const KS<T>& s, const View<T>& v, const KC<T>& c) {
+    T st, ct;
+    DM<T>::sincos_(s.th, &st, &ct);
+    return kerr_rhs_fast_sc(s, st, ct, v, c);
+}
+
 template <class T, bool FAST>
 __device__ __forceinline__ KS<T> kerr_rhs(const KS<T>& s, const View<T>& v, const KC<T>& c) {
     if constexpr (FAST) return kerr_rhs_fast(s, v, c);
@@ -482,13 +499,17 @@ template <class T> __device__ __forceinline__ KS<T> ks_axpy(const KS<T>& y, cons
 // Fixed-step RK4 with the reference's near-pole damping (kerr_hamilton.h:165-178).
 template <class T, bool FAST>
 __device__ __forceinline__ KS<T> kerr_rk4(const KS<T>& y, T h, const View<T>& v, const KC<T>& c) {
-    T st = DM<T>::sin_(y.th);
-    st = (st < DLIT(0.0)) ? -st : st;
+    // sin(theta) of the step's start serves both the pole damping and k1.
+    T s0, c0;
+    DM<T>::sincos_(y.th, &s0, &c0);
+    T st = (s0 < DLIT(0.0)) ? -s0 : s0;
     T ps = st * DLIT(5.0);
     ps = (ps > DLIT(1.0)) ? DLIT(1.0) : ((ps < DLIT(0.05)) ? DLIT(0.05) : ps);
     h = h * ps;
     const T hh = DLIT(0.5) * h;
-    const KS<T> k1 = kerr_rhs<T, FAST>(y, v, c);
+    KS<T> k1;
+    if constexpr (FAST) k1 = kerr_rhs_fast_sc(y, s0, c0, v, c);
+    else k1 = kerr_rhs_ref(y, v, c);
     const KS<T> k2 = kerr_rhs<T, FAST>(ks_axpy(y, k1, hh), v, c);
     const KS<T> k3 = kerr_rhs<T, FAST>(ks_axpy(y, k2, hh), v, c);
     const KS<T> k4 = kerr_rhs<T, FAST>(ks_axpy(y, k3, h), v, c);

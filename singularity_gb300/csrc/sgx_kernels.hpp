@@ -30,7 +30,7 @@ struct PassDesc {
     std::uint32_t S;
     std::uint32_t s0;
     std::uint32_t refill;       // steps between refills
-    float4* results;            // [S][npix] ACES(hdr*exposure).rgb, w = steps
+    void* results;              // [S][npix] hit records, record_bytes(precision) each
     PassCounters* counters;
     // adaptive options
     float tol, h_init_frac, h_max_frac, zone;
@@ -54,16 +54,23 @@ cudaError_t launch_probe(const void* d_view, int metric, int precision, int inte
                          float* hdr3, std::uint32_t* steps, std::uint32_t* term, float tol, float h_init_frac,
                          float h_max_frac, float zone, cudaStream_t st);
 
-// Ordered accumulation of one pass into acc (float4 per pixel); when
-// `finalize`, also writes the frame in `format` to out (scale = 1/spp).
-cudaError_t launch_accumulate(const float4* results, float4* acc, std::uint32_t npix, std::uint32_t S, bool first,
-                              bool finalize, float scale, std::uint32_t format, void* out, cudaStream_t st);
+// Shades the pass's hit records and adds them in sample order into acc
+// (float4 per pixel); when `finalize`, also writes the frame in `format` to
+// out (scale = 1/spp).
+cudaError_t launch_accumulate(const void* d_view, int precision, const void* results, float4* acc,
+                              std::uint32_t npix, std::uint32_t S, bool first, bool finalize, float scale,
+                              std::uint32_t format, void* out, cudaStream_t st);
+
+// Bytes of one hit record (16 for FP32 and mixed, 32 for FP64).
+std::size_t record_bytes(int precision);
+
+// Samples one pass may hold (the per-block offset table).
+constexpr std::uint32_t kMaxPassSamplesHost = 1024;
 
 // Re-encodes the accumulated frame (acc, float4 mean-sum) in another format.
 cudaError_t launch_encode(const float4* acc, std::uint32_t npix, float scale, std::uint32_t format, void* out,
                           cudaStream_t st);
 
 std::size_t view_bytes();
-int max_resident_blocks(int metric, int precision, int integrator, bool fast_math, int block_threads);
 
 }  // namespace sgxk

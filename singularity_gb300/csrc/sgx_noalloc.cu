@@ -20,8 +20,9 @@
 //
 // Rules for callers:
 //   * A frame needs 16 * width * height * (spp + 1) bytes of scratch plus a
-//     4 KiB header; larger requests are rejected with SGX_ERR_INVALID_ARGUMENT
-//     and a message saying so.  spp is the clamped samples per pixel.
+//     4 KiB header (FP64: 16 * width * height * (2 * spp + 1)); larger requests
+//     are rejected with SGX_ERR_INVALID_ARGUMENT and a message saying so.  spp
+//     is the clamped samples per pixel.
 //   * The first call on each device looks up the array's device address
 //     (cudaGetSymbolAddress) with that device current; make that first call
 //     before any stream capture begins.
@@ -120,13 +121,15 @@ extern "C" sgx_status sgx_render_noalloc(const sgx_uniforms* u, const sgx_render
         return SGX_ERR_INVALID_ARGUMENT;
     }
     const std::uint64_t npix = std::uint64_t(u->width) * u->height;
-    const std::uint64_t need = kHeaderBytes + 16ull * npix * (std::uint64_t(spp) + 1ull);
+    const std::uint64_t rec = sgxk::record_bytes(int(o.precision));
+    const std::uint64_t need = kHeaderBytes + 16ull * npix + rec * npix * std::uint64_t(spp);
     if (need > SGX_NOALLOC_SCRATCH_BYTES) {
         char buf[256];
         std::snprintf(buf, sizeof(buf),
-                      "sgx_render_noalloc: frame needs %llu bytes of scratch (16*w*h*(spp+1) + 4096) but the "
-                      "fixed scratch holds %llu; use fewer pixels or samples, or the allocating entry points",
-                      (unsigned long long)need, (unsigned long long)SGX_NOALLOC_SCRATCH_BYTES);
+                      "sgx_render_noalloc: frame needs %llu bytes of scratch (16*w*h + %llu*w*h*spp + 4096) but "
+                      "the fixed scratch holds %llu; use fewer pixels or samples, or the allocating entry points",
+                      (unsigned long long)need, (unsigned long long)rec,
+                      (unsigned long long)SGX_NOALLOC_SCRATCH_BYTES);
         set_err(err, err_len, buf);
         return SGX_ERR_INVALID_ARGUMENT;
     }
@@ -145,7 +148,7 @@ extern "C" sgx_status sgx_render_noalloc(const sgx_uniforms* u, const sgx_render
     auto* d_u = reinterpret_cast<sgx_uniforms*>(base + kUniformsOff);
     void* d_view = base + kViewOff;
     auto* acc = reinterpret_cast<float4*>(base + kHeaderBytes);
-    auto* results = acc + npix;
+    void* results = acc + npix;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
 
     sgxk::PassDesc pass{};
@@ -169,8 +172,8 @@ extern "C" sgx_status sgx_render_noalloc(const sgx_uniforms* u, const sgx_render
         e = sgxk::launch_trace(d_view, int(u->metric_type), int(o.precision), int(o.integrator), o.rhs_form == 0,
                                pass, shape, st);
     if (e == cudaSuccess)
-        e = sgxk::launch_accumulate(results, acc, std::uint32_t(npix), spp, true, true, 1.0f / float(spp), format,
-                                    d_out, st);
+        e = sgxk::launch_accumulate(d_view, int(o.precision), results, acc, std::uint32_t(npix), spp, true, true,
+                                    1.0f / float(spp), format, d_out, st);
     if (e != cudaSuccess) {
         char buf[256];
         std::snprintf(buf, sizeof(buf), "sgx_render_noalloc: %s", cudaGetErrorString(e));

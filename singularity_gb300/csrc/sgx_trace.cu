@@ -11,11 +11,13 @@
 //     whose ray has ended are found with a ballot, their results are shaded
 //     and stored, and one atomic per warp hands them the next ray ids;
 //   * ray id = pixel * S + sample, so fresh warps start on neighbouring rays;
-//   * per-sample tone-mapped colours go to a [S][npix] float4 buffer and an
-//     ordered pass sums them per pixel in sample order, exactly the
-//     accumulation order of the reference loop, so results do not depend on
-//     which warp traced which sample;
-//   * view constants live in shared memory, read by every lane.
+//   * a finished ray leaves a 16-byte hit record (where it crossed the disc
+//     or which direction it escaped in, and how it ended) in a [S][npix]
+//     buffer; the ordered pass then shades each record, tone-maps it and sums
+//     a pixel's samples in sample order — the reference's accumulation order —
+//     so colour work runs converged, once per sample, outside the step loop,
+//     and results do not depend on which warp traced which sample;
+//   * view constants and the pass's Halton offsets live in shared memory.
 // All loops are bounded: a ray ends after max_steps integrator steps, and the
 // queue is a single counter that only grows.
 
@@ -40,6 +42,19 @@ template <class T> __device__ __forceinline__ bool finite_(T x) { return isfinit
 // Ray policies: the state each lane keeps and one loop iteration of the
 // reference (checks on the current state, then one step).
 // ---------------------------------------------------------------------------
+
+// Hit record of one finished ray: (t0, t1, t2) and meta = term | steps << 3.
+//   disc (Kerr):          r_cross, phi, L_z
+//   disc (Schwarzschild): r_cross, phi, u^phi at the crossing
+//   escape:               theta, phi
+template <class T> struct alignas(4 * sizeof(T)) Rec {
+    T t0, t1, t2;
+    std::uint32_t meta;
+};
+
+__device__ __forceinline__ std::uint32_t pack_meta(std::uint32_t term, std::uint32_t steps) {
+    return term | ((steps < 0x1FFFFFFFu ? steps : 0x1FFFFFFFu) << 3);
+}
 
 // Policy flags: bit 0 = shared-reciprocal Kerr RHS, bit 1 = mixed precision.
 constexpr int FL_FAST = 1;
@@ -92,7 +107,7 @@ template <class T, int FL> struct KerrFixed {
                 term = T_local > DLIT(0.0) ? TERM_DISC : TERM_DISC_COLD;
                 t0 = r_cross;
                 t1 = y.ph;
-                t2 = T_local;
+                t2 = c.L;
                 return true;
             }
         }
@@ -106,18 +121,14 @@ template <class T, int FL> struct KerrFixed {
         return false;
     }
 
-    __device__ __forceinline__ V3<T> shade(const View<T>& v) const {
-        if (term == TERM_ESCAPE && (v.flags & SGX_FLAG_STARFIELD_ON)) return sky_color(t0, t1);
-        if (term == TERM_DISC) return kerr_disc(v, c.L, t0, t1, t2);
-        return mk3(DLIT(0.0), DLIT(0.0), DLIT(0.0));
-    }
+    __device__ __forceinline__ Rec<T> record() const { return Rec<T>{t0, t1, t2, pack_meta(term, steps)}; }
 };
 
 // Schwarzschild, fixed step (geodesic_kernel.cu:229-297).
 template <class T, int FL> struct SchwFixed {
     SS<T> y;
     T prev_th, prev_r, prev_uph;
-    T t0, t1, t2, t3;
+    T t0, t1, t2;
     std::uint32_t steps, term;
     static constexpr std::uint32_t rej = 0, zone = 0;
 
@@ -155,8 +166,7 @@ template <class T, int FL> struct SchwFixed {
                 t0 = r_cross;
                 // phi_cross = lerp(phi, phi, frac) in the reference (geodesic_kernel.cu:282)
                 t1 = y.ph + frac * (y.ph - y.ph);
-                t2 = T_local;
-                t3 = uph_cross;
+                t2 = uph_cross;
                 return true;
             }
         }
@@ -171,11 +181,7 @@ template <class T, int FL> struct SchwFixed {
         return false;
     }
 
-    __device__ __forceinline__ V3<T> shade(const View<T>& v) const {
-        if (term == TERM_ESCAPE && (v.flags & SGX_FLAG_STARFIELD_ON)) return sky_color(t0, t1);
-        if (term == TERM_DISC) return schw_disc(v, t3, t0, t1, t2);
-        return mk3(DLIT(0.0), DLIT(0.0), DLIT(0.0));
-    }
+    __device__ __forceinline__ Rec<T> record() const { return Rec<T>{t0, t1, t2, pack_meta(term, steps)}; }
 };
 
 // Kerr, error-controlled RK4 with the FSAL third-order estimate (the adaptive
@@ -265,7 +271,7 @@ template <class T, int FL> struct KerrAdaptive {
                     term = T_local > DLIT(0.0) ? TERM_DISC : TERM_DISC_COLD;
                     t0 = r_cross;
                     t1 = hermite(y.ph, at.y4.ph, k1.ph, at.k5.ph, hs, sfr);
-                    t2 = T_local;
+                    t2 = c.L;
                     y = at.y4;
                     return true;
                 }
@@ -280,12 +286,21 @@ template <class T, int FL> struct KerrAdaptive {
         return false;
     }
 
-    __device__ __forceinline__ V3<T> shade(const View<T>& v) const {
-        if (term == TERM_ESCAPE && (v.flags & SGX_FLAG_STARFIELD_ON)) return sky_color(t0, t1);
-        if (term == TERM_DISC) return kerr_disc(v, c.L, t0, t1, t2);
-        return mk3(DLIT(0.0), DLIT(0.0), DLIT(0.0));
-    }
+    __device__ __forceinline__ Rec<T> record() const { return Rec<T>{t0, t1, t2, pack_meta(term, steps)}; }
 };
+
+// Colour of a hit record (geodesic_kernel.cu:250-296, 354-402): starfield for
+// an escape, disc emission for a hot crossing, black otherwise.
+template <class T> __device__ __forceinline__ V3<T> shade_record(const View<T>& v, const Rec<T>& r) {
+    const std::uint32_t term = r.meta & 7u;
+    if (term == TERM_ESCAPE && (v.flags & SGX_FLAG_STARFIELD_ON)) return sky_color(r.t0, r.t1);
+    if (term == TERM_DISC) {
+        const T T_local = disc_temperature(r.t0, v.r_in, v.peak_T);
+        if (v.metric == SGX_METRIC_KERR) return kerr_disc(v, r.t2, r.t0, r.t1, T_local);
+        return schw_disc(v, r.t2, r.t0, r.t1, T_local);
+    }
+    return mk3(DLIT(0.0), DLIT(0.0), DLIT(0.0));
+}
 
 template <class T> __device__ __forceinline__ void load_view(View<T>& dst, const View<T>* src) {
     // Cooperative copy of the view constants into shared memory.
@@ -295,9 +310,12 @@ template <class T> __device__ __forceinline__ void load_view(View<T>& dst, const
     for (int i = threadIdx.x; i < words; i += blockDim.x) d[i] = s[i];
 }
 
-template <class T> __device__ __forceinline__ float4 tone(const View<T>& v, V3<T> hdr, std::uint32_t steps) {
-    return make_float4(float(aces1(hdr.x * v.exposure)), float(aces1(hdr.y * v.exposure)),
-                       float(aces1(hdr.z * v.exposure)), __uint_as_float(steps));
+// Sub-pixel offsets of the pass's samples [s0, s0 + S), one table per block.
+constexpr std::uint32_t kMaxPassSamples = 1024;
+
+template <class T>
+__device__ __forceinline__ void load_offsets(T* ox, T* oy, const View<T>& v, const PassDesc& pass) {
+    for (std::uint32_t i = threadIdx.x; i < pass.S; i += blockDim.x) sample_offset<T>(v.spp, pass.s0 + i, ox[i], oy[i]);
 }
 
 // Warp-aggregated add of a per-lane counter.
@@ -312,8 +330,12 @@ enum : int { MODE_IDLE = 0, MODE_ACTIVE = 1, MODE_DONE = 2 };
 template <class T, class Ray>
 __global__ void __launch_bounds__(256) trace_persistent(const View<T>* __restrict__ g_view, PassDesc pass) {
     __shared__ View<T> v;
+    __shared__ T off_x[kMaxPassSamples], off_y[kMaxPassSamples];
     load_view(v, g_view);
     __syncthreads();
+    load_offsets(off_x, off_y, v, pass);
+    __syncthreads();
+    Rec<T>* __restrict__ results = static_cast<Rec<T>*>(pass.results);
 
     const unsigned lane = threadIdx.x & 31u;
     const unsigned lt_mask = (1u << lane) - 1u;
@@ -324,11 +346,11 @@ __global__ void __launch_bounds__(256) trace_persistent(const View<T>* __restric
     unsigned long long my_steps = 0, my_budget = 0, my_rays = 0, my_rej = 0, my_zone = 0;
 
     for (;;) {
-        // 1. shade and store rays that ended.
+        // 1. store the hit records of rays that ended.
         if (mode == MODE_DONE) {
             const std::uint32_t pix = std::uint32_t(id / pass.S);
             const std::uint32_t sl = std::uint32_t(id - std::uint64_t(pix) * pass.S);
-            pass.results[std::uint64_t(sl) * pass.npix + pix] = tone(v, ray.shade(v), ray.steps);
+            results[std::uint64_t(sl) * pass.npix + pix] = ray.record();
             my_steps += ray.steps;
             my_rej += ray.rej;
             my_zone += ray.zone;
@@ -352,7 +374,7 @@ __global__ void __launch_bounds__(256) trace_persistent(const View<T>* __restric
                         const std::uint32_t sl = std::uint32_t(id - std::uint64_t(pix) * pass.S);
                         const std::uint32_t gy = pix / v.width;
                         const std::uint32_t gx = pix - gy * v.width;
-                        const CamDir<T> cd = camera_dir(v, gx, gy, pass.s0 + sl);
+                        const CamDir<T> cd = camera_dir(v, gx, gy, off_x[sl], off_y[sl]);
                         mode = ray.init(v, cd, pass) ? MODE_ACTIVE : MODE_DONE;
                     }
                 }
@@ -384,12 +406,14 @@ __global__ void __launch_bounds__(128) trace_probe(const View<T>* __restrict__ g
     const std::uint64_t i = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
     Ray ray;
-    const CamDir<T> cd = camera_dir(v, gx[i], gy[i], s[i]);
+    T ox, oy;
+    sample_offset<T>(v.spp, s[i], ox, oy);
+    const CamDir<T> cd = camera_dir(v, gx[i], gy[i], ox, oy);
     if (ray.init(v, cd, pass)) {
         while (!ray.step(v, pass)) {
         }
     }
-    const V3<T> hdr = ray.shade(v);
+    const V3<T> hdr = shade_record(v, ray.record());
     if (hdr3 != nullptr) {
         hdr3[3 * i + 0] = float(hdr.x);
         hdr3[3 * i + 1] = float(hdr.y);
@@ -421,17 +445,24 @@ __device__ __forceinline__ void encode_pixel(float4 sum, float scale, std::uint3
     }
 }
 
-__global__ void accumulate_kernel(const float4* __restrict__ results, float4* __restrict__ acc, std::uint32_t npix,
-                                  std::uint32_t S, bool first, bool finalize, float scale, std::uint32_t format,
-                                  void* out) {
+template <class T>
+__global__ void __launch_bounds__(256) accumulate_kernel(const View<T>* __restrict__ g_view,
+                                                         const Rec<T>* __restrict__ results,
+                                                         float4* __restrict__ acc, std::uint32_t npix,
+                                                         std::uint32_t S, bool first, bool finalize, float scale,
+                                                         std::uint32_t format, void* out) {
+    __shared__ View<T> v;
+    load_view(v, g_view);
+    __syncthreads();
     const std::uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
     if (pix >= npix) return;
     float4 sum = first ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : acc[pix];
     for (std::uint32_t s = 0; s < S; ++s) {
-        const float4 q = results[std::uint64_t(s) * npix + pix];
-        sum.x = sum.x + q.x;
-        sum.y = sum.y + q.y;
-        sum.z = sum.z + q.z;
+        const Rec<T> rec = results[std::uint64_t(s) * npix + pix];
+        const V3<T> hdr = shade_record(v, rec);
+        sum.x = sum.x + float(aces1(hdr.x * v.exposure));
+        sum.y = sum.y + float(aces1(hdr.y * v.exposure));
+        sum.z = sum.z + float(aces1(hdr.z * v.exposure));
     }
     acc[pix] = sum;
     if (finalize) encode_pixel(sum, scale, format, out, pix);
@@ -545,12 +576,25 @@ cudaError_t launch_probe(const void* d_view, int metric, int precision, int inte
                     });
 }
 
-cudaError_t launch_accumulate(const float4* results, float4* acc, std::uint32_t npix, std::uint32_t S, bool first,
-                              bool finalize, float scale, std::uint32_t format, void* out, cudaStream_t st) {
+cudaError_t launch_accumulate(const void* d_view, int precision, const void* results, float4* acc,
+                              std::uint32_t npix, std::uint32_t S, bool first, bool finalize, float scale,
+                              std::uint32_t format, void* out, cudaStream_t st) {
     const unsigned threads = 256;
     const unsigned blocks = (npix + threads - 1) / threads;
-    accumulate_kernel<<<blocks, threads, 0, st>>>(results, acc, npix, S, first, finalize, scale, format, out);
+    if (precision == SGX_PRECISION_FP64) {
+        accumulate_kernel<double><<<blocks, threads, 0, st>>>(static_cast<const View<double>*>(d_view),
+                                                              static_cast<const Rec<double>*>(results), acc, npix,
+                                                              S, first, finalize, scale, format, out);
+    } else {
+        accumulate_kernel<float><<<blocks, threads, 0, st>>>(static_cast<const View<float>*>(d_view),
+                                                             static_cast<const Rec<float>*>(results), acc, npix, S,
+                                                             first, finalize, scale, format, out);
+    }
     return cudaGetLastError();
+}
+
+std::size_t record_bytes(int precision) {
+    return precision == SGX_PRECISION_FP64 ? sizeof(Rec<double>) : sizeof(Rec<float>);
 }
 
 cudaError_t launch_encode(const float4* acc, std::uint32_t npix, float scale, std::uint32_t format, void* out,
@@ -561,6 +605,6 @@ cudaError_t launch_encode(const float4* acc, std::uint32_t npix, float scale, st
     return cudaGetLastError();
 }
 
-int max_resident_blocks(int, int, int, bool, int) { return 0; }
+static_assert(sizeof(Rec<float>) == 16 && sizeof(Rec<double>) == 32, "hit record sizes");
 
 }  // namespace sgxk
