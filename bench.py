@@ -240,6 +240,34 @@ def precision_study(S, N, O, lib, r, u, d_out, stream, torch, main_opts) -> dict
     return out
 
 
+def batch_study(S, N, r, torch, launches: int = 3) -> dict:
+    """Config 4: the 64 views of workloads.batch_64_views(0) in one persistent
+    launch per batch, replayed from a CUDA graph, launch shape from the
+    autotuner (timed on the views with samples capped at 4)."""
+    views = S.workloads.batch_64_views(0)
+    rays = sum(v.width * v.height * v.supersample for v in views)
+    base = S.default_opts(integrator=N.INTEGRATOR_ADAPTIVE)
+    t0 = time.perf_counter()
+    best, tune_ms = S.autotune(r, views, base, sample_cap=4)
+    tune_s = time.perf_counter() - t0
+    out = {"views": len(views), "pixels": sum(v.width * v.height for v in views), "rays": rays,
+           "autotune": {"block_threads": best.block_threads, "refill_interval": best.refill_interval,
+                        "tile": [best.tile_w, best.tile_h], "probe_ms": tune_ms, "wall_s": tune_s}}
+    for name, opts in (("autotuned", best), ("default", base)):
+        b = S.Batch(r, views, opts)
+        b.launch()
+        b.wait()
+        ms = []
+        for _ in range(launches):
+            b.launch()
+            ms.append(b.wait().total_ms)
+        b.close()
+        out[f"{name}_ms_per_batch"] = float(np.median(ms))
+        out[f"{name}_mrays_s"] = rays / (np.median(ms) / 1e3) / 1e6
+    out["note"] = "one graph replay renders all 64 views (every sample); adaptive FP32, tol 1e-6; device time"
+    return out
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -249,6 +277,7 @@ def main() -> None:
     ap.add_argument("--e2e-steps", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-precision-study", action="store_true")
+    ap.add_argument("--no-batch-study", action="store_true")
     ap.add_argument("--rhs-form", type=int, default=0)
     ap.add_argument("--integrator", choices=["adaptive", "fixed"], default="adaptive")
     ap.add_argument("--precision", choices=["fp32", "mixed", "fp64"], default="fp32")
@@ -398,6 +427,9 @@ def main() -> None:
     study = None
     if not args.no_precision_study and args.precision == "fp32" and integ == N.INTEGRATOR_ADAPTIVE:
         study = precision_study(S, N, O, lib, r, u, d_out, stream, torch, opts)
+    batch = None
+    if not args.no_batch_study and args.precision == "fp32" and integ == N.INTEGRATOR_ADAPTIVE:
+        batch = batch_study(S, N, r, torch)
     cpu = None if args.no_cpu_baseline else cpu_baseline(S, O, u)
     clocks = clk.summary()
     wl = (f"kerr_a0.94_r40_i75_fov30_isco-30M_T1e4_{WIDTH}x{HEIGHT}_256spp_"
@@ -417,6 +449,7 @@ def main() -> None:
         "gpu_launches": 3 * args.steps,
         "budget_exhausted_rays": stats_acc["budget"],
         "precision_study": study,
+        "batched_views": batch,
     }
     print(json.dumps(line), flush=True)
     if world > 1:

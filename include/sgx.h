@@ -78,7 +78,8 @@ typedef struct sgx_render_opts {
     uint32_t refill_interval;/* steps between warp refills of finished rays; 0 = tuned */
     uint32_t rhs_form;       /* Kerr right-hand side: 0 = shared-reciprocal form (default),
                                 1 = the reference's division-for-division form */
-    uint32_t reserved[2];
+    uint32_t tile_w;         /* ray order: tiles of tile_w x tile_h pixels, samples innermost;  */
+    uint32_t tile_h;         /*   0 = whole rows (tile_w = width, tile_h = 1)                  */
 } sgx_render_opts;
 
 /* Counters of the last render (summed over its passes). */
@@ -207,6 +208,39 @@ sgx_status sgx_render_device(sgx_context* ctx, const sgx_uniforms* u, const sgx_
 sgx_status sgx_trace_samples(sgx_context* ctx, const sgx_uniforms* u, const sgx_render_opts* opts, uint64_t n,
                              const uint32_t* gx, const uint32_t* gy, const uint32_t* s, float* hdr3,
                              uint32_t* steps, uint32_t* term);
+
+/* ---- batched views ----------------------------------------------------------- */
+/* No counterpart in the reference (one view per launch there,
+ * render/cuda/cuda_backend.cu:140-152).  A batch is 1..SGX_BATCH_MAX_VIEWS
+ * views of one metric, each with its own size, scene, camera and samples per
+ * pixel, traced by ONE persistent launch over a shared ray queue; creation
+ * captures the whole frame set (counters, per-view constants, trace,
+ * accumulation, encode) into a CUDA graph that sgx_batch_launch replays.
+ * Frames are packed view after view in one device buffer (pixel offsets from
+ * sgx_batch_output), in `format` (RGBA8 sRGB or RGBA32F).  opts may be NULL;
+ * sample_begin/sample_count must be 0 (every sample of every view). */
+#define SGX_BATCH_MAX_VIEWS 128u
+typedef struct sgx_batch sgx_batch;
+sgx_status sgx_batch_create(sgx_context* ctx, const sgx_uniforms* views, uint32_t n, const sgx_render_opts* opts,
+                            uint32_t format, sgx_batch** out);
+/* New uniforms for the same views (each view keeps its size, samples and
+ * metric); the next launch renders them. */
+sgx_status sgx_batch_update(sgx_batch* b, const sgx_uniforms* views);
+/* Replays the graph on `stream` (NULL: the context's stream); asynchronous. */
+sgx_status sgx_batch_launch(sgx_batch* b, void* stream);
+/* Waits for the last launch; stats (may be NULL) get its counters and time. */
+sgx_status sgx_batch_wait(sgx_batch* b, sgx_render_stats* stats);
+/* Device pointer of the packed frames and the n + 1 pixel offsets of the views. */
+sgx_status sgx_batch_output(const sgx_batch* b, const void** d_frames, uint64_t* pixel_offsets);
+/* Copies view `view`'s frame to host memory (waits for the last launch). */
+sgx_status sgx_batch_capture(sgx_batch* b, uint32_t view, void* host_out, size_t bytes);
+void sgx_batch_destroy(sgx_batch* b);
+/* Launch-shape autotuner: times every combination of threads per block
+ * {128, 256}, refill interval {4, 8, 16, 32} and ray-order tile {rows, 8x4,
+ * 16x8, 32x2} on the views with samples capped at sample_cap (0: 4) and writes
+ * the fastest into *best (other fields from base); *best_ms gets its time. */
+sgx_status sgx_autotune(sgx_context* ctx, const sgx_uniforms* views, uint32_t n, const sgx_render_opts* base,
+                        uint32_t sample_cap, sgx_render_opts* best, float* best_ms);
 
 /* ---- allocation-free render ------------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device

@@ -5,14 +5,14 @@ sm_103a behind the C ABI of include/sgx.h); this package is its Python host
 mirror.  Build with ``singularity_gb300.build.build_library()``.
 """
 
-from . import _native
-from .backend import (CameraState, CudaBackend, ImageData, MetricType, RenderConfig, Renderer, Scene,
+from . import _native, workloads
+from .backend import (Batch, CameraState, CudaBackend, ImageData, MetricType, RenderConfig, Renderer, Scene,
                       SceneConfig, SceneLoadResult, SceneLoadStatus, SgxError, build_orbital_camera,
                       default_opts, kerr_isco_prograde, load_scene_config_from_file,
-                      load_scene_config_from_string, pack_uniforms)
+                      load_scene_config_from_string, pack_uniforms, autotune)
 
 __all__ = [
-    "CameraState", "CudaBackend", "ImageData", "MetricType", "RenderConfig", "Renderer", "Scene",
+    "Batch", "autotune", "workloads", "CameraState", "CudaBackend", "ImageData", "MetricType", "RenderConfig", "Renderer", "Scene",
     "SceneConfig", "SceneLoadResult", "SceneLoadStatus", "SgxError", "build_orbital_camera", "default_opts",
     "kerr_isco_prograde", "load_scene_config_from_file", "load_scene_config_from_string", "pack_uniforms",
     "_native",

@@ -78,7 +78,7 @@ class RenderOpts(C.Structure):
         ("fp64_zone", C.c_float),
         ("sample_begin", C.c_uint32), ("sample_count", C.c_uint32), ("block_threads", C.c_uint32),
         ("blocks_per_sm", C.c_uint32), ("refill_interval", C.c_uint32), ("rhs_form", C.c_uint32),
-        ("reserved", C.c_uint32 * 2),
+        ("tile_w", C.c_uint32), ("tile_h", C.c_uint32),
     ]
 
 
@@ -149,6 +149,16 @@ SIGNATURES = [
     ("sgx_render_device", C.c_int, [_P, C.POINTER(Uniforms), C.POINTER(RenderOpts), _P, C.c_uint32, _P]),
     ("sgx_render_noalloc", C.c_int, [C.POINTER(Uniforms), C.POINTER(RenderOpts), _P, C.c_uint32, _P, C.c_char_p,
                                      C.c_size_t]),
+    ("sgx_batch_create", C.c_int, [_P, C.POINTER(Uniforms), C.c_uint32, C.POINTER(RenderOpts), C.c_uint32,
+                                   C.POINTER(_P)]),
+    ("sgx_batch_update", C.c_int, [_P, C.POINTER(Uniforms)]),
+    ("sgx_batch_launch", C.c_int, [_P, _P]),
+    ("sgx_batch_wait", C.c_int, [_P, C.POINTER(RenderStats)]),
+    ("sgx_batch_output", C.c_int, [_P, C.POINTER(_P), C.POINTER(C.c_uint64)]),
+    ("sgx_batch_capture", C.c_int, [_P, C.c_uint32, _P, C.c_size_t]),
+    ("sgx_batch_destroy", None, [_P]),
+    ("sgx_autotune", C.c_int, [_P, C.POINTER(Uniforms), C.c_uint32, C.POINTER(RenderOpts), C.c_uint32,
+                               C.POINTER(RenderOpts), C.POINTER(C.c_float)]),
     ("sgx_measure_fp32_peak", C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
     ("sgx_trace_samples", C.c_int, [_P, C.POINTER(Uniforms), C.POINTER(RenderOpts), C.c_uint64, _U32P, _U32P,
                                     _U32P, _F32P, _U32P, _U32P]),

@@ -279,6 +279,71 @@ class Renderer:
         return hdr, steps, term
 
 
+class Batch:
+    """Many views in one persistent launch replayed from a CUDA graph (sgx_batch)."""
+
+    def __init__(self, renderer: Renderer, views, opts: Optional[N.RenderOpts] = None,
+                 fmt: int = N.FORMAT_RGBA8_SRGB):
+        self._r = renderer
+        self._lib = renderer._lib
+        self.n = len(views)
+        self.fmt = fmt
+        self._views = (N.Uniforms * self.n)(*views)
+        self.sizes = [(v.width, v.height) for v in views]
+        h = C.c_void_p()
+        st = self._lib.sgx_batch_create(renderer.handle, self._views, self.n,
+                                        C.byref(opts) if opts is not None else None, fmt, C.byref(h))
+        renderer._check(st)
+        self._h = h
+
+    def update(self, views) -> None:
+        self._views = (N.Uniforms * self.n)(*views)
+        self._r._check(self._lib.sgx_batch_update(self._h, self._views))
+
+    def launch(self, stream_ptr: int = 0) -> None:
+        self._r._check(self._lib.sgx_batch_launch(self._h, C.c_void_p(stream_ptr) if stream_ptr else None))
+
+    def wait(self) -> N.RenderStats:
+        s = N.RenderStats()
+        self._r._check(self._lib.sgx_batch_wait(self._h, C.byref(s)))
+        return s
+
+    def output(self):
+        ptr = C.c_void_p()
+        offs = (C.c_uint64 * (self.n + 1))()
+        self._r._check(self._lib.sgx_batch_output(self._h, C.byref(ptr), offs))
+        return ptr.value, list(offs)
+
+    def capture(self, view: int) -> np.ndarray:
+        w, h = self.sizes[view]
+        out = (np.empty((h, w, 4), dtype=np.uint8) if self.fmt == N.FORMAT_RGBA8_SRGB
+               else np.empty((h, w, 4), dtype=np.float32))
+        self._r._check(self._lib.sgx_batch_capture(self._h, view, out.ctypes.data_as(C.c_void_p), out.nbytes))
+        return out
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.sgx_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def autotune(renderer: Renderer, views, base: Optional[N.RenderOpts] = None, sample_cap: int = 4):
+    """Fastest launch shape for these views (sgx_autotune): (opts, ms)."""
+    arr = (N.Uniforms * len(views))(*views)
+    best = N.RenderOpts()
+    ms = C.c_float()
+    renderer._check(renderer._lib.sgx_autotune(renderer.handle, arr, len(views),
+                                                C.byref(base) if base is not None else None, sample_cap,
+                                                C.byref(best), C.byref(ms)))
+    return best, ms.value
+
+
 class CudaBackend:
     """The reference's CudaBackend (render/cuda/cuda_backend.hpp:17-46)."""
 

@@ -18,41 +18,13 @@
 #include <string>
 
 #include "sgx.h"
+#include "sgx_context.hpp"
 #include "sgx_kernels.hpp"
-
-struct sgx_context {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    std::uint32_t width = 0, height = 0;
-    void* d_image = nullptr;       // npix * 16 bytes
-    float4* d_acc = nullptr;       // npix
-    void* d_results = nullptr;     // results_cap bytes (hit records)
-    std::size_t results_cap = 0;
-    void* d_view = nullptr;
-    sgx_uniforms* d_u = nullptr;
-    sgxk::PassCounters* d_counters = nullptr;
-    sgxk::PassCounters* h_counters = nullptr;  // pinned
-    cudaEvent_t ev_begin = nullptr, ev_trace0 = nullptr, ev_trace1 = nullptr, ev_end = nullptr;
-    bool frame_valid = false;     // accumulator holds a complete frame
-    std::uint32_t frame_spp = 0;
-    std::uint32_t frame_format = SGX_FORMAT_RGBA8_SRGB;
-    std::uint32_t next_sample = 0;  // progressive passes: next expected sample
-    std::size_t workspace_budget = std::size_t(4) << 30;
-    sgx_render_stats stats{};
-    std::string err;
-};
 
 namespace {
 
-sgx_status fail(sgx_context* ctx, sgx_status s, const std::string& msg) {
-    if (ctx != nullptr) ctx->err = msg;
-    return s;
-}
-
-sgx_status cuda_fail(sgx_context* ctx, cudaError_t e, const char* where) {
-    return fail(ctx, e == cudaErrorMemoryAllocation ? SGX_ERR_OUT_OF_MEMORY : SGX_ERR_CUDA,
-                std::string(where) + ": " + cudaGetErrorString(e));
-}
+using sgx_internal::cuda_fail;
+using sgx_internal::fail;
 
 #define SGX_CUDA(ctx, call)                                  \
     do {                                                     \
@@ -122,6 +94,8 @@ sgx_status check_opts(sgx_context* c, const sgx_render_opts& o) {
     if (o.format > SGX_FORMAT_RGBA16F_HDR) return fail(c, SGX_ERR_INVALID_ARGUMENT, "unknown format");
     if (o.format == SGX_FORMAT_RGBA16F_HDR) return fail(c, SGX_ERR_UNSUPPORTED, "RGBA16F HDR output is not built");
     if (o.rhs_form > 1) return fail(c, SGX_ERR_INVALID_ARGUMENT, "unknown rhs_form");
+    if ((o.tile_w == 0) != (o.tile_h == 0) || o.tile_w > 4096 || o.tile_h > 4096)
+        return fail(c, SGX_ERR_INVALID_ARGUMENT, "tile_w and tile_h must both be 0 or both in [1, 4096]");
     if (o.integrator == SGX_INTEGRATOR_ADAPTIVE) {
         if (!(o.tolerance > 0.0f) || !(o.h_init_frac > 0.0f) || !(o.h_max_frac > 0.0f) || !(o.fp64_zone >= 0.0f))
             return fail(c, SGX_ERR_INVALID_ARGUMENT, "adaptive options must be positive (zone >= 0)");
@@ -156,18 +130,21 @@ sgx_status render_impl(sgx_context* c, const sgx_uniforms* u, const sgx_render_o
     if (s != SGX_OK) return s;
 
     SGX_CUDA(c, cudaMemcpyAsync(c->d_u, u, sizeof(sgx_uniforms), cudaMemcpyHostToDevice, st));
-    SGX_CUDA(c, sgxk::launch_setup_view(c->d_u, c->d_view, int(o.precision), st));
+    SGX_CUDA(c, sgxk::launch_setup_views(c->d_u, 1, c->d_view, int(o.precision), st));
+    const std::uint32_t tw = o.tile_w;
+    const std::uint32_t th = o.tile_h;
 
     sgx_render_stats acc{};
     for (std::uint32_t done = 0; done < count;) {
         const std::uint32_t n = std::min(S, count - done);
         const std::uint32_t s0 = begin + done;
+        sgxk::ViewPlan plan;
+        if (!sgxk::plan_views(u, 1, s0, n, tw, th, plan))
+            return fail(c, SGX_ERR_INVALID_ARGUMENT, "invalid pass or tile shape");
+        SGX_CUDA(c, cudaMemcpyAsync(c->d_words, plan.words, plan.word_count * 8, cudaMemcpyHostToDevice, st));
         sgxk::PassDesc pass{};
-        pass.total_rays = std::uint64_t(npix) * n;
-        pass.npix = npix;
-        pass.S = n;
-        pass.s0 = s0;
-        pass.refill = o.refill_interval == 0 ? 4u : o.refill_interval;
+        pass.vs = sgxk::make_view_set(plan, c->d_view, c->d_words);
+        pass.refill = o.refill_interval == 0 ? 16u : o.refill_interval;
         pass.results = c->d_results;
         pass.counters = c->d_counters;
         pass.tol = o.tolerance;
@@ -178,14 +155,13 @@ sgx_status render_impl(sgx_context* c, const sgx_uniforms* u, const sgx_render_o
         SGX_CUDA(c, cudaMemsetAsync(c->d_counters, 0, sizeof(sgxk::PassCounters), st));
         SGX_CUDA(c, cudaEventRecord(c->ev_trace0, st));
         sgxk::LaunchShape shape{int(o.block_threads), int(o.blocks_per_sm)};
-        SGX_CUDA(c, sgxk::launch_trace(c->d_view, int(u->metric_type), int(o.precision), int(o.integrator),
-                                       o.rhs_form == 0, pass, shape, st));
+        SGX_CUDA(c, sgxk::launch_trace(int(u->metric_type), int(o.precision), int(o.integrator), o.rhs_form == 0,
+                                       pass, shape, st));
         SGX_CUDA(c, cudaEventRecord(c->ev_trace1, st));
         const bool first = (s0 == 0);
         const bool finalize = (s0 + n == spp);
-        const float scale = 1.0f / float(spp);
-        SGX_CUDA(c, sgxk::launch_accumulate(c->d_view, int(o.precision), c->d_results, c->d_acc, npix, n, first,
-                                            finalize, scale, format, out, st));
+        SGX_CUDA(c, sgxk::launch_accumulate(int(o.precision), pass.vs, c->d_results, c->d_acc, first, finalize,
+                                            format, out, st));
         SGX_CUDA(c, cudaMemcpyAsync(c->h_counters, c->d_counters, sizeof(sgxk::PassCounters),
                                     cudaMemcpyDeviceToHost, st));
         SGX_CUDA(c, cudaEventRecord(c->ev_end, st));
@@ -208,6 +184,11 @@ sgx_status render_impl(sgx_context* c, const sgx_uniforms* u, const sgx_render_o
 }
 
 }  // namespace
+
+sgx_status sgx_internal::resolve_and_check(sgx_context* ctx, const sgx_render_opts* in, sgx_render_opts& out) {
+    out = resolve_opts(in);
+    return check_opts(ctx, out);
+}
 
 extern "C" {
 
@@ -250,8 +231,10 @@ sgx_status sgx_create(int device, sgx_context** out) {
     sgx_context* c = new sgx_context();
     c->device = device;
     bool ok = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) == cudaSuccess;
-    ok = ok && cudaMalloc(&c->d_view, sgxk::view_bytes()) == cudaSuccess;
-    ok = ok && cudaMalloc(reinterpret_cast<void**>(&c->d_u), sizeof(sgx_uniforms)) == cudaSuccess;
+    ok = ok && cudaMalloc(&c->d_view, sgxk::view_bytes() * sgxk::kMaxLaunchViews) == cudaSuccess;
+    ok = ok && cudaMalloc(reinterpret_cast<void**>(&c->d_u), sizeof(sgx_uniforms) * sgxk::kMaxLaunchViews) ==
+                   cudaSuccess;
+    ok = ok && cudaMalloc(reinterpret_cast<void**>(&c->d_words), sizeof(sgxk::ViewPlan::words)) == cudaSuccess;
     ok = ok && cudaMalloc(reinterpret_cast<void**>(&c->d_counters), sizeof(sgxk::PassCounters)) == cudaSuccess;
     ok = ok && cudaMallocHost(reinterpret_cast<void**>(&c->h_counters), sizeof(sgxk::PassCounters)) == cudaSuccess;
     ok = ok && cudaEventCreate(&c->ev_begin) == cudaSuccess && cudaEventCreate(&c->ev_trace0) == cudaSuccess
@@ -271,6 +254,7 @@ void sgx_destroy(sgx_context* c) {
     free_image(c);
     if (c->d_view) cudaFree(c->d_view);
     if (c->d_u) cudaFree(c->d_u);
+    if (c->d_words) cudaFree(c->d_words);
     if (c->d_counters) cudaFree(c->d_counters);
     if (c->h_counters) cudaFreeHost(c->h_counters);
     for (cudaEvent_t ev : {c->ev_begin, c->ev_trace0, c->ev_trace1, c->ev_end})
@@ -371,7 +355,7 @@ sgx_status sgx_trace_samples(sgx_context* c, const sgx_uniforms* u, const sgx_re
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_gy, gy, n * 4, cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_s, s, n * 4, cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_u, u, sizeof(sgx_uniforms), cudaMemcpyHostToDevice, c->stream);
-    if (e == cudaSuccess) e = sgxk::launch_setup_view(c->d_u, c->d_view, int(o.precision), c->stream);
+    if (e == cudaSuccess) e = sgxk::launch_setup_views(c->d_u, 1, c->d_view, int(o.precision), c->stream);
     if (e == cudaSuccess)
         e = sgxk::launch_probe(c->d_view, int(u->metric_type), int(o.precision), int(o.integrator), o.rhs_form == 0, n, d_gx,
                                d_gy, d_s, d_hdr, d_steps, d_term, o.tolerance, o.h_init_frac, o.h_max_frac,

@@ -1,0 +1,51 @@
+// singularity_gb300/csrc/sgx_context.hpp
+//
+// Internal definition of the C ABI's opaque sgx_context (shared by the
+// single-view entry points in sgx_api.cu and the batch entry points in
+// sgx_batch.cu).  Not installed.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "sgx.h"
+#include "sgx_kernels.hpp"
+
+struct sgx_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::uint32_t width = 0, height = 0;
+    void* d_image = nullptr;       // npix * 16 bytes
+    float4* d_acc = nullptr;       // npix
+    void* d_results = nullptr;     // results_cap bytes (hit records)
+    std::size_t results_cap = 0;
+    void* d_view = nullptr;            // kMaxLaunchViews view slots
+    sgx_uniforms* d_u = nullptr;       // kMaxLaunchViews uniform blocks
+    std::uint64_t* d_words = nullptr;  // view-set layout words
+    sgxk::PassCounters* d_counters = nullptr;
+    sgxk::PassCounters* h_counters = nullptr;  // pinned
+    cudaEvent_t ev_begin = nullptr, ev_trace0 = nullptr, ev_trace1 = nullptr, ev_end = nullptr;
+    bool frame_valid = false;     // accumulator holds a complete frame
+    std::uint32_t frame_spp = 0;
+    std::uint32_t frame_format = SGX_FORMAT_RGBA8_SRGB;
+    std::uint32_t next_sample = 0;  // progressive passes: next expected sample
+    std::size_t workspace_budget = std::size_t(4) << 30;
+    sgx_render_stats stats{};
+    std::string err;
+};
+
+
+namespace sgx_internal {
+inline sgx_status fail(sgx_context* ctx, sgx_status s, const std::string& msg) {
+    if (ctx != nullptr) ctx->err = msg;
+    return s;
+}
+inline sgx_status cuda_fail(sgx_context* ctx, cudaError_t e, const char* where) {
+    return fail(ctx, e == cudaErrorMemoryAllocation ? SGX_ERR_OUT_OF_MEMORY : SGX_ERR_CUDA,
+                std::string(where) + ": " + cudaGetErrorString(e));
+}
+// Validates and completes render options (defaults for absent fields).
+sgx_status resolve_and_check(sgx_context* ctx, const sgx_render_opts* in, sgx_render_opts& out);
+}  // namespace sgx_internal

@@ -23,14 +23,34 @@ struct PassCounters {
     unsigned long long pad[2];
 };
 
-// One pass of the trace: samples [s0, s0 + S) of every pixel of one view.
+// The views one launch traces (a single view for sgx_render, up to
+// kMaxLaunchViews for a batch), all device pointers into one layout block:
+//   ray_off[n+1]  offsets of each view in the ray-id space (padded pixels x S_v)
+//   rec_off[n]    offsets of each view's hit records (pixels x S_v)
+//   pix_off[n+1]  offsets of each view's pixels in the packed image/accumulator
+//   S[n]          samples of this pass per view
+struct ViewSet {
+    const void* views;  // View<T>[n]
+    const std::uint64_t* ray_off;
+    const std::uint64_t* rec_off;
+    const std::uint64_t* pix_off;
+    const std::uint32_t* S;
+    std::uint32_t n;
+    std::uint32_t max_S;
+    std::uint32_t s0;      // first Halton sample of the pass (progressive single view); 0 for batches
+    std::uint32_t tile_w;  // ray-id order: tiles of tile_w x tile_h pixels, samples innermost; 0 = rows
+    std::uint32_t tile_h;
+    std::uint64_t total_rays;
+    std::uint64_t total_pix;
+};
+
+constexpr std::uint32_t kMaxLaunchViews = 128;
+constexpr std::uint32_t kMaxPassSamplesHost = 1024;
+
 struct PassDesc {
-    std::uint64_t total_rays;  // npix * S
-    std::uint32_t npix;
-    std::uint32_t S;
-    std::uint32_t s0;
-    std::uint32_t refill;       // steps between refills
-    void* results;              // [S][npix] hit records, record_bytes(precision) each
+    ViewSet vs;
+    std::uint32_t refill;  // steps between refills
+    void* results;         // hit records, record_bytes(precision) each
     PassCounters* counters;
     // adaptive options
     float tol, h_init_frac, h_max_frac, zone;
@@ -41,36 +61,50 @@ struct LaunchShape {
     int blocks_per_sm;
 };
 
-// Prepares the per-view constants (device) from a device copy of the uniforms.
-cudaError_t launch_setup_view(const sgx_uniforms* d_u, void* d_view, int precision, cudaStream_t st);
+// Host plan of a ViewSet: the layout block's contents (to copy to the device
+// as one array of 64-bit words) and the totals.  S_pass == 0 -> every view's
+// own samples per pixel.
+struct ViewPlan {
+    std::uint32_t n = 0, max_S = 0, s0 = 0, tile_w = 0, tile_h = 0;
+    std::uint64_t total_rays = 0, total_pix = 0, total_recs = 0;
+    std::uint64_t words[4 * kMaxLaunchViews + 2] = {};  // ray_off | rec_off | pix_off | S (packed 2 per word)
+    std::size_t word_count = 0;
+};
+bool plan_views(const sgx_uniforms* u, std::uint32_t n, std::uint32_t s0, std::uint32_t S_pass, std::uint32_t tile_w,
+                std::uint32_t tile_h, ViewPlan& plan);
+// Device ViewSet over a layout block that holds plan.words at d_words and
+// the views at d_views.
+ViewSet make_view_set(const ViewPlan& plan, const void* d_views, const std::uint64_t* d_words);
 
-// Persistent tracer.  precision: sgx_precision; integrator: sgx_integrator.
-cudaError_t launch_trace(const void* d_view, int metric, int precision, int integrator, bool fast_math,
-                         const PassDesc& pass, LaunchShape shape, cudaStream_t st);
+// Per-view constants (device) from device copies of the uniforms, one thread each.
+cudaError_t launch_setup_views(const sgx_uniforms* d_u, std::uint32_t n, void* d_views, int precision,
+                               cudaStream_t st);
 
-// Per-sample probe (parity tests): n samples, device arrays.
+// Persistent tracer over a ViewSet.  precision: sgx_precision; integrator: sgx_integrator.
+cudaError_t launch_trace(int metric, int precision, int integrator, bool fast_math, const PassDesc& pass,
+                         LaunchShape shape, cudaStream_t st);
+
+// Per-sample probe (parity tests) of a single view: n samples, device arrays.
 cudaError_t launch_probe(const void* d_view, int metric, int precision, int integrator, bool fast_math,
                          std::uint64_t n, const std::uint32_t* gx, const std::uint32_t* gy, const std::uint32_t* s,
                          float* hdr3, std::uint32_t* steps, std::uint32_t* term, float tol, float h_init_frac,
                          float h_max_frac, float zone, cudaStream_t st);
 
-// Shades the pass's hit records and adds them in sample order into acc
-// (float4 per pixel); when `finalize`, also writes the frame in `format` to
-// out (scale = 1/spp).
-cudaError_t launch_accumulate(const void* d_view, int precision, const void* results, float4* acc,
-                              std::uint32_t npix, std::uint32_t S, bool first, bool finalize, float scale,
-                              std::uint32_t format, void* out, cudaStream_t st);
+// Shades a pass's hit records and adds them in sample order into acc (float4
+// per pixel, packed over views); when `finalize`, also writes every view's
+// frame in `format` to out (packed like acc; scale 1/spp of each view).
+cudaError_t launch_accumulate(int precision, const ViewSet& vs, const void* results, float4* acc, bool first,
+                              bool finalize, std::uint32_t format, void* out, cudaStream_t st);
 
-// Bytes of one hit record (16 for FP32 and mixed, 32 for FP64).
-std::size_t record_bytes(int precision);
-
-// Samples one pass may hold (the per-block offset table).
-constexpr std::uint32_t kMaxPassSamplesHost = 1024;
-
-// Re-encodes the accumulated frame (acc, float4 mean-sum) in another format.
+// Re-encodes an accumulated single-view frame (acc, float4 mean-sum) in another format.
 cudaError_t launch_encode(const float4* acc, std::uint32_t npix, float scale, std::uint32_t format, void* out,
                           cudaStream_t st);
 
+// Bytes of one hit record (16 for FP32 and mixed, 32 for FP64).
+std::size_t record_bytes(int precision);
+// Bytes of one View<T> of the precision (256-aligned slot).
 std::size_t view_bytes();
+// Bytes of output per pixel in a format.
+std::size_t format_bytes(std::uint32_t format);
 
 }  // namespace sgxk

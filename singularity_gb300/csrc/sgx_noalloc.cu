@@ -42,10 +42,11 @@
 
 namespace {
 
-constexpr std::size_t kHeaderBytes = 4096;  // counters | uniforms | view constants
+constexpr std::size_t kHeaderBytes = 4096;  // counters | uniforms | view constants | view-set words
 constexpr std::size_t kCountersOff = 0;
 constexpr std::size_t kUniformsOff = 256;
 constexpr std::size_t kViewOff = 512;
+constexpr std::size_t kWordsOff = 2048;
 constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[SGX_NOALLOC_SCRATCH_BYTES];
@@ -96,7 +97,7 @@ extern "C" sgx_status sgx_render_noalloc(const sgx_uniforms* u, const sgx_render
         set_err(err, err_len, "sgx_render_noalloc: width/height must be > 0 and metric_type known");
         return SGX_ERR_INVALID_ARGUMENT;
     }
-    if (kViewOff + sgxk::view_bytes() > kHeaderBytes) {
+    if (kViewOff + sgxk::view_bytes() > kWordsOff) {
         set_err(err, err_len, "sgx_render_noalloc: internal header layout too small");
         return SGX_ERR_UNSUPPORTED;
     }
@@ -147,16 +148,19 @@ extern "C" sgx_status sgx_render_noalloc(const sgx_uniforms* u, const sgx_render
     auto* counters = reinterpret_cast<sgxk::PassCounters*>(base + kCountersOff);
     auto* d_u = reinterpret_cast<sgx_uniforms*>(base + kUniformsOff);
     void* d_view = base + kViewOff;
+    auto* d_words = reinterpret_cast<std::uint64_t*>(base + kWordsOff);
     auto* acc = reinterpret_cast<float4*>(base + kHeaderBytes);
     void* results = acc + npix;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
 
+    sgxk::ViewPlan plan;
+    if (!sgxk::plan_views(u, 1, 0, spp, 0, 0, plan)) {
+        set_err(err, err_len, "sgx_render_noalloc: invalid frame");
+        return SGX_ERR_INVALID_ARGUMENT;
+    }
     sgxk::PassDesc pass{};
-    pass.total_rays = npix * spp;
-    pass.npix = std::uint32_t(npix);
-    pass.S = spp;
-    pass.s0 = 0;
-    pass.refill = o.refill_interval == 0 ? 4u : o.refill_interval;
+    pass.vs = sgxk::make_view_set(plan, d_view, d_words);
+    pass.refill = o.refill_interval == 0 ? 16u : o.refill_interval;
     pass.results = results;
     pass.counters = counters;
     pass.tol = o.tolerance;
@@ -166,14 +170,14 @@ extern "C" sgx_status sgx_render_noalloc(const sgx_uniforms* u, const sgx_render
     sgxk::LaunchShape shape{int(o.block_threads), int(o.blocks_per_sm)};
 
     e = cudaMemcpyAsync(d_u, u, sizeof(sgx_uniforms), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_words, plan.words, plan.word_count * 8, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(counters, 0, sizeof(sgxk::PassCounters), st);
-    if (e == cudaSuccess) e = sgxk::launch_setup_view(d_u, d_view, int(o.precision), st);
+    if (e == cudaSuccess) e = sgxk::launch_setup_views(d_u, 1, d_view, int(o.precision), st);
     if (e == cudaSuccess)
-        e = sgxk::launch_trace(d_view, int(u->metric_type), int(o.precision), int(o.integrator), o.rhs_form == 0,
-                               pass, shape, st);
+        e = sgxk::launch_trace(int(u->metric_type), int(o.precision), int(o.integrator), o.rhs_form == 0, pass,
+                               shape, st);
     if (e == cudaSuccess)
-        e = sgxk::launch_accumulate(d_view, int(o.precision), results, acc, std::uint32_t(npix), spp, true, true,
-                                    1.0f / float(spp), format, d_out, st);
+        e = sgxk::launch_accumulate(int(o.precision), pass.vs, results, acc, true, true, format, d_out, st);
     if (e != cudaSuccess) {
         char buf[256];
         std::snprintf(buf, sizeof(buf), "sgx_render_noalloc: %s", cudaGetErrorString(e));

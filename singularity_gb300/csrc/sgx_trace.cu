@@ -303,19 +303,11 @@ template <class T> __device__ __forceinline__ V3<T> shade_record(const View<T>& 
 }
 
 template <class T> __device__ __forceinline__ void load_view(View<T>& dst, const View<T>* src) {
-    // Cooperative copy of the view constants into shared memory.
+    // Cooperative copy of one view's constants into shared memory.
     const int words = int(sizeof(View<T>) / 4);
     const std::uint32_t* s = reinterpret_cast<const std::uint32_t*>(src);
     std::uint32_t* d = reinterpret_cast<std::uint32_t*>(&dst);
     for (int i = threadIdx.x; i < words; i += blockDim.x) d[i] = s[i];
-}
-
-// Sub-pixel offsets of the pass's samples [s0, s0 + S), one table per block.
-constexpr std::uint32_t kMaxPassSamples = 1024;
-
-template <class T>
-__device__ __forceinline__ void load_offsets(T* ox, T* oy, const View<T>& v, const PassDesc& pass) {
-    for (std::uint32_t i = threadIdx.x; i < pass.S; i += blockDim.x) sample_offset<T>(v.spp, pass.s0 + i, ox[i], oy[i]);
 }
 
 // Warp-aggregated add of a per-lane counter.
@@ -325,15 +317,89 @@ __device__ __forceinline__ void warp_add(unsigned long long* dst, unsigned long 
     if ((threadIdx.x & 31) == 0 && v != 0ull) atomicAdd(dst, v);
 }
 
+// Shared-memory image of a ViewSet: the views, the offset tables and the
+// pass's Halton offsets.  Host and device agree on the layout through
+// set_smem_bytes().
+template <class T> struct SmemSet {
+    View<T>* views;
+    std::uint64_t* ray_off;  // n + 1
+    std::uint64_t* rec_off;  // n
+    std::uint64_t* pix_off;  // n + 1
+    std::uint32_t* S;        // n
+    T* off_x;                // max_S
+    T* off_y;
+};
+
+__host__ __device__ constexpr std::size_t align16(std::size_t x) { return (x + 15) & ~std::size_t(15); }
+
+template <class T> __host__ __device__ std::size_t set_smem_bytes(std::uint32_t n, std::uint32_t max_S) {
+    return align16(n * sizeof(View<T>)) + align16((n + 1) * 8) + align16(n * 8) + align16((n + 1) * 8) +
+           align16(n * 4) + 2 * align16(max_S * sizeof(T));
+}
+
+template <class T> __device__ __forceinline__ SmemSet<T> carve(unsigned char* base, std::uint32_t n, std::uint32_t max_S) {
+    SmemSet<T> m;
+    std::size_t o = 0;
+    m.views = reinterpret_cast<View<T>*>(base + o);
+    o += align16(n * sizeof(View<T>));
+    m.ray_off = reinterpret_cast<std::uint64_t*>(base + o);
+    o += align16((n + 1) * 8);
+    m.rec_off = reinterpret_cast<std::uint64_t*>(base + o);
+    o += align16(n * 8);
+    m.pix_off = reinterpret_cast<std::uint64_t*>(base + o);
+    o += align16((n + 1) * 8);
+    m.S = reinterpret_cast<std::uint32_t*>(base + o);
+    o += align16(n * 4);
+    m.off_x = reinterpret_cast<T*>(base + o);
+    o += align16(max_S * sizeof(T));
+    m.off_y = reinterpret_cast<T*>(base + o);
+    return m;
+}
+
+template <class T> __device__ void load_set(const SmemSet<T>& m, const ViewSet& vs, bool offsets) {
+    const int words = int(vs.n * sizeof(View<T>) / 4);
+    const std::uint32_t* src = static_cast<const std::uint32_t*>(vs.views);
+    std::uint32_t* dst = reinterpret_cast<std::uint32_t*>(m.views);
+    for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+    for (std::uint32_t i = threadIdx.x; i <= vs.n; i += blockDim.x) {
+        m.ray_off[i] = vs.ray_off[i];
+        m.pix_off[i] = vs.pix_off[i];
+        if (i < vs.n) {
+            m.rec_off[i] = vs.rec_off[i];
+            m.S[i] = vs.S[i];
+        }
+    }
+    if (offsets) {
+        // Halton(s0 + i + 1) in bases 2 and 3 (spp == 1 views use the pixel
+        // centre instead, at the point of use).
+        for (std::uint32_t i = threadIdx.x; i < vs.max_S; i += blockDim.x)
+            sample_offset<T>(2u, vs.s0 + i, m.off_x[i], m.off_y[i]);
+    }
+}
+
+// Index of the last offset <= x in off[0..n] (off[0] = 0, off[n] = total).
+__device__ __forceinline__ std::uint32_t find_view(const std::uint64_t* off, std::uint32_t n, std::uint64_t x) {
+    std::uint32_t lo = 0, hi = n;  // invariant: off[lo] <= x < off[hi]
+    while (hi - lo > 1u) {
+        const std::uint32_t mid = (lo + hi) >> 1;
+        if (off[mid] <= x) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
 enum : int { MODE_IDLE = 0, MODE_ACTIVE = 1, MODE_DONE = 2 };
 
+// The persistent tracer over a set of views.  Ray ids enumerate, view by
+// view, tiles of tile_w x tile_h pixels (padded to whole tiles), the pixels
+// of a tile row-major, and a pixel's samples innermost; ids that land in the
+// padding carry no work.
 template <class T, class Ray>
-__global__ void __launch_bounds__(256) trace_persistent(const View<T>* __restrict__ g_view, PassDesc pass) {
-    __shared__ View<T> v;
-    __shared__ T off_x[kMaxPassSamples], off_y[kMaxPassSamples];
-    load_view(v, g_view);
-    __syncthreads();
-    load_offsets(off_x, off_y, v, pass);
+__global__ void __launch_bounds__(256) trace_persistent(PassDesc pass) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const ViewSet& vs = pass.vs;
+    const SmemSet<T> m = carve<T>(smem_raw, vs.n, vs.max_S);
+    load_set(m, vs, true);
     __syncthreads();
     Rec<T>* __restrict__ results = static_cast<Rec<T>*>(pass.results);
 
@@ -341,16 +407,15 @@ __global__ void __launch_bounds__(256) trace_persistent(const View<T>* __restric
     const unsigned lt_mask = (1u << lane) - 1u;
     Ray ray;
     int mode = MODE_IDLE;
-    std::uint64_t id = 0;
+    std::uint32_t vid = 0;
+    std::uint64_t rec = 0;
     bool exhausted = false;
     unsigned long long my_steps = 0, my_budget = 0, my_rays = 0, my_rej = 0, my_zone = 0;
 
     for (;;) {
         // 1. store the hit records of rays that ended.
         if (mode == MODE_DONE) {
-            const std::uint32_t pix = std::uint32_t(id / pass.S);
-            const std::uint32_t sl = std::uint32_t(id - std::uint64_t(pix) * pass.S);
-            results[std::uint64_t(sl) * pass.npix + pix] = ray.record();
+            results[rec] = ray.record();
             my_steps += ray.steps;
             my_rej += ray.rej;
             my_zone += ray.zone;
@@ -368,21 +433,44 @@ __global__ void __launch_bounds__(256) trace_persistent(const View<T>* __restric
                 if (int(lane) == leader) base = atomicAdd(&pass.counters->next_ray, (unsigned long long)n);
                 base = __shfl_sync(kFull, base, leader);
                 if (mode == MODE_IDLE) {
-                    id = base + __popc(idle & lt_mask);
-                    if (id < pass.total_rays) {
-                        const std::uint32_t pix = std::uint32_t(id / pass.S);
-                        const std::uint32_t sl = std::uint32_t(id - std::uint64_t(pix) * pass.S);
-                        const std::uint32_t gy = pix / v.width;
-                        const std::uint32_t gx = pix - gy * v.width;
-                        const CamDir<T> cd = camera_dir(v, gx, gy, off_x[sl], off_y[sl]);
-                        mode = ray.init(v, cd, pass) ? MODE_ACTIVE : MODE_DONE;
+                    const std::uint64_t id = base + __popc(idle & lt_mask);
+                    if (id < vs.total_rays) {
+                        vid = vs.n == 1u ? 0u : find_view(m.ray_off, vs.n, id);
+                        const View<T>& v = m.views[vid];
+                        const std::uint32_t Sv = m.S[vid];
+                        const std::uint64_t local = id - m.ray_off[vid];
+                        const std::uint64_t seq = local / Sv;
+                        const std::uint32_t sl = std::uint32_t(local - seq * Sv);
+                        // tile_w == 0: whole rows of this view (no padding)
+                        const std::uint32_t tw = vs.tile_w == 0u ? v.width : vs.tile_w;
+                        const std::uint32_t th = vs.tile_w == 0u ? 1u : vs.tile_h;
+                        const std::uint32_t tpix = tw * th;
+                        const std::uint32_t tiles_x = (v.width + tw - 1u) / tw;
+                        const std::uint32_t tile = std::uint32_t(seq / tpix);
+                        const std::uint32_t within = std::uint32_t(seq - std::uint64_t(tile) * tpix);
+                        const std::uint32_t ty = tile / tiles_x;
+                        const std::uint32_t wy = within / tw;
+                        const std::uint32_t gx = (tile - ty * tiles_x) * tw + (within - wy * tw);
+                        const std::uint32_t gy = ty * th + wy;
+                        if (gx < v.width && gy < v.height) {
+                            rec = m.rec_off[vid] + std::uint64_t(sl) * (std::uint64_t(v.width) * v.height) +
+                                  std::uint64_t(gy) * v.width + gx;
+                            const T ox = v.spp == 1u ? DLIT(0.5) : m.off_x[sl];
+                            const T oy = v.spp == 1u ? DLIT(0.5) : m.off_y[sl];
+                            const CamDir<T> cd = camera_dir(v, gx, gy, ox, oy);
+                            mode = ray.init(v, cd, pass) ? MODE_ACTIVE : MODE_DONE;
+                        }
                     }
                 }
-                if (base + n >= pass.total_rays) exhausted = true;
+                if (base + n >= vs.total_rays) exhausted = true;
             }
         }
-        if (__ballot_sync(kFull, mode != MODE_IDLE) == 0u) break;
+        if (__ballot_sync(kFull, mode != MODE_IDLE) == 0u) {
+            if (exhausted) break;
+            continue;  // every id this round fell in tile padding
+        }
         // 3. integrate.
+        const View<T>& v = m.views[vid];
         for (std::uint32_t j = 0; j < pass.refill; ++j) {
             if (mode == MODE_ACTIVE && ray.step(v, pass)) mode = MODE_DONE;
             if (__all_sync(kFull, mode != MODE_ACTIVE)) break;
@@ -423,15 +511,14 @@ __global__ void __launch_bounds__(128) trace_probe(const View<T>* __restrict__ g
     if (term != nullptr) term[i] = ray.term;
 }
 
-template <class T> __global__ void setup_view(const sgx_uniforms* u, View<T>* out) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) *out = make_view<T>(*u);
+template <class T> __global__ void setup_views(const sgx_uniforms* u, std::uint32_t n, View<T>* out) {
+    const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = make_view<T>(u[i]);
 }
 
-// Ordered per-pixel sum over the pass's samples (the reference's
-// `ldr = ldr + aces(...)` loop, geodesic_kernel.cu:492-501), then the final
-// encode (geodesic_kernel.cu:502-509) on the last pass.
+// Final encode of a pixel's mean (geodesic_kernel.cu:502-509).
 __device__ __forceinline__ void encode_pixel(float4 sum, float scale, std::uint32_t format, void* out,
-                                             std::uint32_t pix) {
+                                             std::uint64_t pix) {
     const float r = sum.x * scale, g = sum.y * scale, b = sum.z * scale;
     if (format == SGX_FORMAT_RGBA8_SRGB) {
         uchar4 o;
@@ -445,27 +532,35 @@ __device__ __forceinline__ void encode_pixel(float4 sum, float scale, std::uint3
     }
 }
 
+// Shades each hit record of the pass and adds it to the pixel's sum in sample
+// order (the reference's `ldr = ldr + aces(hdr * exposure)`,
+// geodesic_kernel.cu:492-501); the last pass scales by 1/spp and encodes.
 template <class T>
-__global__ void __launch_bounds__(256) accumulate_kernel(const View<T>* __restrict__ g_view,
-                                                         const Rec<T>* __restrict__ results,
-                                                         float4* __restrict__ acc, std::uint32_t npix,
-                                                         std::uint32_t S, bool first, bool finalize, float scale,
+__global__ void __launch_bounds__(256) accumulate_kernel(ViewSet vs, const Rec<T>* __restrict__ results,
+                                                         float4* __restrict__ acc, bool first, bool finalize,
                                                          std::uint32_t format, void* out) {
-    __shared__ View<T> v;
-    load_view(v, g_view);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const SmemSet<T> m = carve<T>(smem_raw, vs.n, 0);
+    load_set(m, vs, false);
     __syncthreads();
-    const std::uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pix >= npix) return;
-    float4 sum = first ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : acc[pix];
+    const std::uint64_t p = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (p >= vs.total_pix) return;
+    const std::uint32_t vid = vs.n == 1u ? 0u : find_view(m.pix_off, vs.n, p);
+    const View<T>& v = m.views[vid];
+    const std::uint64_t pix = p - m.pix_off[vid];
+    const std::uint64_t npix = std::uint64_t(v.width) * v.height;
+    const std::uint64_t base = m.rec_off[vid] + pix;
+    const std::uint32_t S = m.S[vid];
+    float4 sum = first ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : acc[p];
     for (std::uint32_t s = 0; s < S; ++s) {
-        const Rec<T> rec = results[std::uint64_t(s) * npix + pix];
+        const Rec<T> rec = results[base + std::uint64_t(s) * npix];
         const V3<T> hdr = shade_record(v, rec);
         sum.x = sum.x + float(aces1(hdr.x * v.exposure));
         sum.y = sum.y + float(aces1(hdr.y * v.exposure));
         sum.z = sum.z + float(aces1(hdr.z * v.exposure));
     }
-    acc[pix] = sum;
-    if (finalize) encode_pixel(sum, scale, format, out, pix);
+    acc[p] = sum;
+    if (finalize) encode_pixel(sum, 1.0f / float(v.spp), format, out, p);
 }
 
 __global__ void encode_kernel(const float4* __restrict__ acc, std::uint32_t npix, float scale, std::uint32_t format,
@@ -479,22 +574,25 @@ __global__ void encode_kernel(const float4* __restrict__ acc, std::uint32_t npix
 // Dispatch
 // ---------------------------------------------------------------------------
 template <class T, template <class, int> class Policy, int FL>
-cudaError_t run_persistent(const void* d_view, const PassDesc& pass, LaunchShape shape, cudaStream_t st) {
+cudaError_t run_persistent(const PassDesc& pass, LaunchShape shape, cudaStream_t st) {
     auto kern = trace_persistent<T, Policy<T, FL>>;
+    const std::size_t smem = set_smem_bytes<T>(pass.vs.n, pass.vs.max_S);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
     int dev = 0;
     cudaGetDevice(&dev);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int threads = shape.block_threads > 0 ? shape.block_threads : 256;
     int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
     if (e != cudaSuccess) return e;
     if (shape.blocks_per_sm > 0 && shape.blocks_per_sm < per_sm) per_sm = shape.blocks_per_sm;
     if (per_sm < 1) per_sm = 1;
     std::uint64_t blocks = std::uint64_t(sms) * per_sm;
-    const std::uint64_t need = (pass.total_rays + threads - 1) / threads;
+    const std::uint64_t need = (pass.vs.total_rays + threads - 1) / threads;
     if (need < blocks) blocks = need > 0 ? need : 1;
-    kern<<<unsigned(blocks), threads, 0, st>>>(static_cast<const View<T>*>(d_view), pass);
+    kern<<<unsigned(blocks), threads, smem, st>>>(pass);
     return cudaGetLastError();
 }
 
@@ -544,20 +642,88 @@ std::size_t view_bytes() {
     return ((a > b ? a : b) + 255) / 256 * 256;
 }
 
-cudaError_t launch_setup_view(const sgx_uniforms* d_u, void* d_view, int precision, cudaStream_t st) {
+std::size_t record_bytes(int precision) {
+    return precision == SGX_PRECISION_FP64 ? sizeof(Rec<double>) : sizeof(Rec<float>);
+}
+
+std::size_t format_bytes(std::uint32_t format) {
+    return format == SGX_FORMAT_RGBA8_SRGB ? 4 : (format == SGX_FORMAT_RGBA16F_HDR ? 8 : 16);
+}
+
+bool plan_views(const sgx_uniforms* u, std::uint32_t n, std::uint32_t s0, std::uint32_t S_pass, std::uint32_t tile_w,
+                std::uint32_t tile_h, ViewPlan& plan) {
+    if (n == 0 || n > kMaxLaunchViews || (tile_w != 0 && tile_h == 0)) return false;
+    plan = ViewPlan{};
+    plan.n = n;
+    plan.s0 = s0;
+    plan.tile_w = tile_w;
+    plan.tile_h = tile_h;
+    std::uint64_t* ray_off = plan.words;
+    std::uint64_t* rec_off = ray_off + (n + 1);
+    std::uint64_t* pix_off = rec_off + n;
+    std::uint32_t* S = reinterpret_cast<std::uint32_t*>(pix_off + (n + 1));
+    std::uint64_t r = 0, q = 0, px = 0;
+    for (std::uint32_t i = 0; i < n; ++i) {
+        const std::uint32_t spp = u[i].supersample < 1u ? 1u : (u[i].supersample > 1024u ? 1024u : u[i].supersample);
+        const std::uint32_t Sv = S_pass == 0 ? spp : S_pass;
+        if (Sv == 0 || Sv > kMaxPassSamplesHost) return false;
+        const std::uint64_t w = u[i].width, h = u[i].height;
+        // tile_w == 0: whole rows of each view, no padding.
+        const std::uint64_t tw = tile_w == 0 ? w : tile_w, th = tile_w == 0 ? 1 : tile_h;
+        const std::uint64_t padded = ((w + tw - 1) / tw) * tw * (((h + th - 1) / th) * th);
+        ray_off[i] = r;
+        rec_off[i] = q;
+        pix_off[i] = px;
+        S[i] = Sv;
+        r += padded * Sv;
+        q += w * h * Sv;
+        px += w * h;
+        if (Sv > plan.max_S) plan.max_S = Sv;
+    }
+    ray_off[n] = r;
+    pix_off[n] = px;
+    plan.total_rays = r;
+    plan.total_recs = q;
+    plan.total_pix = px;
+    plan.word_count = (n + 1) + n + (n + 1) + (n + 1) / 2;
+    return true;
+}
+
+ViewSet make_view_set(const ViewPlan& plan, const void* d_views, const std::uint64_t* d_words) {
+    ViewSet vs{};
+    const std::uint32_t n = plan.n;
+    vs.views = d_views;
+    vs.ray_off = d_words;
+    vs.rec_off = d_words + (n + 1);
+    vs.pix_off = d_words + (n + 1) + n;
+    vs.S = reinterpret_cast<const std::uint32_t*>(d_words + (n + 1) + n + (n + 1));
+    vs.n = n;
+    vs.max_S = plan.max_S;
+    vs.s0 = plan.s0;
+    vs.tile_w = plan.tile_w;
+    vs.tile_h = plan.tile_h;
+    vs.total_rays = plan.total_rays;
+    vs.total_pix = plan.total_pix;
+    return vs;
+}
+
+cudaError_t launch_setup_views(const sgx_uniforms* d_u, std::uint32_t n, void* d_views, int precision,
+                               cudaStream_t st) {
+    const unsigned threads = 64;
+    const unsigned blocks = (n + threads - 1) / threads;
     if (precision == SGX_PRECISION_FP64) {
-        setup_view<double><<<1, 32, 0, st>>>(d_u, static_cast<View<double>*>(d_view));
+        setup_views<double><<<blocks, threads, 0, st>>>(d_u, n, static_cast<View<double>*>(d_views));
     } else {
-        setup_view<float><<<1, 32, 0, st>>>(d_u, static_cast<View<float>*>(d_view));
+        setup_views<float><<<blocks, threads, 0, st>>>(d_u, n, static_cast<View<float>*>(d_views));
     }
     return cudaGetLastError();
 }
 
-cudaError_t launch_trace(const void* d_view, int metric, int precision, int integrator, bool fast_math,
-                         const PassDesc& pass, LaunchShape shape, cudaStream_t st) {
+cudaError_t launch_trace(int metric, int precision, int integrator, bool fast_math, const PassDesc& pass,
+                         LaunchShape shape, cudaStream_t st) {
     return dispatch(metric, precision, integrator, fast_math,
                     [&]<class T, template <class, int> class Policy, int FL>() {
-                        return run_persistent<T, Policy, FL>(d_view, pass, shape, st);
+                        return run_persistent<T, Policy, FL>(pass, shape, st);
                     });
 }
 
@@ -576,25 +742,20 @@ cudaError_t launch_probe(const void* d_view, int metric, int precision, int inte
                     });
 }
 
-cudaError_t launch_accumulate(const void* d_view, int precision, const void* results, float4* acc,
-                              std::uint32_t npix, std::uint32_t S, bool first, bool finalize, float scale,
-                              std::uint32_t format, void* out, cudaStream_t st) {
+cudaError_t launch_accumulate(int precision, const ViewSet& vs, const void* results, float4* acc, bool first,
+                              bool finalize, std::uint32_t format, void* out, cudaStream_t st) {
     const unsigned threads = 256;
-    const unsigned blocks = (npix + threads - 1) / threads;
+    const std::uint64_t blocks = (vs.total_pix + threads - 1) / threads;
     if (precision == SGX_PRECISION_FP64) {
-        accumulate_kernel<double><<<blocks, threads, 0, st>>>(static_cast<const View<double>*>(d_view),
-                                                              static_cast<const Rec<double>*>(results), acc, npix,
-                                                              S, first, finalize, scale, format, out);
+        const std::size_t smem = set_smem_bytes<double>(vs.n, 0);
+        accumulate_kernel<double><<<unsigned(blocks), threads, smem, st>>>(
+            vs, static_cast<const Rec<double>*>(results), acc, first, finalize, format, out);
     } else {
-        accumulate_kernel<float><<<blocks, threads, 0, st>>>(static_cast<const View<float>*>(d_view),
-                                                             static_cast<const Rec<float>*>(results), acc, npix, S,
-                                                             first, finalize, scale, format, out);
+        const std::size_t smem = set_smem_bytes<float>(vs.n, 0);
+        accumulate_kernel<float><<<unsigned(blocks), threads, smem, st>>>(
+            vs, static_cast<const Rec<float>*>(results), acc, first, finalize, format, out);
     }
     return cudaGetLastError();
-}
-
-std::size_t record_bytes(int precision) {
-    return precision == SGX_PRECISION_FP64 ? sizeof(Rec<double>) : sizeof(Rec<float>);
 }
 
 cudaError_t launch_encode(const float4* acc, std::uint32_t npix, float scale, std::uint32_t format, void* out,

@@ -1,0 +1,102 @@
+"""Batched views (one persistent launch, CUDA-graph replay) and the autotuner.
+
+A batch must give each view exactly the frame a single-view render of that
+view gives (same kernels, same per-ray arithmetic, same accumulation order),
+whatever the ray-order tile or launch shape.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _views(sgx, seed=5, n=6, small=True):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        side = int(rng.integers(2, 9)) * 16 if small else int(rng.integers(2, 17)) * 64
+        w, h = side, int(side * rng.uniform(0.5, 1.0)) // 2 * 2 or 2
+        spin = float(rng.uniform(0, 0.998))
+        incl = float(rng.uniform(10, 89))
+        spp = int(rng.integers(1, 9))
+        isco = sgx.kerr_isco_prograde(1.0, spin)
+        sc = sgx.Scene(spin_a_over_M=spin, disc_inner_M=isco, disc_outer_M=30.0, disc_peak_T_K=1e4,
+                       render_supersample=spp)
+        cam = sgx.build_orbital_camera(float(rng.uniform(20, 60)), np.pi / 2 - np.radians(incl), 0.0, 30.0)
+        out.append(sgx.pack_uniforms(sc, cam, w, h))
+    return out
+
+
+@pytest.mark.parametrize("integrator,precision", [(1, 0), (1, 1), (0, 0)])
+@pytest.mark.parametrize("tile", [(0, 0), (8, 4), (32, 2)])
+def test_batch_equals_single_view_renders(renderer, sgx, integrator, precision, tile):
+    views = _views(sgx)
+    opts = sgx.default_opts(integrator=integrator, precision=precision, tile_w=tile[0], tile_h=tile[1])
+    b = sgx.Batch(renderer, views, opts)
+    b.launch()
+    st = b.wait()
+    assert st.rays == sum(v.width * v.height * max(1, min(v.supersample, 1024)) for v in views)
+    for i, v in enumerate(views):
+        single = renderer.render_image(v, sgx.default_opts(integrator=integrator, precision=precision))
+        np.testing.assert_array_equal(b.capture(i), single, err_msg=f"view {i}")
+    b.close()
+
+
+def test_graph_replay_and_update(renderer, sgx):
+    views = _views(sgx, seed=9)
+    opts = sgx.default_opts(integrator=1)
+    b = sgx.Batch(renderer, views, opts, fmt=sgx._native.FORMAT_RGBA32F)
+    b.launch()
+    b.wait()
+    first = [b.capture(i) for i in range(len(views))]
+    b.launch()  # replay: identical
+    b.wait()
+    for i in range(len(views)):
+        np.testing.assert_array_equal(b.capture(i), first[i])
+    moved = []
+    for v in views:  # new cameras and times, same sizes
+        u = v.copy()
+        u.time_sec = 0.7
+        u.disc_peak_T = 6000.0
+        moved.append(u)
+    b.update(moved)
+    b.launch()
+    b.wait()
+    for i, u in enumerate(moved):
+        want = renderer.render_image(u, opts, fmt=sgx._native.FORMAT_RGBA32F)
+        np.testing.assert_array_equal(b.capture(i), want)
+    bad = [v.copy() for v in views]
+    bad[0].width += 2
+    with pytest.raises(sgx.SgxError):
+        b.update(bad)
+    b.close()
+
+
+def test_batch_rejects_bad_input(renderer, sgx):
+    views = _views(sgx, n=2)
+    mixed = [views[0], views[1].copy()]
+    mixed[1].metric_type = 0
+    with pytest.raises(sgx.SgxError):
+        sgx.Batch(renderer, mixed)
+    with pytest.raises(sgx.SgxError):
+        sgx.Batch(renderer, views, sgx.default_opts(sample_count=2))
+    with pytest.raises(sgx.SgxError):
+        sgx.Batch(renderer, [views[0]] * 129)
+
+
+def test_autotune_picks_a_valid_shape(renderer, sgx):
+    views = _views(sgx, seed=11, n=8, small=False)
+    base = sgx.default_opts(integrator=1)
+    best, ms = sgx.autotune(renderer, views, base, sample_cap=2)
+    assert ms > 0 and best.block_threads in (128, 256) and best.refill_interval in (4, 8, 16, 32)
+    assert (best.tile_w, best.tile_h) in ((0, 0), (8, 4), (16, 8), (32, 2))
+    assert best.integrator == 1
+    b = sgx.Batch(renderer, views[:3], best)
+    b.launch()
+    b.wait()
+    for i in range(3):
+        np.testing.assert_array_equal(b.capture(i), renderer.render_image(views[i], base))
+    b.close()
