@@ -4,7 +4,7 @@ Everything is compiled for sm_103a only, with plain nvcc / g++ calls run in
 parallel (no cmake).  Outputs land in ``singularity_gb300/_build/``:
 
 * ``libsgx.so``      — kernels + C ABI (include/sgx.h)
-* ``sgx_cuda_cli``   — the cuda_cli-compatible command line renderer
+* ``singularity_cuda_cli`` — the cuda_cli-compatible command line renderer
 """
 
 from __future__ import annotations
@@ -75,11 +75,11 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
     lib = BUILD / "libsgx.so"
     if force or jobs or not lib.exists():
         _run([nvcc, *ARCH, "-shared", "-o", str(lib), *map(str, objs), "-lcudart"])
-    cli = BUILD / "sgx_cuda_cli"
+    cli = BUILD / "singularity_cuda_cli"
     cli_srcs = [CSRC / "cuda_backend.cpp", CSRC / "cli_main.cpp"]
     if all(s.exists() for s in cli_srcs) and (force or not _newer(cli, cli_srcs + headers + [lib])):
-        _run(["g++", *CXX_FLAGS, f"-I{cuda / 'include'}", *map(str, cli_srcs), "-o", str(cli),
-              f"-L{BUILD}", "-lsgx", f"-Wl,-rpath,{BUILD}"])
+        _run(["g++", *CXX_FLAGS, "-pthread", f"-I{cuda / 'include'}", *map(str, cli_srcs),
+              str(BUILD / "sgx_host.cpp.o"), "-o", str(cli), f"-L{BUILD}", "-lsgx", "-Wl,-rpath,$ORIGIN"])
     if verbose:
         print(f"built {lib}")
     return lib

@@ -1,0 +1,87 @@
+// singularity_gb300/csrc/cuda_backend.cpp
+//
+// The reference's CudaBackend (render/cuda/cuda_backend.cu:105-166) re-made
+// over the C ABI of include/sgx.h.
+
+#include "cuda_backend.hpp"
+
+#include <cstdio>
+
+namespace singularity {
+
+CudaBackend::CudaBackend() = default;
+
+CudaBackend::~CudaBackend() { shutdown(); }
+
+bool CudaBackend::initialize(WindowHandle /*window*/, RenderConfig config) {
+    width_ = config.width;
+    height_ = config.height;
+    frame_time_sec_ = 0.0f;
+    rendered_ = false;
+    if (ctx_ == nullptr && sgx_create(-1, &ctx_) != SGX_OK) {
+        std::fprintf(stderr, "singularity CUDA backend: sgx_create failed (no CUDA device?)\n");
+        ctx_ = nullptr;
+        return false;
+    }
+    if (sgx_resize(ctx_, width_, height_) != SGX_OK) {
+        std::fprintf(stderr, "singularity CUDA backend: initialize failed: %s\n", sgx_last_error(ctx_));
+        sgx_destroy(ctx_);
+        ctx_ = nullptr;
+        return false;
+    }
+    return true;
+}
+
+void CudaBackend::shutdown() {
+    if (ctx_ != nullptr) {
+        sgx_destroy(ctx_);
+        ctx_ = nullptr;
+    }
+    width_ = 0;
+    height_ = 0;
+    rendered_ = false;
+}
+
+void CudaBackend::resize(std::uint32_t width, std::uint32_t height) {
+    if (width == width_ && height == height_) return;
+    shutdown();
+    RenderConfig cfg{};
+    cfg.width = width;
+    cfg.height = height;
+    initialize(WindowHandle{}, cfg);
+}
+
+void CudaBackend::render_frame(const Scene& scene, const CameraState& camera) {
+    if (ctx_ == nullptr) return;
+    const sgx_uniforms u = sgx::pack_uniforms(scene, camera, width_, height_, frame_time_sec_);
+    const sgx_status s = sgx_render(ctx_, &u, have_opts_ ? &opts_ : nullptr);
+    if (s != SGX_OK) {
+        std::fprintf(stderr, "singularity CUDA backend: render failed: %s\n", sgx_last_error(ctx_));
+    } else {
+        rendered_ = true;
+    }
+    frame_time_sec_ += 1.0f / 30.0f;
+}
+
+ImageData CudaBackend::capture_frame() {
+    ImageData out;
+    out.width = width_;
+    out.height = height_;
+    if (ctx_ == nullptr || !rendered_) return out;
+    out.pixels_rgba.resize(std::size_t(width_) * height_ * 4u);
+    if (sgx_capture(ctx_, out.pixels_rgba.data(), out.pixels_rgba.size(), SGX_FORMAT_RGBA8_SRGB) != SGX_OK) {
+        std::fprintf(stderr, "singularity CUDA backend: capture failed: %s\n", sgx_last_error(ctx_));
+        out.pixels_rgba.clear();
+    }
+    return out;
+}
+
+std::vector<float> CudaBackend::capture_frame_float() {
+    std::vector<float> out;
+    if (ctx_ == nullptr || !rendered_) return out;
+    out.resize(std::size_t(width_) * height_ * 4u);
+    if (sgx_capture(ctx_, out.data(), out.size() * sizeof(float), SGX_FORMAT_RGBA32F) != SGX_OK) out.clear();
+    return out;
+}
+
+}  // namespace singularity

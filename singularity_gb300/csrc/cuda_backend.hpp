@@ -1,0 +1,88 @@
+// singularity_gb300/csrc/cuda_backend.hpp
+//
+// C++20 CudaBackend over the C ABI: the same class, members and behaviour as
+// the reference's render/cuda/cuda_backend.hpp:17-46 behind the abstract
+// RenderBackend of render/include/render_backend.hpp:107-132, so a caller of
+// the reference (its cuda_cli) compiles against this header unchanged.
+//
+// Behaviour kept from the reference: initialize() allocates the frame and
+// returns false on failure; render_frame() is a no-op without a frame,
+// prints CUDA errors to stderr and carries on, and advances a virtual 1/30 s
+// clock after every frame (cuda_backend.cu:140-152); capture_frame() returns
+// an empty ImageData on failure.
+#pragma once
+
+#include <cstdint>
+#include <functional>
+#include <memory>
+#include <vector>
+
+#include "sgx.h"
+#include "sgx_host.hpp"
+
+namespace singularity {
+
+using Scene = sgx::Scene;
+using CameraState = sgx::CameraState;
+using ImageData = sgx::ImageData;
+
+struct WindowHandle {
+    void* native_window{nullptr};
+    void* native_view{nullptr};
+    std::function<void*(void*)> vulkan_create_surface{};
+};
+
+struct RenderConfig {
+    std::uint32_t width{1280};
+    std::uint32_t height{720};
+    bool vsync_enabled{true};
+};
+
+class RenderBackend {
+public:
+    virtual ~RenderBackend() = default;
+    RenderBackend(const RenderBackend&) = delete;
+    RenderBackend& operator=(const RenderBackend&) = delete;
+    RenderBackend(RenderBackend&&) = delete;
+    RenderBackend& operator=(RenderBackend&&) = delete;
+
+    virtual bool initialize(WindowHandle window, RenderConfig config) = 0;
+    virtual void shutdown() = 0;
+    virtual void resize(std::uint32_t width, std::uint32_t height) = 0;
+    virtual void render_frame(const Scene& scene, const CameraState& camera) = 0;
+    virtual ImageData capture_frame() = 0;
+    virtual const char* name() const = 0;
+
+protected:
+    RenderBackend() = default;
+};
+
+class CudaBackend : public RenderBackend {
+public:
+    CudaBackend();
+    ~CudaBackend() override;
+
+    bool initialize(WindowHandle window, RenderConfig config) override;
+    void shutdown() override;
+    void resize(std::uint32_t width, std::uint32_t height) override;
+    void render_frame(const Scene& scene, const CameraState& camera) override;
+    ImageData capture_frame() override;
+    const char* name() const override { return "CUDA"; }
+
+    // Extension (not in the reference): options of every later render_frame
+    // (precision form, integrator, launch shape); defaults = the reference.
+    void set_render_options(const sgx_render_opts& opts) { opts_ = opts; have_opts_ = true; }
+    // Extension: the last frame as RGBA32F (tone-mapped mean before sRGB).
+    std::vector<float> capture_frame_float();
+
+private:
+    std::uint32_t width_{0};
+    std::uint32_t height_{0};
+    sgx_context* ctx_{nullptr};
+    bool rendered_{false};
+    float frame_time_sec_{0.0f};
+    sgx_render_opts opts_{};
+    bool have_opts_{false};
+};
+
+}  // namespace singularity
