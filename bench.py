@@ -268,6 +268,34 @@ def batch_study(S, N, r, torch, launches: int = 3) -> dict:
     return out
 
 
+def hdr_bloom_study(S, N, r, torch, reps: int = 3) -> dict:
+    """Config 2: Kerr a=0.94 1920x1080, 16 spp, adaptive tol 1e-6, half-float HDR,
+    bloom sigma 8 px, ACES -> RGBA8; device time of render + post-process."""
+    u = S.workloads.kerr_1080p_16spp()
+    opts = S.default_opts(integrator=N.INTEGRATOR_ADAPTIVE, format=N.FORMAT_RGBA16F_HDR)
+    bo = N.BloomOpts(C.sizeof(N.BloomOpts), 8.0, -1.0, -1.0, N.FORMAT_RGBA8_SRGB)
+    lib = N.load()
+    r.render(u, opts)
+    lib.sgx_bloom(r.handle, C.byref(bo))
+    t_render, t_post = [], []
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r.render(u, opts)
+        t1 = time.perf_counter()
+        st = lib.sgx_bloom(r.handle, C.byref(bo))
+        t2 = time.perf_counter()
+        if st != 0:
+            raise RuntimeError(lib.sgx_last_error(r.handle).decode())
+        t_render.append(r.stats().total_ms)
+        t_post.append((t2 - t1) * 1e3)
+    rays = u.width * u.height * u.supersample
+    ms = float(np.median(t_render)) + float(np.median(t_post))
+    return {"rays": rays, "render_ms": float(np.median(t_render)), "bloom_ms_wall": float(np.median(t_post)),
+            "mrays_s_incl_post": rays / (ms / 1e3) / 1e6,
+            "note": "render device time (trace + HDR accumulation) + bloom sigma 8 px/ACES wall time (synchronous)"}
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -427,6 +455,9 @@ def main() -> None:
     study = None
     if not args.no_precision_study and args.precision == "fp32" and integ == N.INTEGRATOR_ADAPTIVE:
         study = precision_study(S, N, O, lib, r, u, d_out, stream, torch, opts)
+    hdr = None
+    if not args.no_batch_study and args.precision == "fp32" and integ == N.INTEGRATOR_ADAPTIVE:
+        hdr = hdr_bloom_study(S, N, r, torch)
     batch = None
     if not args.no_batch_study and args.precision == "fp32" and integ == N.INTEGRATOR_ADAPTIVE:
         batch = batch_study(S, N, r, torch)
@@ -450,6 +481,7 @@ def main() -> None:
         "budget_exhausted_rays": stats_acc["budget"],
         "precision_study": study,
         "batched_views": batch,
+        "hdr_bloom_1080p": hdr,
     }
     print(json.dumps(line), flush=True)
     if world > 1:

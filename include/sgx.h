@@ -209,6 +209,23 @@ sgx_status sgx_trace_samples(sgx_context* ctx, const sgx_uniforms* u, const sgx_
                              const uint32_t* gx, const uint32_t* gy, const uint32_t* s, float* hdr3,
                              uint32_t* steps, uint32_t* term);
 
+/* ---- HDR bloom and display transform ------------------------------------------ */
+/* The realtime backends' post-process (render/vulkan/shaders/bloom.hlsl:8-77,
+ * blit.hlsl:120-134), which the reference's CUDA path lacks: on the last frame,
+ * rendered in SGX_FORMAT_RGBA16F_HDR (the per-pixel mean HDR colour), a
+ * half-resolution Karis-weighted extract with a soft-knee threshold, a
+ * separable blur, and the compose hdr + bloom * strength, times exposure,
+ * ACES, then sRGB (RGBA8) or linear (RGBA32F).  Capture the result with
+ * sgx_capture in that format. */
+typedef struct sgx_bloom_opts {
+    uint32_t struct_size;
+    float sigma_px;  /* blur sigma in full-resolution pixels; <= 0: the reference's 7-tap kernel */
+    float threshold; /* < 0: the uniforms' bloom_threshold */
+    float strength;  /* < 0: the uniforms' bloom_strength */
+    uint32_t format; /* SGX_FORMAT_RGBA8_SRGB or SGX_FORMAT_RGBA32F */
+} sgx_bloom_opts;
+sgx_status sgx_bloom(sgx_context* ctx, const sgx_bloom_opts* opts);
+
 /* ---- batched views ----------------------------------------------------------- */
 /* No counterpart in the reference (one view per launch there,
  * render/cuda/cuda_backend.cu:140-152).  A batch is 1..SGX_BATCH_MAX_VIEWS

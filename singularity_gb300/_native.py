@@ -120,6 +120,11 @@ class SceneConfigC(C.Structure):
     ]
 
 
+class BloomOpts(C.Structure):
+    _fields_ = [("struct_size", C.c_uint32), ("sigma_px", C.c_float), ("threshold", C.c_float),
+                ("strength", C.c_float), ("format", C.c_uint32)]
+
+
 _P = C.c_void_p
 _U32P = C.POINTER(C.c_uint32)
 _F32P = C.POINTER(C.c_float)
@@ -149,6 +154,7 @@ SIGNATURES = [
     ("sgx_render_device", C.c_int, [_P, C.POINTER(Uniforms), C.POINTER(RenderOpts), _P, C.c_uint32, _P]),
     ("sgx_render_noalloc", C.c_int, [C.POINTER(Uniforms), C.POINTER(RenderOpts), _P, C.c_uint32, _P, C.c_char_p,
                                      C.c_size_t]),
+    ("sgx_bloom", C.c_int, [_P, C.POINTER(BloomOpts)]),
     ("sgx_batch_create", C.c_int, [_P, C.POINTER(Uniforms), C.c_uint32, C.POINTER(RenderOpts), C.c_uint32,
                                    C.POINTER(_P)]),
     ("sgx_batch_update", C.c_int, [_P, C.POINTER(Uniforms)]),

@@ -256,6 +256,13 @@ class Renderer:
         self.render(u, opts)
         return self.capture(fmt)
 
+    def bloom(self, sigma_px: float = 0.0, threshold: float = -1.0, strength: float = -1.0,
+              fmt: int = N.FORMAT_RGBA8_SRGB) -> np.ndarray:
+        """Bloom + ACES on the last frame (rendered with FORMAT_RGBA16F_HDR)."""
+        o = N.BloomOpts(C.sizeof(N.BloomOpts), sigma_px, threshold, strength, fmt)
+        self._check(self._lib.sgx_bloom(self._h, C.byref(o)))
+        return self.capture(fmt)
+
     def stats(self) -> N.RenderStats:
         s = N.RenderStats()
         self._check(self._lib.sgx_get_stats(self._h, C.byref(s)))

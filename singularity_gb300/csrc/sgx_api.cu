@@ -34,6 +34,12 @@ using sgx_internal::fail;
 
 void free_image(sgx_context* c) {
     if (c->d_image) cudaFree(c->d_image);
+    if (c->d_bloom) cudaFree(c->d_bloom);
+    if (c->d_post) cudaFree(c->d_post);
+    c->d_bloom = nullptr;
+    c->d_post = nullptr;
+    c->bloom_cap = 0;
+    c->post_valid = false;
     if (c->d_acc) cudaFree(c->d_acc);
     if (c->d_results) cudaFree(c->d_results);
     c->d_image = nullptr;
@@ -92,7 +98,6 @@ sgx_status check_opts(sgx_context* c, const sgx_render_opts& o) {
     if (o.precision > SGX_PRECISION_FP64) return fail(c, SGX_ERR_INVALID_ARGUMENT, "unknown precision");
     if (o.integrator > SGX_INTEGRATOR_ADAPTIVE) return fail(c, SGX_ERR_INVALID_ARGUMENT, "unknown integrator");
     if (o.format > SGX_FORMAT_RGBA16F_HDR) return fail(c, SGX_ERR_INVALID_ARGUMENT, "unknown format");
-    if (o.format == SGX_FORMAT_RGBA16F_HDR) return fail(c, SGX_ERR_UNSUPPORTED, "RGBA16F HDR output is not built");
     if (o.rhs_form > 1) return fail(c, SGX_ERR_INVALID_ARGUMENT, "unknown rhs_form");
     if ((o.tile_w == 0) != (o.tile_h == 0) || o.tile_w > 4096 || o.tile_h > 4096)
         return fail(c, SGX_ERR_INVALID_ARGUMENT, "tile_w and tile_h must both be 0 or both in [1, 4096]");
@@ -180,6 +185,8 @@ sgx_status render_impl(sgx_context* c, const sgx_uniforms* u, const sgx_render_o
     c->frame_spp = spp;
     c->frame_format = format;
     c->stats = acc;
+    c->last_u = *u;
+    c->post_valid = false;
     return SGX_OK;
 }
 
@@ -300,18 +307,29 @@ sgx_status sgx_capture(sgx_context* c, void* host_out, size_t bytes, uint32_t fo
     if (c == nullptr) return SGX_ERR_INVALID_ARGUMENT;
     if (host_out == nullptr) return fail(c, SGX_ERR_INVALID_ARGUMENT, "host_out is NULL");
     if (!c->frame_valid) return fail(c, SGX_ERR_NOT_RENDERED, "no complete frame to capture");
-    if (format != SGX_FORMAT_RGBA8_SRGB && format != SGX_FORMAT_RGBA32F)
-        return fail(c, SGX_ERR_UNSUPPORTED, "capture format not built");
-    const std::size_t px = format == SGX_FORMAT_RGBA8_SRGB ? 4 : 16;
-    const std::size_t need = std::size_t(c->width) * c->height * px;
+    if (format > SGX_FORMAT_RGBA16F_HDR) return fail(c, SGX_ERR_INVALID_ARGUMENT, "unknown format");
+    const std::size_t need = std::size_t(c->width) * c->height * sgxk::format_bytes(format);
     if (bytes < need) return fail(c, SGX_ERR_INVALID_ARGUMENT, "host buffer too small");
     cudaSetDevice(c->device);
-    if (format != c->frame_format) {
-        SGX_CUDA(c, sgxk::launch_encode(c->d_acc, c->width * c->height, 1.0f / float(c->frame_spp), format,
-                                        c->d_image, c->stream));
-        c->frame_format = format;
+    const void* src = c->d_image;
+    if (c->frame_format == SGX_FORMAT_RGBA16F_HDR) {
+        // An HDR frame: the raw half image, or the bloom-composed display image.
+        if (format != SGX_FORMAT_RGBA16F_HDR) {
+            if (!c->post_valid || c->post_format != format)
+                return fail(c, SGX_ERR_NOT_RENDERED,
+                            "an HDR frame is captured as RGBA16F, or in the format of its sgx_bloom output");
+            src = c->d_post;
+        }
+    } else {
+        if (format == SGX_FORMAT_RGBA16F_HDR)
+            return fail(c, SGX_ERR_UNSUPPORTED, "render with SGX_FORMAT_RGBA16F_HDR to capture HDR");
+        if (format != c->frame_format) {
+            SGX_CUDA(c, sgxk::launch_encode(c->d_acc, c->width * c->height, 1.0f / float(c->frame_spp), format,
+                                            c->d_image, c->stream));
+            c->frame_format = format;
+        }
     }
-    SGX_CUDA(c, cudaMemcpyAsync(host_out, c->d_image, need, cudaMemcpyDeviceToHost, c->stream));
+    SGX_CUDA(c, cudaMemcpyAsync(host_out, src, need, cudaMemcpyDeviceToHost, c->stream));
     SGX_CUDA(c, cudaStreamSynchronize(c->stream));
     return SGX_OK;
 }

@@ -34,6 +34,12 @@ struct sgx_context {
     std::size_t workspace_budget = std::size_t(4) << 30;
     sgx_render_stats stats{};
     std::string err;
+    sgx_uniforms last_u{};        // uniforms of the last render (bloom reads exposure, threshold, strength)
+    void* d_bloom = nullptr;      // two half-resolution half4 targets
+    std::size_t bloom_cap = 0;    // bytes of one target
+    void* d_post = nullptr;       // composed frame after sgx_bloom (16 B / pixel)
+    bool post_valid = false;
+    std::uint32_t post_format = SGX_FORMAT_RGBA8_SRGB;
 };
 
 

@@ -21,6 +21,7 @@
 // All loops are bounded: a ray ends after max_steps integrator steps, and the
 // queue is a single counter that only grows.
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -520,7 +521,13 @@ template <class T> __global__ void setup_views(const sgx_uniforms* u, std::uint3
 __device__ __forceinline__ void encode_pixel(float4 sum, float scale, std::uint32_t format, void* out,
                                              std::uint64_t pix) {
     const float r = sum.x * scale, g = sum.y * scale, b = sum.z * scale;
-    if (format == SGX_FORMAT_RGBA8_SRGB) {
+    if (format == SGX_FORMAT_RGBA16F_HDR) {
+        // scene-referred HDR mean in half precision, as the realtime backends'
+        // rgba16f target holds it
+        __half2* o = static_cast<__half2*>(out) + 2 * pix;
+        o[0] = __floats2half2_rn(r, g);
+        o[1] = __floats2half2_rn(b, 1.0f);
+    } else if (format == SGX_FORMAT_RGBA8_SRGB) {
         uchar4 o;
         o.x = to_u8(r);
         o.y = to_u8(g);
@@ -535,6 +542,8 @@ __device__ __forceinline__ void encode_pixel(float4 sum, float scale, std::uint3
 // Shades each hit record of the pass and adds it to the pixel's sum in sample
 // order (the reference's `ldr = ldr + aces(hdr * exposure)`,
 // geodesic_kernel.cu:492-501); the last pass scales by 1/spp and encodes.
+// For the HDR format the sum is of the raw HDR colour (no exposure, no tone
+// map), the input of the bloom/blit pipeline.
 template <class T>
 __global__ void __launch_bounds__(256) accumulate_kernel(ViewSet vs, const Rec<T>* __restrict__ results,
                                                          float4* __restrict__ acc, bool first, bool finalize,
@@ -552,12 +561,19 @@ __global__ void __launch_bounds__(256) accumulate_kernel(ViewSet vs, const Rec<T
     const std::uint64_t base = m.rec_off[vid] + pix;
     const std::uint32_t S = m.S[vid];
     float4 sum = first ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : acc[p];
+    const bool raw = format == SGX_FORMAT_RGBA16F_HDR;
     for (std::uint32_t s = 0; s < S; ++s) {
         const Rec<T> rec = results[base + std::uint64_t(s) * npix];
         const V3<T> hdr = shade_record(v, rec);
-        sum.x = sum.x + float(aces1(hdr.x * v.exposure));
-        sum.y = sum.y + float(aces1(hdr.y * v.exposure));
-        sum.z = sum.z + float(aces1(hdr.z * v.exposure));
+        if (raw) {
+            sum.x = sum.x + float(hdr.x);
+            sum.y = sum.y + float(hdr.y);
+            sum.z = sum.z + float(hdr.z);
+        } else {
+            sum.x = sum.x + float(aces1(hdr.x * v.exposure));
+            sum.y = sum.y + float(aces1(hdr.y * v.exposure));
+            sum.z = sum.z + float(aces1(hdr.z * v.exposure));
+        }
     }
     acc[p] = sum;
     if (finalize) encode_pixel(sum, 1.0f / float(v.spp), format, out, p);
