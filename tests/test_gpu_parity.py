@@ -170,7 +170,10 @@ def test_errors_are_status_codes(renderer, sgx):
         renderer.render(u, sgx.default_opts(sample_begin=5))
     assert e.value.status == 1
     with pytest.raises(sgx.SgxError) as e:
-        renderer.render(u, sgx.default_opts(format=N.FORMAT_RGBA16F_HDR))
+        renderer.render(u, sgx.default_opts(format=7))
+    assert e.value.status == 1
+    with pytest.raises(sgx.SgxError):
+        renderer.render(u, sgx.default_opts(tile_w=8, tile_h=0))
     # the context stays usable after rejected calls
     img = renderer.render_image(u)
     assert img.shape == (8, 8, 4)
