@@ -279,6 +279,52 @@ sgx_status sgx_autotune(sgx_context* ctx, const sgx_uniforms* views, uint32_t n,
 sgx_status sgx_render_noalloc(const sgx_uniforms* u, const sgx_render_opts* opts, void* d_out, uint32_t format,
                               void* stream, char* err, size_t err_len);
 
+/* ---- differentiable render and its adjoint ---------------------------------- */
+/* No counterpart in the reference.  A Kerr render form that is differentiable
+ * in four scene parameters, and the gradient of an image loss with respect to
+ * them by a reverse (adjoint) sweep of the fixed-step RK4.  The form keeps the
+ * reference's integrator, termination and disc shading
+ * (geodesic_kernel.cu:300-401, kerr_hamilton.h:97-178) and changes what makes
+ * the image discontinuous in the parameters: the camera orbits at azimuth 0
+ * with its frame a closed-form function of the inclination, the starfield is
+ * off, the annulus edges are soft (each crossing at radius r emits with weight
+ * w = S((r - r_in)/e) S((r_out - r)/e), S the cubic smoothstep, e =
+ * edge_width * M, through a transmittance that each crossing multiplies by
+ * 1 - w), and, when fade_start > 0, images whose ray has swept an angle psi
+ * around the hole are faded by 1 - S((psi - fade_start)/fade_width).  The
+ * image is W x H x 3 floats, per pixel the mean over samples of
+ * ACES(hdr * exposure) (the reference's tone map, before sRGB encoding). */
+typedef struct sgx_diff_params {
+    double spin;     /* a / M, in [0, 1) */
+    double incl;     /* inclination of the camera from the spin axis, radians, in (0, pi) */
+    double r_in;     /* disc inner radius, units of M */
+    double t_scale;  /* multiplies the disc's peak temperature */
+} sgx_diff_params;
+typedef struct sgx_diff_opts {
+    uint32_t struct_size;
+    uint32_t precision;  /* SGX_PRECISION_FP32 or SGX_PRECISION_FP64 */
+    float edge_width;    /* soft annulus edge, units of M (0.1) */
+    float fade_start;    /* swept angle where higher-order images fade, rad (pi); <= 0: no fade */
+    float fade_width;    /* fade length, rad (pi / 2) */
+    uint32_t reserved[3];
+} sgx_diff_opts;
+void sgx_diff_opts_default(sgx_diff_opts* opts);
+/* Forward pass: renders the form for `params` with size, samples, distance
+ * (|cam_pos|), field of view, mass, r_out, peak temperature, step, max_steps,
+ * escape radius, exposure, turbulence, time and the Doppler/redshift flags
+ * from `base` (a Kerr uniform block), into d_image (device, W*H*3 floats; NULL:
+ * an internal buffer) and keeps what the backward pass needs (a state
+ * checkpoint every 64 steps and up to 8 crossings per ray).  Synchronous. */
+sgx_status sgx_diff_forward(sgx_context* ctx, const sgx_uniforms* base, const sgx_diff_params* params,
+                            const sgx_diff_opts* opts, float* d_image, void* stream);
+/* Backward pass of the last forward: d_grad_image (device, W*H*3 floats) is
+ * dLoss/dImage; grad[4] (host) receives dLoss/d(spin, incl, r_in, t_scale).
+ * The per-ray terms are summed in a fixed order (deterministic). */
+sgx_status sgx_diff_backward(sgx_context* ctx, const float* d_grad_image, double* grad, void* stream);
+/* Rays of the last forward, and how many crossings beyond the 8 recorded per
+ * ray were dropped from the backward pass (0 in normal scenes). */
+sgx_status sgx_diff_stats(sgx_context* ctx, uint64_t* rays, uint64_t* crossing_overflow);
+
 /* ---- measurement --------------------------------------------------------- */
 /* No counterpart in the reference: the device's FP32 FMA issue ceiling in
  * TFLOP/s (2 flops per FMA), measured with a register-resident FMA kernel of

@@ -1,0 +1,235 @@
+// oracle/diff_oracle.hpp
+//
+// TEST INFRASTRUCTURE — CPU specification of the differentiable render form
+// (the GPU's forward and adjoint kernels in singularity_gb300/csrc/sgx_diff.cu
+// implement it).  Only tests/ and bench.py's checks use it.
+//
+// The reference renders images that are discontinuous in the scene
+// parameters (hard annulus edges, a 1000 K colour floor at the inner edge,
+// starfield cells, geodesic_kernel.cu:77-171,262-289), so a per-ray derivative
+// and a finite difference disagree by boundary terms.  The differentiable form
+// changes exactly that, and nothing else:
+//   * the camera orbits at azimuth 0 with elevation pi/2 - incl, its frame
+//     written in closed form (position (d sin i, 0, d cos i), forward
+//     (-sin i, 0, -cos i), right (0, 1, 0), up (cos i, 0, -sin i): the values
+//     cuda_cli/main.cpp:68-109 computes, as functions of i);
+//   * the starfield is off (escaped and captured rays are black);
+//   * the annulus edges are soft: a crossing at radius r emits with weight
+//     w(r) = S((r - r_in)/eps) S((r_out - r)/eps), S(x) = 3x^2 - 2x^3 on [0, 1];
+//     the ray carries a transmittance tau (1 at launch): each crossing adds
+//     tau w c to the colour and multiplies tau by (1 - w); tau = 0 ends the ray.
+//     With eps -> 0 this is the reference's first-hit rule;
+//   * optionally, the emission of a crossing is multiplied by
+//     1 - S((psi - fade_start) / fade_width), psi the angle the ray has swept
+//     around the hole when it crosses (accumulated per step as
+//     sqrt(dtheta^2 + sin^2(theta) dphi^2) and interpolated to the crossing):
+//     images that wind past fade_start fade out, so rays near the critical
+//     curve — whose winding grows without bound and whose higher-order
+//     images jump in and out as parameters move — contribute nothing;
+//   * the blackbody fit (Tanner Helland's, geodesic_kernel.cu:77-104) jumps at
+//     6600 K where it switches branch (green by 0.013, blue by 0.01); the form
+//     blends the two branches over 6500-6700 K with S, so colour is continuous
+//     in temperature (identical outside that band);
+//   * the disc temperature scale multiplies the peak temperature.
+// Integration is the reference's fixed-step Kerr RK4 with its pole damping
+// (kerr_hamilton.h:165-178), checks and termination as geodesic_kernel.cu:351-401.
+
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+
+#include "geodesic_oracle.hpp"
+
+namespace oracle {
+
+struct DiffParams {
+    double spin;      // a / M
+    double incl;      // inclination, radians
+    double r_in;      // disc inner radius, M
+    double t_scale;   // multiplies the peak temperature
+};
+
+struct DiffOpts {
+    float eps;         // soft-edge width, M (0.1)
+    float fade_start;  // swept angle (rad) where higher-order images start to fade; <= 0: no fade
+    float fade_width;  // fade length in swept angle (rad)
+    std::uint32_t pad;
+};
+
+template <class T> inline T smooth01(T x) {
+    if (x <= OLIT(0.0)) return OLIT(0.0);
+    if (x >= OLIT(1.0)) return OLIT(1.0);
+    return x * x * (OLIT(3.0) - OLIT(2.0) * x);
+}
+
+// Blackbody colour continuous at 6600 K: the fit's low (t <= 66) and high
+// (t > 66) branches, t = temperature / 100 K, blended by S((t - 65) / 2).
+template <class T> inline V3<T> blackbody_c0(T temp) {
+    const T t = vclamp(temp, OLIT(1000.0), OLIT(40000.0)) * OLIT(0.01);
+    V3<T> lo, hi;
+    const bool need_lo = t < OLIT(67.0), need_hi = t > OLIT(65.0);
+    if (need_lo) {
+        lo.x = OLIT(1.0);
+        lo.y = vclamp(OLIT(0.39008157876901960784) * M<T>::log(t) - OLIT(0.63184144378862745098), OLIT(0.0),
+                      OLIT(1.0));
+        lo.z = (t <= OLIT(19.0)) ? OLIT(0.0)
+                                 : vclamp(OLIT(0.54320678911019607843) * M<T>::log(t - OLIT(10.0)) -
+                                              OLIT(1.19625408914),
+                                          OLIT(0.0), OLIT(1.0));
+    }
+    if (need_hi) {
+        const T t1 = t - OLIT(60.0);
+        hi.x = vclamp(OLIT(1.29293618606274509804) * M<T>::pow(t1, OLIT(-0.1332047592)), OLIT(0.0), OLIT(1.0));
+        hi.y = vclamp(OLIT(1.12989086089529411765) * M<T>::pow(t1, OLIT(-0.0755148492)), OLIT(0.0), OLIT(1.0));
+        hi.z = OLIT(1.0);
+    }
+    if (!need_hi) return lo;
+    if (!need_lo) return hi;
+    const T sb = smooth01((t - OLIT(65.0)) * OLIT(0.5));
+    return v3(lo.x + sb * (hi.x - lo.x), lo.y + sb * (hi.y - lo.y), lo.z + sb * (hi.z - lo.z));
+}
+
+// Kerr disc colour of the form (geodesic_kernel.cu:368-393 with blackbody_c0).
+template <class T>
+inline V3<T> diff_disc_colour(const Params<T>& u, const KConst<T>& c, T cam_r, T r_cross, T phi_cross, T T_local) {
+    const T Mm = u.mass_M;
+    const T f_emit = OLIT(1.0) - OLIT(2.0) * Mm / r_cross;
+    const T f_obs = OLIT(1.0) - OLIT(2.0) * Mm / cam_r;
+    const T g_grav = (u.flags & SGX_FLAG_REDSHIFT_ON)
+                         ? M<T>::sqrt(M<T>::fmax(f_emit, OLIT(1e-6)) / M<T>::fmax(f_obs, OLIT(1e-6)))
+                         : OLIT(1.0);
+    T g_dop = OLIT(1.0);
+    if (u.flags & SGX_FLAG_DOPPLER_ON) {
+        const T om0 = M<T>::sqrt(Mm / (r_cross * r_cross * r_cross));
+        const T omega_K = om0 / (OLIT(1.0) + u.spin_a * om0);
+        const T v = r_cross * omega_K / M<T>::sqrt(M<T>::fmax(f_emit, OLIT(1e-6)));
+        const T cos_psi = vclamp(c.L / r_cross, OLIT(-1.0), OLIT(1.0));
+        g_dop = M<T>::sqrt(M<T>::fmax(OLIT(1.0) - v * v, OLIT(0.0))) / M<T>::fmax(OLIT(1.0) - v * cos_psi, OLIT(1e-4));
+    }
+    const T g = g_grav * g_dop;
+    const V3<T> col = blackbody_c0(g * T_local);
+    const T flux = vclamp(M<T>::pow(u.r_in / r_cross, OLIT(3.0)), OLIT(0.05), OLIT(1.5));
+    const T bands = disc_band_mask(r_cross, phi_cross, u.r_in, u.turbulence, u.time_sec);
+    const T g2 = g * g;
+    return vmul(col, flux * bands * g2 * g2);
+}
+
+template <class T> struct DiffOut {
+    V3<T> hdr;
+    std::uint32_t steps, crossings;
+};
+
+// One sample of the differentiable form.  u supplies size, spp, distance
+// (|cam_pos|), FOV, aspect, mass, r_out, peak T, h, max_steps, escape radius,
+// exposure, turbulence, time and the Doppler/redshift flags.
+template <class T>
+inline DiffOut<T> diff_trace(const sgx_uniforms& ub, const DiffParams& dp, const DiffOpts& o, std::uint32_t gx,
+                             std::uint32_t gy, std::uint32_t s) {
+    const Params<T> u = promote<T>(ub);
+    const T Mm = u.mass_M;
+    const T a = T(dp.spin) * Mm;
+    const T incl = T(dp.incl);
+    const T r_in = T(dp.r_in) * Mm;
+    const T peak_T = u.peak_T * T(dp.t_scale);
+    const T eps = T(o.eps) * Mm;
+    const T dcam = M<T>::sqrt(T(ub.cam_pos.x) * T(ub.cam_pos.x) + T(ub.cam_pos.y) * T(ub.cam_pos.y) +
+                              T(ub.cam_pos.z) * T(ub.cam_pos.z));
+    const T si = M<T>::sin(incl), ci = M<T>::cos(incl);
+    // camera frame
+    const V3<T> fwd = v3(-si, OLIT(0.0), -ci);
+    const V3<T> right = v3(OLIT(0.0), OLIT(1.0), OLIT(0.0));
+    const V3<T> up = v3(ci, OLIT(0.0), -si);
+    T ox, oy;
+    if (u.spp == 1u) {
+        ox = OLIT(0.5);
+        oy = OLIT(0.5);
+    } else {
+        ox = halton<T>(s + 1u, 2u);
+        oy = halton<T>(s + 1u, 3u);
+    }
+    const T fx = T(float(gx)) + ox, fy = T(float(gy)) + oy;
+    const T u_ndc = (OLIT(2.0) * fx / T(float(u.width)) - OLIT(1.0)) * u.aspect * u.tan_half_fov;
+    const T v_ndc = -(OLIT(2.0) * fy / T(float(u.height)) - OLIT(1.0)) * u.tan_half_fov;
+    const V3<T> dir = vnormalize(vadd(fwd, vadd(vmul(right, u_ndc), vmul(up, v_ndc))));
+    // spherical frame at the camera: theta = incl, phi = 0
+    const V3<T> rhat = v3(si, OLIT(0.0), ci);
+    const V3<T> that = v3(ci, OLIT(0.0), -si);
+    const V3<T> phat = v3(OLIT(0.0), OLIT(1.0), OLIT(0.0));
+    CamRay<T> cam;
+    cam.cart = dir;
+    cam.cam_r = dcam;
+    cam.cam_theta = incl;
+    cam.cam_phi = OLIT(0.0);
+    cam.sin_th = si;
+    cam.ur = vdot(dir, rhat);
+    cam.utheta = vdot(dir, that) / dcam;
+    cam.uphi = vdot(dir, phat) / (dcam * M<T>::fmax(si, OLIT(1e-6)));
+
+    Params<T> up_ = u;
+    up_.spin_a = a;
+    up_.r_in = r_in;
+    up_.peak_T = peak_T;
+    KState<T> y;
+    KConst<T> c;
+    DiffOut<T> out{v3(OLIT(0.0), OLIT(0.0), OLIT(0.0)), 0u, 0u};
+    // kerr_init reads cos(cam_theta) itself; the closed-form frame above agrees with it.
+    if (!kerr_init(cam, up_, y, c)) return out;
+    const T hcut = kerr_horizon_cut(Mm, a);
+    T tau = OLIT(1.0);
+    KState<T> prev = y;
+    T psi = OLIT(0.0), psi_prev = OLIT(0.0);
+    const bool fade = o.fade_start > 0.0f;
+    std::uint32_t step = 0;
+    for (; step < u.max_steps; ++step) {
+        if (!M<T>::isfinite(y.r) || y.r < hcut) break;
+        if (y.r > u.escape_r) break;
+        if (u.flags & SGX_FLAG_DISC_ON) {
+            const Crossing<T> x = equatorial_crossing(prev.theta, y.theta);
+            if (x.crossed) {
+                const T r_c = lerp_s(prev.r, y.r, x.frac);
+                T w = smooth01((r_c - r_in) / eps) * smooth01((u.r_out - r_c) / eps);
+                if (fade) {
+                    const T psi_c = lerp_s(psi_prev, psi, x.frac);
+                    w = w * (OLIT(1.0) - smooth01((psi_c - T(o.fade_start)) / T(o.fade_width)));
+                }
+                if (w > OLIT(0.0)) {
+                    ++out.crossings;
+                    const T T_local = disc_temperature(r_c, r_in, peak_T);
+                    V3<T> col = v3(OLIT(0.0), OLIT(0.0), OLIT(0.0));
+                    if (T_local > OLIT(0.0)) col = diff_disc_colour(up_, c, dcam, r_c, y.phi, T_local);
+                    const T k = tau * w;
+                    out.hdr = vadd(out.hdr, vmul(col, k));
+                    tau = tau * (OLIT(1.0) - w);
+                    if (!(tau > OLIT(0.0))) break;
+                }
+            }
+        }
+        prev = y;
+        y = kerr_rk4(y, u.h_step, c);
+        if (fade) {
+            const T dth = y.theta - prev.theta, dph = y.phi - prev.phi, st = M<T>::sin(y.theta);
+            psi_prev = psi;
+            psi = psi + M<T>::sqrt(dth * dth + st * st * dph * dph);
+        }
+    }
+    out.steps = step;
+    return out;
+}
+
+// Image of the form: per pixel the mean over samples of ACES(hdr * exposure),
+// samples summed in order (geodesic_kernel.cu:482-503).
+template <class T>
+inline V3<T> diff_pixel(const sgx_uniforms& ub, const DiffParams& dp, const DiffOpts& o, std::uint32_t gx,
+                        std::uint32_t gy) {
+    const std::uint32_t spp = ub.supersample < 1u ? 1u : (ub.supersample > 1024u ? 1024u : ub.supersample);
+    const T exposure = T(ub.exposure);
+    V3<T> ldr = v3(OLIT(0.0), OLIT(0.0), OLIT(0.0));
+    for (std::uint32_t s = 0; s < spp; ++s) {
+        const DiffOut<T> t = diff_trace<T>(ub, dp, o, gx, gy, s);
+        ldr = vadd(ldr, aces(vmul(t.hdr, exposure)));
+    }
+    return vmul(ldr, OLIT(1.0) / T(float(spp)));
+}
+
+}  // namespace oracle

@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "adaptive_oracle.hpp"
+#include "diff_oracle.hpp"
 #include "geodesic_oracle.hpp"
 
 namespace {
@@ -224,5 +225,48 @@ int oracle_crossing_f32(float th_prev, float th_curr, float* frac) {
 
 // Spherical photon orbit radius for xi = L/E (adaptive_oracle.hpp).
 double oracle_photon_orbit_radius(double a, double M, double xi) { return oracle::photon_orbit_radius<double>(a, M, xi); }
+
+// Differentiable render form (diff_oracle.hpp): the LDR mean image, H*W*3.
+int oracle_diff_render_f32(const sgx_uniforms* u, const oracle::DiffParams* p, const oracle::DiffOpts* o,
+                           float* ldr3, int threads) {
+    if (u == nullptr || p == nullptr || o == nullptr || ldr3 == nullptr) return 1;
+    const std::int64_t npix = std::int64_t(u->width) * u->height;
+    parallel_for(npix, threads, [&](std::int64_t i) {
+        const auto l = oracle::diff_pixel<float>(*u, *p, *o, std::uint32_t(i % u->width), std::uint32_t(i / u->width));
+        ldr3[3 * i] = l.x;
+        ldr3[3 * i + 1] = l.y;
+        ldr3[3 * i + 2] = l.z;
+    });
+    return 0;
+}
+int oracle_diff_render_f64(const sgx_uniforms* u, const oracle::DiffParams* p, const oracle::DiffOpts* o,
+                           double* ldr3, int threads) {
+    if (u == nullptr || p == nullptr || o == nullptr || ldr3 == nullptr) return 1;
+    const std::int64_t npix = std::int64_t(u->width) * u->height;
+    parallel_for(npix, threads, [&](std::int64_t i) {
+        const auto l = oracle::diff_pixel<double>(*u, *p, *o, std::uint32_t(i % u->width), std::uint32_t(i / u->width));
+        ldr3[3 * i] = l.x;
+        ldr3[3 * i + 1] = l.y;
+        ldr3[3 * i + 2] = l.z;
+    });
+    return 0;
+}
+// Per-sample HDR, steps and crossing count of the form.
+int oracle_diff_trace_f64(const sgx_uniforms* u, const oracle::DiffParams* p, const oracle::DiffOpts* o,
+                          std::int64_t n, const std::uint32_t* gx, const std::uint32_t* gy, const std::uint32_t* s,
+                          double* hdr3, std::uint32_t* steps, std::uint32_t* crossings, int threads) {
+    if (u == nullptr || p == nullptr || o == nullptr) return 1;
+    parallel_for(n, threads, [&](std::int64_t i) {
+        const auto t = oracle::diff_trace<double>(*u, *p, *o, gx[i], gy[i], s[i]);
+        if (hdr3) {
+            hdr3[3 * i] = t.hdr.x;
+            hdr3[3 * i + 1] = t.hdr.y;
+            hdr3[3 * i + 2] = t.hdr.z;
+        }
+        if (steps) steps[i] = t.steps;
+        if (crossings) crossings[i] = t.crossings;
+    });
+    return 0;
+}
 
 }  // extern "C"

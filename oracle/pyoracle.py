@@ -13,6 +13,7 @@ this module, and only as the checker.  It loads:
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 import subprocess
 from pathlib import Path
@@ -39,6 +40,47 @@ class RayDiag(C.Structure):
     _fields_ = [("E", C.c_double), ("L", C.c_double), ("Q0", C.c_double), ("Q_end", C.c_double),
                 ("H2_end", C.c_double), ("norm_Q", C.c_double), ("accepted", C.c_uint32),
                 ("rejected", C.c_uint32), ("zone_steps", C.c_uint32), ("pad", C.c_uint32)]
+
+
+class DiffParams(C.Structure):
+    _fields_ = [("spin", C.c_double), ("incl", C.c_double), ("r_in", C.c_double), ("t_scale", C.c_double)]
+
+
+class DiffOpts(C.Structure):
+    _fields_ = [("eps", C.c_float), ("fade_start", C.c_float), ("fade_width", C.c_float), ("pad", C.c_uint32)]
+
+
+DIFF_FADE = (math.pi, math.pi / 2)  # the library's default winding fade (start, width), rad
+
+
+def diff_render(u, params, eps: float = 0.1, precision: str = "f64", threads: int | None = None,
+                fade=DIFF_FADE) -> np.ndarray:
+    """LDR image (H, W, 3) of the differentiable form at params = (spin, incl_rad, r_in, t_scale).
+    fade = (start, width) of the winding fade; start <= 0 turns it off."""
+    threads = threads or default_threads()
+    p = DiffParams(*[float(x) for x in params])
+    o = DiffOpts(eps, fade[0], fade[1], 0)
+    dt = np.float32 if precision == "f32" else np.float64
+    out = np.zeros((u.height, u.width, 3), dtype=dt)
+    fn = lib().oracle_diff_render_f32 if precision == "f32" else lib().oracle_diff_render_f64
+    rc = fn(_u(u), C.byref(p), C.byref(o), _p(out), C.c_int(threads))
+    if rc != 0:
+        raise RuntimeError("oracle diff render failed")
+    return out
+
+
+def diff_fd_gradient(u, params, target: np.ndarray, step: float = 1e-3, eps: float = 0.1,
+                     precision: str = "f64", fade=DIFF_FADE) -> np.ndarray:
+    """Central finite differences (step in each parameter) of mean((I - target)^2)."""
+    params = np.asarray(params, dtype=np.float64)
+    g = np.zeros(4)
+    for k in range(4):
+        d = np.zeros(4)
+        d[k] = step
+        lp = np.mean((diff_render(u, params + d, eps, precision, fade=fade).astype(np.float64) - target) ** 2)
+        lm = np.mean((diff_render(u, params - d, eps, precision, fade=fade).astype(np.float64) - target) ** 2)
+        g[k] = (lp - lm) / (2 * step)
+    return g
 
 
 def build(ref: bool = True) -> None:

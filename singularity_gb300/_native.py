@@ -125,6 +125,15 @@ class BloomOpts(C.Structure):
                 ("strength", C.c_float), ("format", C.c_uint32)]
 
 
+class DiffParams(C.Structure):
+    _fields_ = [("spin", C.c_double), ("incl", C.c_double), ("r_in", C.c_double), ("t_scale", C.c_double)]
+
+
+class DiffOpts(C.Structure):
+    _fields_ = [("struct_size", C.c_uint32), ("precision", C.c_uint32), ("edge_width", C.c_float),
+                ("fade_start", C.c_float), ("fade_width", C.c_float), ("reserved", C.c_uint32 * 3)]
+
+
 _P = C.c_void_p
 _U32P = C.POINTER(C.c_uint32)
 _F32P = C.POINTER(C.c_float)
@@ -165,6 +174,10 @@ SIGNATURES = [
     ("sgx_batch_destroy", None, [_P]),
     ("sgx_autotune", C.c_int, [_P, C.POINTER(Uniforms), C.c_uint32, C.POINTER(RenderOpts), C.c_uint32,
                                C.POINTER(RenderOpts), C.POINTER(C.c_float)]),
+    ("sgx_diff_opts_default", None, [C.POINTER(DiffOpts)]),
+    ("sgx_diff_forward", C.c_int, [_P, C.POINTER(Uniforms), C.POINTER(DiffParams), C.POINTER(DiffOpts), _P, _P]),
+    ("sgx_diff_backward", C.c_int, [_P, _P, C.POINTER(C.c_double), _P]),
+    ("sgx_diff_stats", C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     ("sgx_measure_fp32_peak", C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
     ("sgx_trace_samples", C.c_int, [_P, C.POINTER(Uniforms), C.POINTER(RenderOpts), C.c_uint64, _U32P, _U32P,
                                     _U32P, _F32P, _U32P, _U32P]),

@@ -259,6 +259,7 @@ void sgx_destroy(sgx_context* c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     free_image(c);
+    sgx_internal_free_diff(c);
     if (c->d_view) cudaFree(c->d_view);
     if (c->d_u) cudaFree(c->d_u);
     if (c->d_words) cudaFree(c->d_words);

@@ -13,6 +13,8 @@
 #include "sgx.h"
 #include "sgx_kernels.hpp"
 
+struct sgx_diff_state;  // differentiable form (sgx_diff.cu)
+
 struct sgx_context {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -40,7 +42,11 @@ struct sgx_context {
     void* d_post = nullptr;       // composed frame after sgx_bloom (16 B / pixel)
     bool post_valid = false;
     std::uint32_t post_format = SGX_FORMAT_RGBA8_SRGB;
+    sgx_diff_state* diff = nullptr;  // forward records of sgx_diff_forward
 };
+
+// Releases the differentiable form's buffers (defined in sgx_diff.cu).
+void sgx_internal_free_diff(sgx_context* ctx);
 
 
 namespace sgx_internal {

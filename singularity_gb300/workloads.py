@@ -67,3 +67,18 @@ def differentiation_target(w=512, h=512, spp=4):
 def differentiation_guess(w=512, h=512, spp=4):
     """Config 5 initial guess: a = 0.5, i = 50 deg, r_in = 1.2 ISCO(0.5), temperature scale 0.8."""
     return dict(spin=0.5, incl_deg=50.0, r_in=1.2 * B.kerr_isco_prograde(1.0, 0.5), t_scale=0.8, w=w, h=h, spp=spp)
+
+
+def differentiation_base(w=512, h=512, spp=4, distance=40.0, fov_deg=30.0, h_step=0.2, max_steps=2000):
+    """Uniform block of the parameter-recovery scene: camera at 40 M with a 30 degree
+    field of view, disc out to 30 M at 10^4 K, step 0.2, 2000 steps.  The
+    differentiable form takes spin, inclination, inner radius and temperature
+    scale from its parameters, everything else from this block."""
+    sc = B.Scene(spin_a_over_M=0.7, disc_outer_M=30.0, disc_peak_T_K=1e4, render_supersample=spp, h_step=h_step,
+                 max_steps=max_steps)
+    return B.pack_uniforms(sc, B.build_orbital_camera(distance, 0.3, 0.0, fov_deg), w, h)
+
+
+def differentiation_params(d):
+    """(spin, inclination in rad, r_in, t_scale) of a differentiation_target/guess dict."""
+    return (d["spin"], math.radians(d["incl_deg"]), d["r_in"], d["t_scale"])

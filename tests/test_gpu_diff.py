@@ -1,0 +1,138 @@
+"""The differentiable render form and its adjoint on the GPU, through the C ABI.
+
+Forward: the GPU image against the oracle's image of the same form
+(oracle/diff_oracle.hpp) in the same precision.  Adjoint: the GPU's gradient
+of an image loss against central differences (step 1e-3, the oracle's FP64
+image) and the FP32 adjoint against the FP64 adjoint.  Tolerances are stated
+per test."""
+
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FD_STEP = 1e-3
+
+
+@pytest.fixture(scope="module")
+def diff(sgx, renderer):
+    from singularity_gb300 import diff as D
+    return D.DiffRenderer(renderer)
+
+
+def _setup(sgx, w=64, h=48, spp=2):
+    W = sgx.workloads
+    base = W.differentiation_base(w, h, spp)
+    tgt = W.differentiation_params(W.differentiation_target())
+    guess = W.differentiation_params(W.differentiation_guess())
+    return base, tgt, guess
+
+
+def _loss_grad_image(img, target):
+    import torch
+    return 2.0 * (img - target) / img.numel()
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_forward_matches_oracle(diff, sgx, oracle, prec):
+    from singularity_gb300 import diff as D
+    N = sgx._native
+    base, tgt, guess = _setup(sgx)
+    opts = D.DiffOptions(precision=N.PRECISION_FP32 if prec == "f32" else N.PRECISION_FP64)
+    for p in (tgt, guess):
+        img = diff.forward(base, p, opts).cpu().numpy()
+        ref = oracle.diff_render(base, p, precision=prec).astype(np.float32)
+        e = np.abs(img - ref)
+        print(f"{prec} {p}: mean {e.mean():.2e} max {e.max():.2e}")
+        if prec == "f64":
+            assert e.mean() <= 1e-6 and e.max() <= 1e-4
+        else:
+            assert e.mean() <= 2e-5 and (e <= 1e-3).mean() >= 0.999
+
+
+def test_adjoint_matches_central_differences(diff, sgx, oracle):
+    import torch
+    from singularity_gb300 import diff as D
+    N = sgx._native
+    base, tgt, guess = _setup(sgx)
+    target = oracle.diff_render(base, tgt)
+    fd = oracle.diff_fd_gradient(base, guess, target, step=FD_STEP)
+    t_dev = torch.as_tensor(target.astype(np.float32), device="cuda")
+    out = {}
+    for prec in (N.PRECISION_FP64, N.PRECISION_FP32):
+        img = diff.forward(base, guess, D.DiffOptions(precision=prec))
+        out[prec] = diff.backward(_loss_grad_image(img, t_dev))
+    g64, g32 = out[N.PRECISION_FP64], out[N.PRECISION_FP32]
+    rel64 = np.abs(g64 - fd) / np.abs(fd)
+    rel32 = np.abs(g32 - g64) / np.abs(g64)
+    print("fd  ", fd)
+    print("fp64", g64, "rel vs fd", rel64)
+    print("fp32", g32, "rel vs fp64", rel32)
+    # the target image is rendered in FP32 on the device from the FP64 oracle:
+    # its rounding (1e-7) perturbs the loss gradient far below these bars
+    assert np.all(np.sign(g64) == np.sign(fd))
+    assert rel64[2] <= 1e-2 and rel64[3] <= 1e-2, rel64
+    assert np.all(rel32 <= 2e-2), rel32
+
+
+def test_backward_is_deterministic(diff, sgx):
+    import torch
+    base, tgt, guess = _setup(sgx, 40, 30, 2)
+    img = diff.forward(base, guess)
+    g = torch.ones_like(img) * 1e-3
+    a = diff.backward(g)
+    b = diff.backward(g)
+    np.testing.assert_array_equal(a, b)
+    assert diff.stats()["crossing_overflow"] == 0
+
+
+def test_autograd_function(diff, sgx):
+    import torch
+    from singularity_gb300 import diff as D
+    base, tgt, guess = _setup(sgx, 40, 30, 2)
+    target = diff.forward(base, tgt).clone()
+    p = torch.tensor(guess, dtype=torch.float64, requires_grad=True)
+    img = D.render(p, diff, base)
+    loss = torch.mean((img - target) ** 2)
+    loss.backward()
+    direct_img = diff.forward(base, guess)
+    direct = diff.backward(2.0 * (direct_img - target) / direct_img.numel())
+    np.testing.assert_allclose(p.grad.numpy(), direct, rtol=1e-6, atol=1e-12)
+    # a forward in between: the function recomputes its records
+    p.grad = None
+    img = D.render(p, diff, base)
+    diff.forward(base, tgt)
+    torch.mean((img - target) ** 2).backward()
+    np.testing.assert_allclose(p.grad.numpy(), direct, rtol=1e-6, atol=1e-12)
+
+
+def test_errors(diff, sgx):
+    import torch
+    from singularity_gb300 import diff as D
+    base, tgt, guess = _setup(sgx, 16, 16, 1)
+    with pytest.raises(sgx.SgxError):
+        diff.forward(base, (1.5, 1.0, 5.0, 1.0))
+    with pytest.raises(sgx.SgxError):
+        diff.forward(base, guess, D.DiffOptions(precision=sgx._native.PRECISION_MIXED))
+    schw = base.copy()
+    schw.metric_type = 0
+    with pytest.raises(sgx.SgxError):
+        diff.forward(schw, guess)
+
+
+def test_adam_reduces_loss(diff, sgx):
+    """A short recovery run: the loss falls and every parameter moves toward the target."""
+    from singularity_gb300 import diff as D
+    base, tgt, guess = _setup(sgx, 64, 64, 1)
+    target = diff.forward(base, tgt).clone()
+    res = D.fit(diff, base, target, guess, steps=40)
+    print("loss", res.loss[0], "->", res.loss[-1])
+    print("params", res.params[-1], "target", tgt)
+    assert res.loss[-1] < 0.25 * res.loss[0]
+    d0 = np.abs(np.array(guess) - np.array(tgt))
+    d1 = np.abs(res.params[-1] - np.array(tgt))
+    assert np.sum(d1 / d0) < np.sum(np.ones(4))
