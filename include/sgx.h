@@ -282,17 +282,31 @@ sgx_status sgx_render_noalloc(const sgx_uniforms* u, const sgx_render_opts* opts
 /* ---- differentiable render and its adjoint ---------------------------------- */
 /* No counterpart in the reference.  A Kerr render form that is differentiable
  * in four scene parameters, and the gradient of an image loss with respect to
- * them by a reverse (adjoint) sweep of the fixed-step RK4.  The form keeps the
- * reference's integrator, termination and disc shading
- * (geodesic_kernel.cu:300-401, kerr_hamilton.h:97-178) and changes what makes
- * the image discontinuous in the parameters: the camera orbits at azimuth 0
- * with its frame a closed-form function of the inclination, the starfield is
- * off, the annulus edges are soft (each crossing at radius r emits with weight
- * w = S((r - r_in)/e) S((r_out - r)/e), S the cubic smoothstep, e =
- * edge_width * M, through a transmittance that each crossing multiplies by
- * 1 - w), and, when fade_start > 0, images whose ray has swept an angle psi
- * around the hole are faded by 1 - S((psi - fade_start)/fade_width).  The
- * image is W x H x 3 floats, per pixel the mean over samples of
+ * them by a reverse (adjoint) sweep of the fixed-step RK4 with a state
+ * checkpoint every 64 steps.  The form keeps the reference's integrator
+ * (kerr_hamilton.h:97-178), escape test and disc shading
+ * (geodesic_kernel.cu:300-401) and changes what makes the image discontinuous
+ * in the parameters:
+ *   - the camera orbits at azimuth 0, its frame a closed-form function of the
+ *     inclination; the starfield is off;
+ *   - the disc (SGX_DIFF_MODEL_SLAB, the default) is an emitting, absorbing
+ *     layer of half-thickness H = half_thickness * M with the vertical profile
+ *     (1 - (z/H)^2)^2: every RK4 step inside it absorbs
+ *     alpha = w (1 - exp(-kappa rho ds)) (ds the step's length, kappa set so
+ *     that a perpendicular pass has optical depth tau_perp) and adds
+ *     tau alpha c to the colour, tau the ray's transmittance;
+ *     SGX_DIFF_MODEL_CROSSING keeps the reference's equatorial crossings,
+ *     each emitting with weight w through the transmittance (its image jumps
+ *     where a ray grazes the plane, so only r_in and t_scale are smooth);
+ *   - w = S((r - r_in)/e) S((r_out - r)/e) softens the annulus edges (S the
+ *     cubic smoothstep, e = edge_width * M); with fade_start > 0, w is also
+ *     multiplied by 1 - S((psi - fade_start)/fade_width), psi the angle the ray
+ *     has swept around the hole, which removes the rays near the critical
+ *     curve whose images appear and vanish as parameters move;
+ *   - the blackbody fit is blended across its 6600 K branch switch;
+ *   - rays are captured inside the prograde photon orbit radius less 0.05 M
+ *     (the reference's 1.02 r_+ lets the fixed-step RK4 blow up first).
+ * The image is W x H x 3 floats, per pixel the mean over samples of
  * ACES(hdr * exposure) (the reference's tone map, before sRGB encoding). */
 typedef struct sgx_diff_params {
     double spin;     /* a / M, in [0, 1) */
@@ -300,30 +314,35 @@ typedef struct sgx_diff_params {
     double r_in;     /* disc inner radius, units of M */
     double t_scale;  /* multiplies the disc's peak temperature */
 } sgx_diff_params;
+#define SGX_DIFF_MODEL_CROSSING 0u
+#define SGX_DIFF_MODEL_SLAB 1u
 typedef struct sgx_diff_opts {
     uint32_t struct_size;
-    uint32_t precision;  /* SGX_PRECISION_FP32 or SGX_PRECISION_FP64 */
-    float edge_width;    /* soft annulus edge, units of M (0.1) */
-    float fade_start;    /* swept angle where higher-order images fade, rad (pi); <= 0: no fade */
-    float fade_width;    /* fade length, rad (pi / 2) */
-    uint32_t reserved[3];
+    uint32_t precision;    /* SGX_PRECISION_FP32 or SGX_PRECISION_FP64 */
+    float edge_width;      /* soft annulus edge, units of M (0.1) */
+    float fade_start;      /* swept angle where images fade, rad (3 pi / 4); <= 0: no fade */
+    float fade_width;      /* fade length, rad (pi / 2) */
+    uint32_t model;        /* SGX_DIFF_MODEL_SLAB (default) or SGX_DIFF_MODEL_CROSSING */
+    float half_thickness;  /* slab half-thickness, units of M (0.3) */
+    float tau_perp;        /* slab optical depth across (4) */
 } sgx_diff_opts;
 void sgx_diff_opts_default(sgx_diff_opts* opts);
 /* Forward pass: renders the form for `params` with size, samples, distance
  * (|cam_pos|), field of view, mass, r_out, peak temperature, step, max_steps,
  * escape radius, exposure, turbulence, time and the Doppler/redshift flags
  * from `base` (a Kerr uniform block), into d_image (device, W*H*3 floats; NULL:
- * an internal buffer) and keeps what the backward pass needs (a state
- * checkpoint every 64 steps and up to 8 crossings per ray).  Synchronous. */
+ * an internal buffer) and keeps what the backward pass needs (a state and
+ * transmittance checkpoint every 64 steps, (max_steps/64 + 1) * 7 values per
+ * ray).  Synchronous. */
 sgx_status sgx_diff_forward(sgx_context* ctx, const sgx_uniforms* base, const sgx_diff_params* params,
                             const sgx_diff_opts* opts, float* d_image, void* stream);
 /* Backward pass of the last forward: d_grad_image (device, W*H*3 floats) is
  * dLoss/dImage; grad[4] (host) receives dLoss/d(spin, incl, r_in, t_scale).
  * The per-ray terms are summed in a fixed order (deterministic). */
 sgx_status sgx_diff_backward(sgx_context* ctx, const float* d_grad_image, double* grad, void* stream);
-/* Rays of the last forward, and how many crossings beyond the 8 recorded per
- * ray were dropped from the backward pass (0 in normal scenes). */
-sgx_status sgx_diff_stats(sgx_context* ctx, uint64_t* rays, uint64_t* crossing_overflow);
+/* Rays and RK4 steps of the last forward, and (crossing model) how many
+ * crossings beyond the 8 recorded per ray were left out of the backward pass. */
+sgx_status sgx_diff_stats(sgx_context* ctx, uint64_t* rays, uint64_t* steps, uint64_t* crossing_overflow);
 
 /* ---- measurement --------------------------------------------------------- */
 /* No counterpart in the reference: the device's FP32 FMA issue ceiling in

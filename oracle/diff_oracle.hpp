@@ -31,8 +31,10 @@
 //     blends the two branches over 6500-6700 K with S, so colour is continuous
 //     in temperature (identical outside that band);
 //   * the disc temperature scale multiplies the peak temperature.
+//   * a ray is captured inside the prograde photon orbit radius less 0.05 M
+//     instead of at 1.02 r_+ (see diff_trace).
 // Integration is the reference's fixed-step Kerr RK4 with its pole damping
-// (kerr_hamilton.h:165-178), checks and termination as geodesic_kernel.cu:351-401.
+// (kerr_hamilton.h:165-178), checks and escape as geodesic_kernel.cu:351-401.
 
 #pragma once
 
@@ -54,8 +56,20 @@ struct DiffOpts {
     float eps;         // soft-edge width, M (0.1)
     float fade_start;  // swept angle (rad) where higher-order images start to fade; <= 0: no fade
     float fade_width;  // fade length in swept angle (rad)
-    std::uint32_t pad;
+    std::uint32_t model;  // DIFF_MODEL_CROSSING or DIFF_MODEL_SLAB
+    float half_thickness;  // slab: half-thickness H of the emitting layer, M
+    float tau_perp;        // slab: optical depth of a perpendicular pass through the layer
+    float pad0, pad1;
 };
+enum : std::uint32_t { DIFF_MODEL_CROSSING = 0, DIFF_MODEL_SLAB = 1 };
+
+// Slab profile: (1 - (z/H)^2)^2 on |z| < H (integral 16 H / 15), C1 at |z| = H.
+template <class T> inline T slab_profile(T z, T H) {
+    const T q = z / H;
+    if (!(q * q < OLIT(1.0))) return OLIT(0.0);
+    const T b = OLIT(1.0) - q * q;
+    return b * b;
+}
 
 template <class T> inline T smooth01(T x) {
     if (x <= OLIT(0.0)) return OLIT(0.0);
@@ -175,16 +189,43 @@ inline DiffOut<T> diff_trace(const sgx_uniforms& ub, const DiffParams& dp, const
     DiffOut<T> out{v3(OLIT(0.0), OLIT(0.0), OLIT(0.0)), 0u, 0u};
     // kerr_init reads cos(cam_theta) itself; the closed-form frame above agrees with it.
     if (!kerr_init(cam, up_, y, c)) return out;
-    const T hcut = kerr_horizon_cut(Mm, a);
+    // Capture radius: the prograde equatorial photon orbit radius (the smallest
+    // photon orbit; an ingoing ray from outside that gets inside it falls in)
+    // less 0.05 M.  The fixed-step RK4 turns unstable as Delta -> 0, and the
+    // reference's cut at 1.02 r_+ lets a blown-up state emit before it stops.
+    const T r_pro = OLIT(2.0) * Mm * (OLIT(1.0) + M<T>::cos(OLIT(2.0) / OLIT(3.0) * M<T>::acos(-a / Mm)));
+    const T hcut = M<T>::fmax(r_pro - OLIT(0.05) * Mm, kerr_horizon_cut(Mm, a));
     T tau = OLIT(1.0);
     KState<T> prev = y;
     T psi = OLIT(0.0), psi_prev = OLIT(0.0);
     const bool fade = o.fade_start > 0.0f;
     std::uint32_t step = 0;
+    const bool slab = o.model == DIFF_MODEL_SLAB;
+    const T H = T(o.half_thickness) * Mm;
+    const T kappa = T(o.tau_perp) / (OLIT(16.0) / OLIT(15.0) * H);
     for (; step < u.max_steps; ++step) {
         if (!M<T>::isfinite(y.r) || y.r < hcut) break;
         if (y.r > u.escape_r) break;
-        if (u.flags & SGX_FLAG_DISC_ON) {
+        if (slab && (u.flags & SGX_FLAG_DISC_ON) && step > 0) {
+            // emission and absorption of the step prev -> y, evaluated at y
+            const T z = y.r * M<T>::cos(y.theta);
+            const T rho = slab_profile(z, H);
+            T w = smooth01((y.r - r_in) / eps) * smooth01((u.r_out - y.r) / eps);
+            if (fade) w = w * (OLIT(1.0) - smooth01((psi - T(o.fade_start)) / T(o.fade_width)));
+            if (rho > OLIT(0.0) && w > OLIT(0.0)) {
+                const T dr = y.r - prev.r, dth = y.theta - prev.theta, dph = y.phi - prev.phi;
+                const T st = M<T>::sin(y.theta);
+                const T ds = M<T>::sqrt(dr * dr + y.r * y.r * (dth * dth + st * st * dph * dph));
+                const T alpha = w * (OLIT(1.0) - M<T>::exp(-kappa * rho * ds));
+                ++out.crossings;
+                const T T_local = disc_temperature(y.r, r_in, peak_T);
+                V3<T> col = v3(OLIT(0.0), OLIT(0.0), OLIT(0.0));
+                if (T_local > OLIT(0.0)) col = diff_disc_colour(up_, c, dcam, y.r, y.phi, T_local);
+                out.hdr = vadd(out.hdr, vmul(col, tau * alpha));
+                tau = tau * (OLIT(1.0) - alpha);
+            }
+        }
+        if (!slab && (u.flags & SGX_FLAG_DISC_ON)) {
             const Crossing<T> x = equatorial_crossing(prev.theta, y.theta);
             if (x.crossed) {
                 const T r_c = lerp_s(prev.r, y.r, x.frac);

@@ -67,6 +67,7 @@ inline bool operator>=(Counted a, Counted b) { return a.v >= b.v; }
 template <class T> struct M;
 template <> struct M<float> {
     static float sqrt(float x) { return ::sqrtf(x); }
+    static float exp(float x) { return ::expf(x); }
     static float sin(float x) { return ::sinf(x); }
     static float cos(float x) { return ::cosf(x); }
     static float acos(float x) { return ::acosf(x); }
@@ -80,6 +81,7 @@ template <> struct M<float> {
 };
 template <> struct M<double> {
     static double sqrt(double x) { return std::sqrt(x); }
+    static double exp(double x) { return std::exp(x); }
     static double sin(double x) { return std::sin(x); }
     static double cos(double x) { return std::cos(x); }
     static double acos(double x) { return std::acos(x); }
@@ -421,6 +423,20 @@ inline V3<T> disc_shade(const Params<T>& u, T r_cross, T phi_cross, T T_local, T
     return vmul(col, flux * bands * g2 * g2);
 }
 
+// Radius-adaptive step (geodesic_math.h:91-96), gated by SING_FLAG_ADAPTIVE_STEP:
+// h = h_base * clamp(r / 6M, 1, 40).  The reference applies it in its WebGPU
+// kernel for both metrics (geodesic_kernel.wgsl:117-122,486,591); its CUDA
+// kernel ignores the flag.
+template <class T> inline T radius_adaptive_h(T h_base, T r, T mass_M) {
+    T mult = r / (OLIT(6.0) * mass_M);
+    mult = (mult < OLIT(1.0)) ? OLIT(1.0) : mult;
+    mult = (mult > OLIT(40.0)) ? OLIT(40.0) : mult;
+    return h_base * mult;
+}
+template <class T> inline T step_h(const Params<T>& u, T r) {
+    return (u.flags & SGX_FLAG_ADAPTIVE_STEP) ? radius_adaptive_h(u.h_step, r, u.mass_M) : u.h_step;
+}
+
 template <class T> inline TraceOut<T> trace_schwarzschild(const CamRay<T>& cam, const Params<T>& u) {
     SState<T> s;
     s.t = OLIT(0.0);
@@ -476,7 +492,7 @@ template <class T> inline TraceOut<T> trace_schwarzschild(const CamRay<T>& cam, 
         prev_theta = s.theta;
         prev_r = s.r;
         prev_uphi = s.uphi;
-        s = schw_rk4(s, u.h_step, u.rs);
+        s = schw_rk4(s, step_h(u, s.r), u.rs);
     }
     return {black, u.max_steps, TERM_BUDGET};
 }
@@ -683,7 +699,7 @@ template <class T> inline TraceOut<T> trace_kerr(const CamRay<T>& cam, const Par
         }
         prev_theta = s.theta;
         prev_r = s.r;
-        s = kerr_rk4(s, u.h_step, c);
+        s = kerr_rk4(s, step_h(u, s.r), c);
     }
     return {black, u.max_steps, TERM_BUDGET};
 }

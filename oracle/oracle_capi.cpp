@@ -216,6 +216,38 @@ void oracle_schw_rhs_f64(const double* y8, double rs, double* d8) {
     for (int i = 0; i < 8; ++i) d8[i] = o[i];
 }
 
+// Integrates a Schwarzschild state with fixed h or the radius-adaptive step
+// until r > r_out (test_adaptive_step.cpp:71-80); returns the steps taken, -1 if
+// the budget ran out.  max_e / max_l get the largest relative drift of
+// E = (1 - rs/r) u^t and L = r^2 sin^2(theta) u^phi along the way.
+int oracle_schw_integrate_f32(float* y8, float h_base, float rs, float r_out, int adaptive, int budget,
+                              float* max_e, float* max_l) {
+    oracle::SState<float> y{y8[0], y8[1], y8[2], y8[3], y8[4], y8[5], y8[6], y8[7]};
+    auto energy = [&](const oracle::SState<float>& s) { return (1.0f - rs / s.r) * s.ut; };
+    auto ang = [&](const oracle::SState<float>& s) {
+        const float st = std::sin(s.theta);
+        return s.r * s.r * st * st * s.uphi;
+    };
+    const float E0 = energy(y), L0 = ang(y);
+    float me = 0.0f, ml = 0.0f;
+    int steps = -1;
+    for (int i = 0; i < budget; ++i) {
+        const float h = adaptive ? oracle::radius_adaptive_h(h_base, y.r, 0.5f * rs) : h_base;
+        y = oracle::schw_rk4(y, h, rs);
+        me = std::max(me, std::fabs(energy(y) - E0) / std::fabs(E0));
+        ml = std::max(ml, std::fabs(ang(y) - L0) / std::fabs(L0));
+        if (y.r > r_out) {
+            steps = i + 1;
+            break;
+        }
+    }
+    const float o[8] = {y.t, y.r, y.theta, y.phi, y.ut, y.ur, y.utheta, y.uphi};
+    for (int i = 0; i < 8; ++i) y8[i] = o[i];
+    if (max_e) *max_e = me;
+    if (max_l) *max_l = ml;
+    return steps;
+}
+
 // Equatorial crossing (disc_intersection.h:30-55): returns crossed, writes frac.
 int oracle_crossing_f32(float th_prev, float th_curr, float* frac) {
     const oracle::Crossing<float> x = oracle::equatorial_crossing(th_prev, th_curr);

@@ -47,19 +47,23 @@ class DiffParams(C.Structure):
 
 
 class DiffOpts(C.Structure):
-    _fields_ = [("eps", C.c_float), ("fade_start", C.c_float), ("fade_width", C.c_float), ("pad", C.c_uint32)]
+    _fields_ = [("eps", C.c_float), ("fade_start", C.c_float), ("fade_width", C.c_float), ("model", C.c_uint32),
+                ("half_thickness", C.c_float), ("tau_perp", C.c_float), ("pad0", C.c_float), ("pad1", C.c_float)]
 
 
-DIFF_FADE = (math.pi, math.pi / 2)  # the library's default winding fade (start, width), rad
+DIFF_MODEL_CROSSING, DIFF_MODEL_SLAB = 0, 1
+
+
+DIFF_FADE = (0.75 * math.pi, 0.5 * math.pi)  # the library's default winding fade (start, width), rad
 
 
 def diff_render(u, params, eps: float = 0.1, precision: str = "f64", threads: int | None = None,
-                fade=DIFF_FADE) -> np.ndarray:
+                fade=DIFF_FADE, model: int = 1, half_thickness: float = 0.3, tau_perp: float = 4.0) -> np.ndarray:
     """LDR image (H, W, 3) of the differentiable form at params = (spin, incl_rad, r_in, t_scale).
     fade = (start, width) of the winding fade; start <= 0 turns it off."""
     threads = threads or default_threads()
     p = DiffParams(*[float(x) for x in params])
-    o = DiffOpts(eps, fade[0], fade[1], 0)
+    o = DiffOpts(eps, fade[0], fade[1], model, half_thickness, tau_perp, 0.0, 0.0)
     dt = np.float32 if precision == "f32" else np.float64
     out = np.zeros((u.height, u.width, 3), dtype=dt)
     fn = lib().oracle_diff_render_f32 if precision == "f32" else lib().oracle_diff_render_f64
@@ -69,18 +73,48 @@ def diff_render(u, params, eps: float = 0.1, precision: str = "f64", threads: in
     return out
 
 
+def diff_trace(u, params, gx, gy, s, eps: float = 0.1, fade=DIFF_FADE, model: int = 1, half_thickness: float = 0.3,
+               tau_perp: float = 4.0, threads: int | None = None):
+    """Per-sample FP64 HDR colour, steps and emitting events of the differentiable form."""
+    threads = threads or default_threads()
+    gx = np.ascontiguousarray(gx, dtype=np.uint32)
+    gy = np.ascontiguousarray(gy, dtype=np.uint32)
+    s = np.ascontiguousarray(s, dtype=np.uint32)
+    n = gx.size
+    p = DiffParams(*[float(x) for x in params])
+    o = DiffOpts(eps, fade[0], fade[1], model, half_thickness, tau_perp, 0.0, 0.0)
+    hdr = np.zeros((n, 3), dtype=np.float64)
+    steps = np.zeros(n, dtype=np.uint32)
+    events = np.zeros(n, dtype=np.uint32)
+    rc = lib().oracle_diff_trace_f64(_u(u), C.byref(p), C.byref(o), C.c_int64(n), _p(gx), _p(gy), _p(s), _p(hdr),
+                                     _p(steps), _p(events), C.c_int(threads))
+    if rc != 0:
+        raise RuntimeError("oracle diff trace failed")
+    return hdr, steps, events
+
+
 def diff_fd_gradient(u, params, target: np.ndarray, step: float = 1e-3, eps: float = 0.1,
-                     precision: str = "f64", fade=DIFF_FADE) -> np.ndarray:
+                     precision: str = "f64", fade=DIFF_FADE, **form) -> np.ndarray:
     """Central finite differences (step in each parameter) of mean((I - target)^2)."""
     params = np.asarray(params, dtype=np.float64)
     g = np.zeros(4)
     for k in range(4):
         d = np.zeros(4)
         d[k] = step
-        lp = np.mean((diff_render(u, params + d, eps, precision, fade=fade).astype(np.float64) - target) ** 2)
-        lm = np.mean((diff_render(u, params - d, eps, precision, fade=fade).astype(np.float64) - target) ** 2)
+        lp = np.mean((diff_render(u, params + d, eps, precision, fade=fade, **form).astype(np.float64) - target) ** 2)
+        lm = np.mean((diff_render(u, params - d, eps, precision, fade=fade, **form).astype(np.float64) - target) ** 2)
         g[k] = (lp - lm) / (2 * step)
     return g
+
+
+def schw_integrate(y8, h_base: float, rs: float, r_out: float, adaptive: bool, budget: int = 400000):
+    """FP32 Schwarzschild integration to r > r_out, fixed or radius-adaptive
+    step: (final state, steps or -1, max |dE/E|, max |dL/L|)."""
+    y = np.ascontiguousarray(y8, dtype=np.float32).copy()
+    me, ml = C.c_float(), C.c_float()
+    n = lib().oracle_schw_integrate_f32(_p(y), C.c_float(h_base), C.c_float(rs), C.c_float(r_out),
+                                        C.c_int(int(adaptive)), C.c_int(budget), C.byref(me), C.byref(ml))
+    return y, n, me.value, ml.value
 
 
 def build(ref: bool = True) -> None:

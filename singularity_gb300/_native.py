@@ -131,7 +131,11 @@ class DiffParams(C.Structure):
 
 class DiffOpts(C.Structure):
     _fields_ = [("struct_size", C.c_uint32), ("precision", C.c_uint32), ("edge_width", C.c_float),
-                ("fade_start", C.c_float), ("fade_width", C.c_float), ("reserved", C.c_uint32 * 3)]
+                ("fade_start", C.c_float), ("fade_width", C.c_float), ("model", C.c_uint32),
+                ("half_thickness", C.c_float), ("tau_perp", C.c_float)]
+
+
+DIFF_MODEL_CROSSING, DIFF_MODEL_SLAB = 0, 1
 
 
 _P = C.c_void_p
@@ -177,7 +181,7 @@ SIGNATURES = [
     ("sgx_diff_opts_default", None, [C.POINTER(DiffOpts)]),
     ("sgx_diff_forward", C.c_int, [_P, C.POINTER(Uniforms), C.POINTER(DiffParams), C.POINTER(DiffOpts), _P, _P]),
     ("sgx_diff_backward", C.c_int, [_P, _P, C.POINTER(C.c_double), _P]),
-    ("sgx_diff_stats", C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    ("sgx_diff_stats", C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     ("sgx_measure_fp32_peak", C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
     ("sgx_trace_samples", C.c_int, [_P, C.POINTER(Uniforms), C.POINTER(RenderOpts), C.c_uint64, _U32P, _U32P,
                                     _U32P, _F32P, _U32P, _U32P]),

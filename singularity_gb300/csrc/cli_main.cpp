@@ -66,6 +66,7 @@ void print_help() {
         "  --exposure X                  exposure before tone mapping (default 1.8)\n"
         "  --turbulence X                disc band amplitude (default 0.5)\n"
         "  --h-step H / --max-steps N    integrator step and budget (default 0.4 / 2500)\n"
+        "  --adaptive-step               radius-adaptive fixed step h * clamp(r / 6M, 1, 40)\n"
         "  --disc-inner-isco             disc inner edge at the prograde ISCO of the spin\n"
         "  --use-scene-camera            take camera_distance/elevation/fov from the scene file\n"
         "  --use-scene-integrator        take h_step/max_steps from the scene file\n"
@@ -173,7 +174,7 @@ int main(int argc, char** argv) {
     // extensions
     sgx_render_opts opts;
     sgx_render_opts_default(&opts);
-    bool have_opts = false, isco_inner = false, scene_camera = false, scene_integrator = false, pfm = false;
+    bool have_opts = false, isco_inner = false, scene_camera = false, scene_integrator = false, pfm = false, adaptive_step = false;
     float peak_temp = -1.0f, exposure = -1.0f, turbulence = -1.0f, h_step = 0.0f;
     std::uint32_t max_steps = 0;
 
@@ -265,6 +266,8 @@ int main(int argc, char** argv) {
             h_step = std::strtof(argv[++i], nullptr);
         } else if (a == "--max-steps" && has_val) {
             max_steps = static_cast<std::uint32_t>(std::strtoul(argv[++i], nullptr, 10));
+        } else if (a == "--adaptive-step") {
+            adaptive_step = true;
         } else if (a == "--disc-inner-isco") {
             isco_inner = true;
         } else if (a == "--use-scene-camera") {
@@ -318,6 +321,7 @@ int main(int argc, char** argv) {
     if (exposure >= 0.0f) scene.exposure = exposure;
     if (turbulence >= 0.0f) scene.disc_turbulence = turbulence;
     if (h_step > 0.0f) scene.h_step = h_step;
+    if (adaptive_step) scene.adaptive_step_on = true;
     if (max_steps > 0) scene.max_steps = max_steps;
 
     if (frames > 1 && output_pattern.empty()) {

@@ -40,6 +40,7 @@ template <> struct DM<float> {
     static __device__ __forceinline__ float atan2_(float y, float x) { return atan2f(y, x); }
     static __device__ __forceinline__ float pow_(float x, float y) { return powf(x, y); }
     static __device__ __forceinline__ float log_(float x) { return logf(x); }
+    static __device__ __forceinline__ float exp_(float x) { return expf(x); }
     static __device__ __forceinline__ float fmin_(float a, float b) { return fminf(a, b); }
     static __device__ __forceinline__ float fmax_(float a, float b) { return fmaxf(a, b); }
     static __device__ __forceinline__ float rcp_(float x) { return 1.0f / x; }
@@ -60,6 +61,7 @@ template <> struct DM<double> {
     static __device__ __forceinline__ double atan2_(double y, double x) { return atan2(y, x); }
     static __device__ __forceinline__ double pow_(double x, double y) { return pow(x, y); }
     static __device__ __forceinline__ double log_(double x) { return log(x); }
+    static __device__ __forceinline__ double exp_(double x) { return exp(x); }
     static __device__ __forceinline__ double fmin_(double a, double b) { return fmin(a, b); }
     static __device__ __forceinline__ double fmax_(double a, double b) { return fmax(a, b); }
     static __device__ __forceinline__ double rcp_(double x) { return 1.0 / x; }
@@ -494,6 +496,17 @@ __device__ __forceinline__ KS<T> kerr_rhs(const KS<T>& s, const View<T>& v, cons
 
 template <class T> __device__ __forceinline__ KS<T> ks_axpy(const KS<T>& y, const KS<T>& k, T f) {
     return KS<T>{y.r + k.r * f, y.th + k.th * f, y.ph + k.ph * f, y.pr + k.pr * f, y.pth + k.pth * f};
+}
+
+// Step of the fixed-step integrators: h_step, or with SGX_FLAG_ADAPTIVE_STEP
+// the radius-adaptive h_step * clamp(r / 6M, 1, 40) (geodesic_math.h:91-96,
+// applied by the reference's WebGPU kernel, geodesic_kernel.wgsl:117-122).
+template <class T> __device__ __forceinline__ T fixed_step_h(const View<T>& v, T r) {
+    if (!(v.flags & SGX_FLAG_ADAPTIVE_STEP)) return v.h;
+    T mult = r / (DLIT(6.0) * v.M);
+    mult = (mult < DLIT(1.0)) ? DLIT(1.0) : mult;
+    mult = (mult > DLIT(40.0)) ? DLIT(40.0) : mult;
+    return v.h * mult;
 }
 
 // Fixed-step RK4 with the reference's near-pole damping (kerr_hamilton.h:165-178).

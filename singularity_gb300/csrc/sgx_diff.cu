@@ -30,6 +30,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <string>
 
 #include "sgx.h"
 #include "sgx_context.hpp"
@@ -43,13 +44,14 @@ namespace {
 using namespace sgxd;
 
 constexpr int kCk = 64;       // steps between checkpoints
-constexpr int kMaxCross = 8;  // crossings recorded per ray
+constexpr int kMaxCross = 8;  // crossings recorded per ray (crossing model)
 constexpr int NS = 6;         // state: r, theta, phi, p_r, p_theta, psi (swept angle)
+constexpr int NC = NS + 1;    // checkpoint: state and transmittance
 
 template <class T> struct DiffConst {
     T M, dcam, aspect, tanh_, width_f, height_f;
     T r_out, peak_T, escape_r, h, exposure, turbulence, time_sec;
-    T eps, fade_start, fade_width;
+    T eps, fade_start, fade_width, H, kappa;
     std::uint32_t width, height, spp, max_steps, flags, fade;
 };
 
@@ -61,17 +63,17 @@ template <class T> struct DiffParamsT {
 template <class T> struct DiffBufs {
     std::uint64_t n;  // rays
     std::uint32_t slots;
-    T* ckpt;          // [slots][NS][n]
+    T* ckpt;          // [slots][NC][n]
     T* hdr;           // [3][n]
     std::uint32_t* nsteps;
-    std::uint32_t* ncross;
-    std::uint32_t* xk;  // [kMaxCross][n]
+    std::uint32_t* ncross;  // crossings (crossing model) or emitting steps (slab)
+    std::uint32_t* xk;  // [kMaxCross][n]: crossing steps; slab: [0] = last emitting step
     T* xw;              // [kMaxCross][n]
     T* xc;              // [kMaxCross][3][n]
     double* grads;      // [4][n]
     const T* ox;        // [spp] sub-pixel offsets
     const T* oy;
-    unsigned long long* overflow;
+    unsigned long long* overflow;  // [0] dropped crossings, [1] steps of all rays
 };
 
 template <class S> __device__ __forceinline__ S selv(bool c, const S& a, const S& b) { return c ? a : b; }
@@ -293,6 +295,43 @@ __device__ __forceinline__ bool init_g(const S& a, const S& incl, const DiffCons
     return true;
 }
 
+// Slab emission of the step y0 -> y1, evaluated at y1: absorption alpha and
+// colour; false (alpha = 0) outside the layer, the annulus or past the fade.
+template <class S, class T>
+__device__ __forceinline__ bool slab_g(const S& r0, const S& th0, const S& ph0, const S& r1, const S& th1,
+                                       const S& ph1, const S& psi1, const S& L, const S& a, const S& r_in,
+                                       const S& t_scale, const DiffConst<T>& k, S* col, S& alpha) {
+    const S q = r1 * DM<S>::cos_(th1) / S(k.H);
+    if (!(value_of(q) * value_of(q) < T(1))) return false;
+    S w = smooth01((r1 - r_in) / S(k.eps)) * smooth01((S(k.r_out) - r1) / S(k.eps));
+    if (k.fade) w = w * (S(T(1)) - smooth01((psi1 - S(k.fade_start)) / S(k.fade_width)));
+    if (!(value_of(w) > T(0))) return false;
+    const S b = S(T(1)) - q * q;
+    const S rho = b * b;
+    const S dr = r1 - r0, dth = th1 - th0, dph = ph1 - ph0;
+    const S st = DM<S>::sin_(th1);
+    const S ds = DM<S>::sqrt_(dr * dr + r1 * r1 * (dth * dth + st * st * dph * dph));
+    alpha = w * (S(T(1)) - DM<S>::exp_(-(S(k.kappa) * rho * ds)));
+    const S T_local = disc_temperature(r1, r_in, S(k.peak_T) * t_scale);
+    if (value_of(T_local) > T(0)) {
+        disc_colour_g(r1, ph1, L, a, r_in, T_local, k, col);
+    } else {
+        col[0] = col[1] = col[2] = S(T(0));
+    }
+    return true;
+}
+
+// Capture radius of the form: the prograde equatorial photon orbit radius
+// (the smallest photon orbit: an ingoing ray from outside that gets inside it
+// falls in) less 0.05 M, at least the reference's 1.02 r_+.  Closer to the
+// horizon the fixed-step RK4 turns unstable (p_r ~ 1/Delta) and a blown-up
+// state could emit.
+template <class T> __device__ __forceinline__ T capture_radius(T M, T a) {
+    const T r_pro = T(2) * M * (T(1) + DM<T>::cos_(T(2) / T(3) * DM<T>::acos_(-a / M)));
+    const T hcut = DM<T>::lit(1.02f, 1.02) * (M + DM<T>::sqrt_(DM<T>::fmax_(M * M - a * a, T(0))));
+    return DM<T>::fmax_(r_pro - DM<T>::lit(0.05f, 0.05) * M, hcut);
+}
+
 template <class T>
 __device__ __forceinline__ void ray_pixel(const DiffConst<T>& k, std::uint64_t id, std::uint32_t& gx, std::uint32_t& gy,
                                           std::uint32_t& s) {
@@ -303,59 +342,92 @@ __device__ __forceinline__ void ray_pixel(const DiffConst<T>& k, std::uint64_t i
 }
 
 template <class T>
+__device__ __forceinline__ void store_ckpt(const DiffBufs<T>& b, std::uint64_t id, std::uint32_t n, const T* y, T tau) {
+    const std::uint64_t base = std::uint64_t(n / kCk) * NC * b.n + id;
+#pragma unroll
+    for (int i = 0; i < NS; ++i) b.ckpt[base + std::uint64_t(i) * b.n] = y[i];
+    b.ckpt[base + std::uint64_t(NS) * b.n] = tau;
+}
+
+// Forward: one thread per ray.  SLAB: emission and absorption every step in
+// the layer; otherwise soft crossings of the equatorial plane.
+template <class T, bool SLAB>
 __global__ void __launch_bounds__(128) diff_forward_kernel(DiffConst<T> k, DiffParamsT<T> p, DiffBufs<T> b) {
     const std::uint64_t id = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (id >= b.n) return;
-    std::uint32_t gx, gy, s;
-    ray_pixel(k, id, gx, gy, s);
-    const T a = p.spin * k.M;
-    const T r_in = p.r_in * k.M;
-    T y[NS], prev[NS], E, L;
-    T hdr[3] = {T(0), T(0), T(0)};
-    std::uint32_t n = 0, nc = 0;
-    const bool ok = init_g<T, T>(a, p.incl, k, gx, gy, b.ox[s], b.oy[s], y, E, L);
-    if (ok) {
-        const T hcut = T(1.02) * (k.M + DM<T>::sqrt_(DM<T>::fmax_(k.M * k.M - a * a, T(0))));
-        T tau = T(1);
-#pragma unroll
-        for (int i = 0; i < NS; ++i) prev[i] = y[i];
-        for (; n < k.max_steps; ++n) {
-            if (n % kCk == 0) {
-                const std::uint64_t base = std::uint64_t(n / kCk) * NS * b.n + id;
-#pragma unroll
-                for (int i = 0; i < NS; ++i) b.ckpt[base + std::uint64_t(i) * b.n] = y[i];
-            }
-            if (!isfinite(y[0]) || y[0] < hcut) break;
-            if (y[0] > k.escape_r) break;
-            const T mid = T(1.5707963267948966);
-            if ((k.flags & SGX_FLAG_DISC_ON) && n > 0 && ((prev[1] - mid) * (y[1] - mid) < T(0))) {
-                T col[3], w;
-                crossing_g<T, T>(prev[0], prev[1], prev[5], y[0], y[1], y[2], y[5], L, a, r_in, p.t_scale, k, col, w);
-                if (w > T(0)) {
-                    if (nc < kMaxCross) {
-                        b.xk[std::uint64_t(nc) * b.n + id] = n;
-                        b.xw[std::uint64_t(nc) * b.n + id] = w;
-#pragma unroll
-                        for (int c = 0; c < 3; ++c) b.xc[(std::uint64_t(nc) * 3 + c) * b.n + id] = col[c];
-                    } else {
-                        atomicAdd(b.overflow, 1ull);
-                    }
-                    ++nc;
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) hdr[c] = hdr[c] + tau * w * col[c];
-                    tau = tau * (T(1) - w);
-                    if (!(tau > T(0))) break;
-                }
-            }
+    std::uint32_t n = 0;
+    if (id < b.n) {
+        std::uint32_t gx, gy, s;
+        ray_pixel(k, id, gx, gy, s);
+        const T a = p.spin * k.M;
+        const T r_in = p.r_in * k.M;
+        T y[NS], prev[NS], E, L;
+        T hdr[3] = {T(0), T(0), T(0)};
+        std::uint32_t nc = 0, last = 0;
+        if (init_g<T, T>(a, p.incl, k, gx, gy, b.ox[s], b.oy[s], y, E, L)) {
+            const T hcut = capture_radius(k.M, a);
+            const bool disc = (k.flags & SGX_FLAG_DISC_ON) != 0u;
+            T tau = T(1);
 #pragma unroll
             for (int i = 0; i < NS; ++i) prev[i] = y[i];
-            step_g<T, T>(prev, E, L, a, k.M, k.h, k.fade != 0u, y);
+            for (; n < k.max_steps; ++n) {
+                if (!SLAB && n % kCk == 0) store_ckpt(b, id, n, y, tau);
+                if (!isfinite(y[0]) || y[0] < hcut) break;
+                if (y[0] > k.escape_r) break;
+                if constexpr (SLAB) {
+                    T col[3], alpha;
+                    if (disc && n > 0 &&
+                        slab_g<T, T>(prev[0], prev[1], prev[2], y[0], y[1], y[2], y[5], L, a, r_in, p.t_scale, k,
+                                     col, alpha)) {
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) hdr[c] = hdr[c] + tau * alpha * col[c];
+                        tau = tau * (T(1) - alpha);
+                        ++nc;
+                        last = n;
+                    }
+                    if (n % kCk == 0) store_ckpt(b, id, n, y, tau);
+                } else {
+                    const T mid = T(1.5707963267948966);
+                    if (disc && n > 0 && ((prev[1] - mid) * (y[1] - mid) < T(0))) {
+                        T col[3], w;
+                        crossing_g<T, T>(prev[0], prev[1], prev[5], y[0], y[1], y[2], y[5], L, a, r_in, p.t_scale,
+                                         k, col, w);
+                        if (w > T(0)) {
+                            if (nc < kMaxCross) {
+                                b.xk[std::uint64_t(nc) * b.n + id] = n;
+                                b.xw[std::uint64_t(nc) * b.n + id] = w;
+#pragma unroll
+                                for (int c = 0; c < 3; ++c) b.xc[(std::uint64_t(nc) * 3 + c) * b.n + id] = col[c];
+                            } else {
+                                atomicAdd(b.overflow, 1ull);
+                            }
+                            ++nc;
+#pragma unroll
+                            for (int c = 0; c < 3; ++c) hdr[c] = hdr[c] + tau * w * col[c];
+                            tau = tau * (T(1) - w);
+                            if (!(tau > T(0))) break;
+                        }
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < NS; ++i) prev[i] = y[i];
+                step_g<T, T>(prev, E, L, a, k.M, k.h, k.fade != 0u, y);
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) b.hdr[std::uint64_t(c) * b.n + id] = hdr[c];
+        b.nsteps[id] = n;
+        if constexpr (SLAB) {
+            b.ncross[id] = nc;
+            b.xk[id] = last;
+        } else {
+            b.ncross[id] = nc < kMaxCross ? nc : kMaxCross;
         }
     }
+    // steps of the launch, one atomic per warp
+    unsigned long long v = n;
 #pragma unroll
-    for (int c = 0; c < 3; ++c) b.hdr[std::uint64_t(c) * b.n + id] = hdr[c];
-    b.nsteps[id] = n;
-    b.ncross[id] = nc < kMaxCross ? nc : kMaxCross;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31u) == 0u) atomicAdd(b.overflow + 1, v);
 }
 
 // Per pixel: mean over samples of ACES(hdr * exposure) (geodesic_kernel.cu:482-503).
@@ -383,15 +455,46 @@ template <class T> __device__ __forceinline__ T aces_d(T x) {
     return ((T(2) * a * x + bb) * D - N * (T(2) * c * x + d)) / (D * D);
 }
 
+// lam <- J^T lam + pend for the step y_{k-1} -> y_k (J over the 6 state
+// components), and the step's terms of dLoss/d(E, L, a).
 template <class T>
+__device__ __forceinline__ void step_adjoint(const T* yp, T E, T L, T a, const DiffConst<T>& k, bool fade, T* lam,
+                                             const T* pend, T& muE, T& muL, T& mua) {
+    using D9 = Dual<T, 9>;
+    D9 yd[NS], od[NS];
+#pragma unroll
+    for (int i = 0; i < NS; ++i) yd[i] = D9::var(yp[i], i);
+    step_g<D9, T>(yd, D9::var(E, 6), D9::var(L, 7), D9::var(a, 8), k.M, k.h, fade, od);
+    T nl[NS];
+#pragma unroll
+    for (int i = 0; i < NS; ++i) {
+        T acc = T(0);
+#pragma unroll
+        for (int j = 0; j < NS; ++j) acc += lam[j] * od[j].d[i];
+        nl[i] = acc;
+    }
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+        muE += lam[j] * od[j].d[6];
+        muL += lam[j] * od[j].d[7];
+        mua += lam[j] * od[j].d[8];
+    }
+#pragma unroll
+    for (int i = 0; i < NS; ++i) lam[i] = nl[i] + pend[i];
+}
+
+// Adjoint: one thread per ray, a reverse sweep from the ray's last emitting
+// step to the camera, one checkpoint segment at a time.
+template <class T, bool SLAB>
 __global__ void __launch_bounds__(128) diff_backward_kernel(DiffConst<T> k, DiffParamsT<T> p, DiffBufs<T> b,
                                                             const float* __restrict__ gimg) {
     const std::uint64_t id = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (id >= b.n) return;
     double* gout = b.grads;
     const std::uint32_t nc = b.ncross[id];
-    const std::uint32_t n = b.nsteps[id];
-    if (nc == 0 || n == 0) {
+    // the last step whose state the image depends on
+    const std::uint32_t klast = nc == 0 ? 0u : (SLAB ? b.xk[id] : b.xk[std::uint64_t(nc - 1) * b.n + id]);
+    if (klast == 0) {
 #pragma unroll
         for (int q = 0; q < 4; ++q) gout[std::uint64_t(q) * b.n + id] = 0.0;
         return;
@@ -406,31 +509,6 @@ __global__ void __launch_bounds__(128) diff_backward_kernel(DiffConst<T> k, Diff
         const T x = b.hdr[std::uint64_t(c) * b.n + id] * k.exposure;
         g[c] = T(gimg[pix * 3 + c]) * inv_spp * aces_d(x) * k.exposure;
     }
-    // Transmittance chain: colour = sum_j tau_j w_j c_j, tau_{j+1} = tau_j (1 - w_j).
-    T w[kMaxCross], gcs[kMaxCross], gw[kMaxCross], c3[kMaxCross][3];
-    std::uint32_t xk[kMaxCross];
-    for (std::uint32_t j = 0; j < nc; ++j) {
-        xk[j] = b.xk[std::uint64_t(j) * b.n + id];
-        w[j] = b.xw[std::uint64_t(j) * b.n + id];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) c3[j][c] = b.xc[(std::uint64_t(j) * 3 + c) * b.n + id];
-    }
-    {
-        T R[3] = {T(0), T(0), T(0)};
-        T tau_j[kMaxCross];
-        T tau = T(1);
-        for (std::uint32_t j = 0; j < nc; ++j) {
-            tau_j[j] = tau;
-            tau = tau * (T(1) - w[j]);
-        }
-        for (int j = int(nc) - 1; j >= 0; --j) {
-            // gcs[j] = tau_j w_j (g . dc/dx) scale; gw[j] = tau_j g.(c_j - R_{j+1})
-            gcs[j] = tau_j[j] * w[j];
-            gw[j] = tau_j[j] * (g[0] * (c3[j][0] - R[0]) + g[1] * (c3[j][1] - R[1]) + g[2] * (c3[j][2] - R[2]));
-#pragma unroll
-            for (int c = 0; c < 3; ++c) R[c] = w[j] * c3[j][c] + (T(1) - w[j]) * R[c];
-        }
-    }
     const T a = p.spin * k.M;
     const T r_in = p.r_in * k.M;
     T E, L, y0[NS];
@@ -438,66 +516,121 @@ __global__ void __launch_bounds__(128) diff_backward_kernel(DiffConst<T> k, Diff
 
     T lam[NS] = {T(0), T(0), T(0), T(0), T(0), T(0)};
     T muE = T(0), muL = T(0), mua = T(0), g_a = T(0), g_rin = T(0), g_ts = T(0);
-    T Y[kCk + 1][NS];
     const bool fade = k.fade != 0u;
-    const int mlast = int((n - 1) / kCk);
+    T Y[kCk + 1][NS];
+
+    // Crossing model: seeds of the transmittance chain
+    //   colour = sum_j tau_j w_j c_j,  tau_{j+1} = tau_j (1 - w_j):
+    //   dcolour/dc_j = tau_j w_j,  dcolour/dw_j = tau_j (c_j - R_{j+1}),
+    //   R_j = w_j c_j + (1 - w_j) R_{j+1}.
+    T xcs[kMaxCross], xgw[kMaxCross];
+    std::uint32_t xkk[kMaxCross];
+    if constexpr (!SLAB) {
+        T w[kMaxCross], c3[kMaxCross][3], tau_j[kMaxCross];
+        T tau = T(1);
+        for (std::uint32_t j = 0; j < nc; ++j) {
+            xkk[j] = b.xk[std::uint64_t(j) * b.n + id];
+            w[j] = b.xw[std::uint64_t(j) * b.n + id];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) c3[j][c] = b.xc[(std::uint64_t(j) * 3 + c) * b.n + id];
+            tau_j[j] = tau;
+            tau = tau * (T(1) - w[j]);
+        }
+        T R[3] = {T(0), T(0), T(0)};
+        for (int j = int(nc) - 1; j >= 0; --j) {
+            xcs[j] = tau_j[j] * w[j];
+            xgw[j] = tau_j[j] * (g[0] * (c3[j][0] - R[0]) + g[1] * (c3[j][1] - R[1]) + g[2] * (c3[j][2] - R[2]));
+#pragma unroll
+            for (int c = 0; c < 3; ++c) R[c] = w[j] * c3[j][c] + (T(1) - w[j]) * R[c];
+        }
+    }
+    // Slab model: the same chain over every emitting step, R carried through the sweep.
+    T R[3] = {T(0), T(0), T(0)};
+    T tb[kCk + 1];
+
+    const int mlast = int((klast - 1) / kCk);
     for (int m = mlast; m >= 0; --m) {
         const std::uint32_t kbeg = std::uint32_t(m) * kCk;
-        const std::uint32_t kend = (kbeg + kCk < n) ? kbeg + kCk : n;
-        const std::uint64_t cb = std::uint64_t(m) * NS * b.n + id;
+        const std::uint32_t kend = (kbeg + kCk < klast) ? kbeg + kCk : klast;
+        const std::uint64_t cb = std::uint64_t(m) * NC * b.n + id;
 #pragma unroll
         for (int i = 0; i < NS; ++i) Y[0][i] = b.ckpt[cb + std::uint64_t(i) * b.n];
-        for (std::uint32_t kk = kbeg + 1; kk <= kend; ++kk) step_g<T, T>(Y[kk - 1 - kbeg], E, L, a, k.M, k.h, fade, Y[kk - kbeg]);
+        T tau = b.ckpt[cb + std::uint64_t(NS) * b.n];
+        for (std::uint32_t kk = kbeg + 1; kk <= kend; ++kk) {
+            const T* yp = Y[kk - 1 - kbeg];
+            T* yc = Y[kk - kbeg];
+            step_g<T, T>(yp, E, L, a, k.M, k.h, fade, yc);
+            if constexpr (SLAB) {
+                tb[kk - kbeg] = tau;  // transmittance before step kk's emission
+                T col[3], alpha;
+                if (slab_g<T, T>(yp[0], yp[1], yp[2], yc[0], yc[1], yc[2], yc[5], L, a, r_in, p.t_scale, k, col,
+                                 alpha))
+                    tau = tau * (T(1) - alpha);
+            }
+        }
         for (std::uint32_t kk = kend; kk > kbeg; --kk) {
             const T* yp = Y[kk - 1 - kbeg];
             const T* yc = Y[kk - kbeg];
             T pend[NS] = {T(0), T(0), T(0), T(0), T(0), T(0)};
-            for (std::uint32_t j = 0; j < nc; ++j) {
-                if (xk[j] != kk) continue;
-                // d(colour, weight)/d(r0, th0, psi0, r1, th1, ph1, psi1, L, a, r_in, t_scale)
-                using D = Dual<T, 11>;
-                D col[3], wd;
-                crossing_g<D, T>(D::var(yp[0], 0), D::var(yp[1], 1), D::var(yp[5], 2), D::var(yc[0], 3),
+            using D = Dual<T, 11>;
+            if constexpr (SLAB) {
+                T colv[3], alv;
+                if ((k.flags & SGX_FLAG_DISC_ON) &&
+                    slab_g<T, T>(yp[0], yp[1], yp[2], yc[0], yc[1], yc[2], yc[5], L, a, r_in, p.t_scale, k, colv,
+                                 alv)) {
+                    // d(colour, alpha)/d(r0, th0, ph0, r1, th1, ph1, psi1, L, a, r_in, t_scale)
+                    D col[3], ald;
+                    slab_g<D, T>(D::var(yp[0], 0), D::var(yp[1], 1), D::var(yp[2], 2), D::var(yc[0], 3),
                                  D::var(yc[1], 4), D::var(yc[2], 5), D::var(yc[5], 6), D::var(L, 7), D::var(a, 8),
-                                 D::var(r_in, 9), D::var(p.t_scale, 10), k, col, wd);
-                T qv[11];
+                                 D::var(r_in, 9), D::var(p.t_scale, 10), k, col, ald);
+                    const T tj = tb[kk - kbeg];
+                    const T gcs = tj * alv;
+                    const T gal = tj * (g[0] * (colv[0] - R[0]) + g[1] * (colv[1] - R[1]) + g[2] * (colv[2] - R[2]));
 #pragma unroll
-                for (int x = 0; x < 11; ++x)
-                    qv[x] = gcs[j] * (g[0] * col[0].d[x] + g[1] * col[1].d[x] + g[2] * col[2].d[x]) + gw[j] * wd.d[x];
-                pend[0] += qv[0];
-                pend[1] += qv[1];
-                pend[5] += qv[2];
-                lam[0] += qv[3];
-                lam[1] += qv[4];
-                lam[2] += qv[5];
-                lam[5] += qv[6];
-                muL += qv[7];
-                g_a += qv[8] * k.M;
-                g_rin += qv[9] * k.M;
-                g_ts += qv[10];
+                    for (int c = 0; c < 3; ++c) R[c] = alv * colv[c] + (T(1) - alv) * R[c];
+                    T qv[11];
+#pragma unroll
+                    for (int x = 0; x < 11; ++x)
+                        qv[x] = gcs * (g[0] * col[0].d[x] + g[1] * col[1].d[x] + g[2] * col[2].d[x]) + gal * ald.d[x];
+                    pend[0] += qv[0];
+                    pend[1] += qv[1];
+                    pend[2] += qv[2];
+                    lam[0] += qv[3];
+                    lam[1] += qv[4];
+                    lam[2] += qv[5];
+                    lam[5] += qv[6];
+                    muL += qv[7];
+                    g_a += qv[8] * k.M;
+                    g_rin += qv[9] * k.M;
+                    g_ts += qv[10];
+                }
+            } else {
+                for (std::uint32_t j = 0; j < nc; ++j) {
+                    if (xkk[j] != kk) continue;
+                    // d(colour, weight)/d(r0, th0, psi0, r1, th1, ph1, psi1, L, a, r_in, t_scale)
+                    D col[3], wd;
+                    crossing_g<D, T>(D::var(yp[0], 0), D::var(yp[1], 1), D::var(yp[5], 2), D::var(yc[0], 3),
+                                     D::var(yc[1], 4), D::var(yc[2], 5), D::var(yc[5], 6), D::var(L, 7),
+                                     D::var(a, 8), D::var(r_in, 9), D::var(p.t_scale, 10), k, col, wd);
+                    T qv[11];
+#pragma unroll
+                    for (int x = 0; x < 11; ++x)
+                        qv[x] = xcs[j] * (g[0] * col[0].d[x] + g[1] * col[1].d[x] + g[2] * col[2].d[x]) +
+                                xgw[j] * wd.d[x];
+                    pend[0] += qv[0];
+                    pend[1] += qv[1];
+                    pend[5] += qv[2];
+                    lam[0] += qv[3];
+                    lam[1] += qv[4];
+                    lam[2] += qv[5];
+                    lam[5] += qv[6];
+                    muL += qv[7];
+                    g_a += qv[8] * k.M;
+                    g_rin += qv[9] * k.M;
+                    g_ts += qv[10];
+                }
             }
-            // Jacobian of y_k = step(y_{k-1}; E, L, a): directions 0..5 state, 6 E, 7 L, 8 a.
-            using D9 = Dual<T, 9>;
-            D9 yd[NS], od[NS];
-#pragma unroll
-            for (int i = 0; i < NS; ++i) yd[i] = D9::var(yp[i], i);
-            step_g<D9, T>(yd, D9::var(E, 6), D9::var(L, 7), D9::var(a, 8), k.M, k.h, fade, od);
-            T nl[NS];
-#pragma unroll
-            for (int i = 0; i < NS; ++i) {
-                T acc = T(0);
-#pragma unroll
-                for (int j2 = 0; j2 < NS; ++j2) acc += lam[j2] * od[j2].d[i];
-                nl[i] = acc;
-            }
-#pragma unroll
-            for (int j2 = 0; j2 < NS; ++j2) {
-                muE += lam[j2] * od[j2].d[6];
-                muL += lam[j2] * od[j2].d[7];
-                mua += lam[j2] * od[j2].d[8];
-            }
-#pragma unroll
-            for (int i = 0; i < NS; ++i) lam[i] = nl[i] + pend[i];
+            step_adjoint(yp, E, L, a, k, fade, lam, pend, muE, muL, mua);
         }
     }
     // Chain through the camera set-up: y0, E, L as functions of (a, incl).
@@ -505,6 +638,7 @@ __global__ void __launch_bounds__(128) diff_backward_kernel(DiffConst<T> k, Diff
     D2 yd0[NS], Ed, Ld;
     init_g<D2, T>(D2::var(a, 0), D2::var(p.incl, 1), k, gx, gy, b.ox[s], b.oy[s], yd0, Ed, Ld);
     T grad_a = g_a + mua * k.M, grad_i = T(0);
+#pragma unroll
     for (int i = 0; i < NS; ++i) {
         grad_a += lam[i] * yd0[i].d[0] * k.M;
         grad_i += lam[i] * yd0[i].d[1];
@@ -580,6 +714,8 @@ DiffConst<T> make_const(const sgx_uniforms& u, const sgx_diff_opts& o) {
     k.fade_start = T(o.fade_start);
     k.fade_width = T(o.fade_width);
     k.fade = o.fade_start > 0.0f ? 1u : 0u;
+    k.H = T(o.half_thickness) * T(u.mass_M);
+    k.kappa = T(o.tau_perp) / (T(16) / T(15) * k.H);
     k.width = u.width;
     k.height = u.height;
     k.spp = u.supersample < 1u ? 1u : (u.supersample > 1024u ? 1024u : u.supersample);
@@ -597,6 +733,7 @@ struct sgx_diff_state {
     std::uint64_t n = 0;
     std::uint32_t slots = 0;
     std::uint32_t precision = SGX_PRECISION_FP32;
+    std::uint32_t nx = kMaxCross;  // crossing records per ray (1 for the slab model)
     sgx_uniforms u{};
     sgx_diff_params p{};
     sgx_diff_opts o{};
@@ -619,13 +756,14 @@ DiffBufs<T> carve_bufs(sgx_diff_state& st, std::uint32_t spp) {
     };
     b.n = n;
     b.slots = st.slots;
-    b.ckpt = reinterpret_cast<T*>(take(std::size_t(st.slots) * NS * n * sizeof(T)));
+    const std::size_t nx = st.nx;
+    b.ckpt = reinterpret_cast<T*>(take(std::size_t(st.slots) * NC * n * sizeof(T)));
     b.hdr = reinterpret_cast<T*>(take(3 * n * sizeof(T)));
     b.nsteps = reinterpret_cast<std::uint32_t*>(take(n * 4));
     b.ncross = reinterpret_cast<std::uint32_t*>(take(n * 4));
-    b.xk = reinterpret_cast<std::uint32_t*>(take(std::size_t(kMaxCross) * n * 4));
-    b.xw = reinterpret_cast<T*>(take(std::size_t(kMaxCross) * n * sizeof(T)));
-    b.xc = reinterpret_cast<T*>(take(std::size_t(kMaxCross) * 3 * n * sizeof(T)));
+    b.xk = reinterpret_cast<std::uint32_t*>(take(nx * n * 4));
+    b.xw = nx > 1 ? reinterpret_cast<T*>(take(nx * n * sizeof(T))) : nullptr;
+    b.xc = nx > 1 ? reinterpret_cast<T*>(take(nx * 3 * n * sizeof(T))) : nullptr;
     b.grads = reinterpret_cast<double*>(take(4 * n * 8));
     T* off = reinterpret_cast<T*>(take(2 * std::size_t(spp) * sizeof(T)));
     b.ox = off;
@@ -634,11 +772,12 @@ DiffBufs<T> carve_bufs(sgx_diff_state& st, std::uint32_t spp) {
     return b;
 }
 
-template <class T> std::size_t state_bytes(std::uint64_t n, std::uint32_t slots, std::uint32_t spp) {
+template <class T>
+std::size_t state_bytes(std::uint64_t n, std::uint32_t slots, std::uint32_t spp, std::size_t nx) {
     auto r = [](std::size_t x) { return (x + 255) / 256 * 256; };
-    return r(std::size_t(slots) * NS * n * sizeof(T)) + r(3 * n * sizeof(T)) + 2 * r(n * 4) +
-           r(std::size_t(kMaxCross) * n * 4) + r(std::size_t(kMaxCross) * n * sizeof(T)) +
-           r(std::size_t(kMaxCross) * 3 * n * sizeof(T)) + r(4 * n * 8) + r(2 * std::size_t(spp) * sizeof(T)) + 256 +
+    return r(std::size_t(slots) * NC * n * sizeof(T)) + r(3 * n * sizeof(T)) + 2 * r(n * 4) + r(nx * n * 4) +
+           (nx > 1 ? r(nx * n * sizeof(T)) + r(nx * 3 * n * sizeof(T)) : 0) + r(4 * n * 8) +
+           r(2 * std::size_t(spp) * sizeof(T)) + 256 +
            // reduction scratch: 4 x chunk sums + 4 results
            r(4 * ((n + 1023) / 1024) * 8) + 256;
 }
@@ -648,10 +787,13 @@ cudaError_t run_forward(sgx_diff_state& st, float* img, cudaStream_t s) {
     const DiffConst<T> k = make_const<T>(st.u, st.o);
     const DiffParamsT<T> p{T(st.p.spin), T(st.p.incl), T(st.p.r_in), T(st.p.t_scale)};
     DiffBufs<T> b = carve_bufs<T>(st, k.spp);
-    cudaError_t e = cudaMemsetAsync(b.overflow, 0, 8, s);
+    cudaError_t e = cudaMemsetAsync(b.overflow, 0, 16, s);
     if (e != cudaSuccess) return e;
     offsets_kernel<T><<<(k.spp + 127) / 128, 128, 0, s>>>(k.spp, const_cast<T*>(b.ox), const_cast<T*>(b.oy));
-    diff_forward_kernel<T><<<unsigned((st.n + 127) / 128), 128, 0, s>>>(k, p, b);
+    if (st.o.model == SGX_DIFF_MODEL_SLAB)
+        diff_forward_kernel<T, true><<<unsigned((st.n + 127) / 128), 128, 0, s>>>(k, p, b);
+    else
+        diff_forward_kernel<T, false><<<unsigned((st.n + 127) / 128), 128, 0, s>>>(k, p, b);
     const std::uint64_t npix = std::uint64_t(k.width) * k.height;
     diff_image_kernel<T><<<unsigned((npix + 255) / 256), 256, 0, s>>>(k, b, img);
     return cudaGetLastError();
@@ -662,7 +804,10 @@ cudaError_t run_backward(sgx_diff_state& st, const float* gimg, double* d_out4, 
     const DiffConst<T> k = make_const<T>(st.u, st.o);
     const DiffParamsT<T> p{T(st.p.spin), T(st.p.incl), T(st.p.r_in), T(st.p.t_scale)};
     DiffBufs<T> b = carve_bufs<T>(st, k.spp);
-    diff_backward_kernel<T><<<unsigned((st.n + 127) / 128), 128, 0, s>>>(k, p, b, gimg);
+    if (st.o.model == SGX_DIFF_MODEL_SLAB)
+        diff_backward_kernel<T, true><<<unsigned((st.n + 127) / 128), 128, 0, s>>>(k, p, b, gimg);
+    else
+        diff_backward_kernel<T, false><<<unsigned((st.n + 127) / 128), 128, 0, s>>>(k, p, b, gimg);
     const std::uint32_t nchunks = std::uint32_t((st.n + 1023) / 1024);
     double* part = reinterpret_cast<double*>(reinterpret_cast<unsigned char*>(b.overflow) + 256);
     reduce_chunks<<<dim3(nchunks, 4), 256, 0, s>>>(b.grads, st.n, part, nchunks);
@@ -680,8 +825,11 @@ void sgx_diff_opts_default(sgx_diff_opts* o) {
     o->struct_size = sizeof(*o);
     o->precision = SGX_PRECISION_FP32;
     o->edge_width = 0.1f;
-    o->fade_start = 3.14159265358979f;
-    o->fade_width = 1.57079632679490f;
+    o->fade_start = 2.35619449019234f;  // 3 pi / 4
+    o->fade_width = 1.57079632679490f;  // pi / 2
+    o->model = SGX_DIFF_MODEL_SLAB;
+    o->half_thickness = 0.3f;
+    o->tau_perp = 4.0f;
 }
 
 sgx_status sgx_diff_forward(sgx_context* c, const sgx_uniforms* base, const sgx_diff_params* params,
@@ -694,23 +842,37 @@ sgx_status sgx_diff_forward(sgx_context* c, const sgx_uniforms* base, const sgx_
         return fail(c, SGX_ERR_INVALID_ARGUMENT, "max_steps must be in [1, 200000]");
     sgx_diff_opts o;
     sgx_diff_opts_default(&o);
-    if (opts != nullptr) o = *opts;
+    if (opts != nullptr) {
+        if (opts->struct_size != sizeof(sgx_diff_opts))
+            return fail(c, SGX_ERR_INVALID_ARGUMENT, "sgx_diff_opts.struct_size mismatch");
+        o = *opts;
+    }
     if (o.precision != SGX_PRECISION_FP32 && o.precision != SGX_PRECISION_FP64)
         return fail(c, SGX_ERR_INVALID_ARGUMENT, "the differentiable form runs in FP32 or FP64");
+    if (o.model != SGX_DIFF_MODEL_SLAB && o.model != SGX_DIFF_MODEL_CROSSING)
+        return fail(c, SGX_ERR_INVALID_ARGUMENT, "unknown disc model");
     if (!(o.edge_width > 0.0f) || (o.fade_start > 0.0f && !(o.fade_width > 0.0f)))
         return fail(c, SGX_ERR_INVALID_ARGUMENT, "edge_width and fade_width must be positive");
+    if (o.model == SGX_DIFF_MODEL_SLAB && !(o.half_thickness > 0.0f && o.tau_perp > 0.0f))
+        return fail(c, SGX_ERR_INVALID_ARGUMENT, "half_thickness and tau_perp must be positive");
     if (!(params->spin >= 0.0 && params->spin < 1.0) || !(params->incl > 0.0 && params->incl < 3.14159265) ||
         !(params->r_in > 0.0) || !(params->t_scale > 0.0))
-        return fail(c, SGX_ERR_INVALID_ARGUMENT, "parameters out of range (0 <= spin < 1, 0 < incl < pi, r_in, t_scale > 0)");
+        return fail(c, SGX_ERR_INVALID_ARGUMENT,
+                    "parameters out of range (0 <= spin < 1, 0 < incl < pi, r_in > 0, t_scale > 0)");
     cudaSetDevice(c->device);
     if (c->diff == nullptr) c->diff = new sgx_diff_state();
     sgx_diff_state& st = *c->diff;
+    st.valid = false;
     const std::uint32_t spp = base->supersample < 1u ? 1u : (base->supersample > 1024u ? 1024u : base->supersample);
     st.n = std::uint64_t(base->width) * base->height * spp;
     st.slots = base->max_steps / kCk + 1;
     st.precision = o.precision;
-    const std::size_t need = o.precision == SGX_PRECISION_FP64 ? state_bytes<double>(st.n, st.slots, spp)
-                                                               : state_bytes<float>(st.n, st.slots, spp);
+    st.nx = o.model == SGX_DIFF_MODEL_SLAB ? 1u : std::uint32_t(kMaxCross);
+    const std::size_t need = o.precision == SGX_PRECISION_FP64 ? state_bytes<double>(st.n, st.slots, spp, st.nx)
+                                                               : state_bytes<float>(st.n, st.slots, spp, st.nx);
+    if (need > c->workspace_budget * 4)
+        return fail(c, SGX_ERR_INVALID_ARGUMENT, "differentiable render needs " + std::to_string(need >> 20) +
+                                                     " MiB of records: fewer rays or max_steps");
     if (st.cap < need) {
         if (st.mem) cudaFree(st.mem);
         st.mem = nullptr;
@@ -738,10 +900,7 @@ sgx_status sgx_diff_forward(sgx_context* c, const sgx_uniforms* base, const sgx_
     cudaError_t e = o.precision == SGX_PRECISION_FP64 ? run_forward<double>(st, d_image, s)
                                                       : run_forward<float>(st, d_image, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) {
-        st.valid = false;
-        return cuda_fail(c, e, "sgx_diff_forward");
-    }
+    if (e != cudaSuccess) return cuda_fail(c, e, "sgx_diff_forward");
     st.valid = true;
     return SGX_OK;
 }
@@ -756,8 +915,8 @@ sgx_status sgx_diff_backward(sgx_context* c, const float* d_grad_image, double* 
     cudaStream_t s = stream != nullptr ? static_cast<cudaStream_t>(stream) : c->stream;
     // results land after the reduction scratch
     const std::uint32_t spp = st.u.supersample < 1u ? 1u : (st.u.supersample > 1024u ? 1024u : st.u.supersample);
-    const std::size_t used = st.precision == SGX_PRECISION_FP64 ? state_bytes<double>(st.n, st.slots, spp)
-                                                                : state_bytes<float>(st.n, st.slots, spp);
+    const std::size_t used = st.precision == SGX_PRECISION_FP64 ? state_bytes<double>(st.n, st.slots, spp, st.nx)
+                                                                : state_bytes<float>(st.n, st.slots, spp, st.nx);
     double* d_out4 = reinterpret_cast<double*>(static_cast<unsigned char*>(st.mem) + used - 256);
     cudaError_t e = st.precision == SGX_PRECISION_FP64 ? run_backward<double>(st, d_grad_image, d_out4, s)
                                                        : run_backward<float>(st, d_grad_image, d_out4, s);
@@ -767,20 +926,19 @@ sgx_status sgx_diff_backward(sgx_context* c, const float* d_grad_image, double* 
     return SGX_OK;
 }
 
-sgx_status sgx_diff_stats(sgx_context* c, uint64_t* rays, uint64_t* crossing_overflow) {
+sgx_status sgx_diff_stats(sgx_context* c, uint64_t* rays, uint64_t* steps, uint64_t* crossing_overflow) {
     if (c == nullptr) return SGX_ERR_INVALID_ARGUMENT;
     if (c->diff == nullptr || !c->diff->valid) return fail(c, SGX_ERR_NOT_RENDERED, "no differentiable render");
     sgx_diff_state& st = *c->diff;
     if (rays != nullptr) *rays = st.n;
-    if (crossing_overflow != nullptr) {
-        const std::uint32_t spp = st.u.supersample < 1u ? 1u : (st.u.supersample > 1024u ? 1024u : st.u.supersample);
-        unsigned long long h = 0;
-        void* ov = nullptr;
-        if (st.precision == SGX_PRECISION_FP64) ov = carve_bufs<double>(st, spp).overflow;
-        else ov = carve_bufs<float>(st, spp).overflow;
-        if (cudaMemcpy(&h, ov, 8, cudaMemcpyDeviceToHost) != cudaSuccess) return SGX_ERR_CUDA;
-        *crossing_overflow = h;
-    }
+    const std::uint32_t spp = st.u.supersample < 1u ? 1u : (st.u.supersample > 1024u ? 1024u : st.u.supersample);
+    unsigned long long h[2] = {0, 0};
+    void* ov = st.precision == SGX_PRECISION_FP64 ? static_cast<void*>(carve_bufs<double>(st, spp).overflow)
+                                                  : static_cast<void*>(carve_bufs<float>(st, spp).overflow);
+    cudaError_t e = cudaMemcpy(h, ov, sizeof(h), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(c, e, "sgx_diff_stats");
+    if (steps != nullptr) *steps = h[1];
+    if (crossing_overflow != nullptr) *crossing_overflow = h[0];
     return SGX_OK;
 }
 

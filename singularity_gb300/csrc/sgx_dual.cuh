@@ -108,6 +108,10 @@ template <class T, int N> struct DM<Dual<T, N>> {
         return chain(x, p, x.v != T(0) ? y.v * p / x.v : T(0));
     }
     static __device__ __forceinline__ D log_(const D& x) { return chain(x, DM<T>::log_(x.v), T(1) / x.v); }
+    static __device__ __forceinline__ D exp_(const D& x) {
+        const T e = DM<T>::exp_(x.v);
+        return chain(x, e, e);
+    }
     static __device__ __forceinline__ D fmin_(const D& a, const D& b) { return (b.v < a.v) ? b : a; }
     static __device__ __forceinline__ D fmax_(const D& a, const D& b) { return (b.v > a.v) ? b : a; }
     static __device__ __forceinline__ D rcp_(const D& x) { return D(T(1)) / x; }

@@ -162,6 +162,10 @@ sgx_uniforms pack_uniforms(const Scene& scene, const CameraState& cam, std::uint
     if (scene.disc_texture_on) flags |= SGX_FLAG_DISC_ON;
     if (scene.disc_doppler_on) flags |= SGX_FLAG_DOPPLER_ON;
     if (scene.disc_redshift_on) flags |= SGX_FLAG_REDSHIFT_ON;
+    // adaptive_step_on (render_backend.hpp:78-81) is honoured as the WebGPU
+    // backend does (webgpu_backend.cpp:159-160); the reference CUDA backend
+    // drops it.  Off by default, so default scenes pack identically.
+    if (scene.adaptive_step_on) flags |= SGX_FLAG_ADAPTIVE_STEP;
     u.flags = flags;
     u.max_steps = scene.max_steps != 0 ? scene.max_steps : kMaxSteps;
     u.frame_index = 0;

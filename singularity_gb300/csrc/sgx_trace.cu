@@ -114,7 +114,7 @@ template <class T, int FL> struct KerrFixed {
         }
         prev_th = y.th;
         prev_r = y.r;
-        y = kerr_rk4<T, FAST>(y, v.h, v, c);
+        y = kerr_rk4<T, FAST>(y, fixed_step_h(v, y.r), v, c);
         if (++steps >= v.max_steps) {
             term = TERM_BUDGET;
             return true;
@@ -174,7 +174,7 @@ template <class T, int FL> struct SchwFixed {
         prev_th = y.th;
         prev_r = y.r;
         prev_uph = y.uph;
-        y = schw_rk4(y, v.h, v.rs);
+        y = schw_rk4(y, fixed_step_h(v, y.r), v.rs);
         if (++steps >= v.max_steps) {
             term = TERM_BUDGET;
             return true;

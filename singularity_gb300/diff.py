@@ -30,11 +30,16 @@ PARAM_NAMES = ("spin", "incl", "r_in", "t_scale")
 
 @dataclass
 class DiffOptions:
-    """Options of the form: FP32 or FP64, soft edge width (M), winding fade."""
+    """Options of the form (sgx_diff_opts): FP32 or FP64, disc model (emitting
+    slab or equatorial crossings), soft edge width (M), winding fade (rad),
+    slab half-thickness (M) and optical depth across."""
     precision: int = N.PRECISION_FP32
     edge_width: float = 0.1
-    fade_start: float = math.pi
-    fade_width: float = math.pi / 2
+    fade_start: float = 0.75 * math.pi
+    fade_width: float = 0.5 * math.pi
+    model: int = N.DIFF_MODEL_SLAB
+    half_thickness: float = 0.3
+    tau_perp: float = 4.0
 
     def to_c(self) -> N.DiffOpts:
         o = N.DiffOpts()
@@ -43,7 +48,15 @@ class DiffOptions:
         o.edge_width = self.edge_width
         o.fade_start = self.fade_start
         o.fade_width = self.fade_width
+        o.model = self.model
+        o.half_thickness = self.half_thickness
+        o.tau_perp = self.tau_perp
         return o
+
+    def oracle_form(self) -> dict:
+        """The same form as keyword arguments of the oracle's diff_render."""
+        return dict(eps=self.edge_width, fade=(self.fade_start, self.fade_width), model=self.model,
+                    half_thickness=self.half_thickness, tau_perp=self.tau_perp)
 
 
 def _params_c(p: Sequence[float]) -> N.DiffParams:
@@ -93,9 +106,9 @@ class DiffRenderer:
         return np.array(out[:], dtype=np.float64)
 
     def stats(self):
-        rays, over = C.c_uint64(), C.c_uint64()
-        self._r._check(self._lib.sgx_diff_stats(self._r.handle, C.byref(rays), C.byref(over)))
-        return {"rays": rays.value, "crossing_overflow": over.value}
+        rays, steps, over = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        self._r._check(self._lib.sgx_diff_stats(self._r.handle, C.byref(rays), C.byref(steps), C.byref(over)))
+        return {"rays": rays.value, "steps": steps.value, "crossing_overflow": over.value}
 
 
 def _autograd_fn():
@@ -144,7 +157,7 @@ class FitResult:
 
 def fit(dr: DiffRenderer, u: N.Uniforms, target, init: Sequence[float], steps: int = 200,
         lr: Sequence[float] = (0.01, 0.01, 0.05, 0.01), opts: Optional[DiffOptions] = None,
-        bounds: Sequence[tuple] = ((0.0, 0.998), (0.05, math.pi - 0.05), (1.0, 20.0), (0.2, 5.0))) -> FitResult:
+        bounds: Sequence[tuple] = ((0.0, 0.998), (0.05, math.pi - 0.05), (2.0, 20.0), (0.2, 5.0))) -> FitResult:
     """Adam on the mean-squared image error to `target` (a CUDA tensor of the
     form's image), one learning rate per parameter; parameters are clamped to
     `bounds` after every step."""

@@ -17,9 +17,10 @@ def _scene(S, w, h, spp):
 
 
 def test_form_reduces_to_reference_render(oracle):
-    """Soft edge -> 0, no fade: the reference's first-hit render with the
-    starfield off (orbital camera at elevation pi/2 - i, azimuth 0).  Pixels
-    may differ only where the blackbody blend band (6500-6700 K) is hit."""
+    """Crossing model, soft edge -> 0, no fade: the reference's first-hit
+    render with the starfield off (orbital camera at elevation pi/2 - i,
+    azimuth 0).  Pixels may differ only where the blackbody blend band
+    (6500-6700 K) is hit or a ray ends inside the photon orbit."""
     import singularity_gb300 as S
     a, i, rin, ts = 0.7, math.radians(60.0), S.kerr_isco_prograde(1.0, 0.7), 1.0
     w, h = 64, 40
@@ -29,7 +30,8 @@ def test_form_reduces_to_reference_render(oracle):
     u = S.pack_uniforms(sc, cam, w, h)
     u.flags &= ~N.SGX_FLAG_STARFIELD_ON
     _, ref = oracle.render(u, precision="f64")
-    form = oracle.diff_render(_scene(S, w, h, 2), (a, i, rin, ts), eps=1e-5, fade=(0.0, 1.0))
+    form = oracle.diff_render(_scene(S, w, h, 2), (a, i, rin, ts), eps=1e-5, fade=(0.0, 1.0),
+                              model=oracle.DIFF_MODEL_CROSSING)
     e = np.abs(form - ref.reshape(h, w, 3))
     assert e.mean() <= 1e-5
     assert (e.max(axis=-1) <= 1e-6).mean() >= 0.95
@@ -44,15 +46,30 @@ def test_fp32_form_tracks_fp64(oracle):
 
 
 def test_central_differences_settle(oracle):
-    """FD of the image loss at steps 1e-3 and 3e-4 agree in inner radius and
-    temperature scale: the soft edges and the continuous blackbody leave no
-    jumps in them."""
+    """Slab model (the default): FD of the image loss at steps 1e-3 and 3e-4
+    agree to 2e-3 in all four parameters; the form has no jumps.  (The
+    remaining difference is the O(step) bias of the clamps' kinks.)"""
     import singularity_gb300 as S
     W = S.workloads
-    base = _scene(S, 48, 32, 2)
+    base = _scene(S, 64, 48, 2)
     target = oracle.diff_render(base, W.differentiation_params(W.differentiation_target()))
     guess = W.differentiation_params(W.differentiation_guess())
     g1 = oracle.diff_fd_gradient(base, guess, target, step=1e-3)
     g2 = oracle.diff_fd_gradient(base, guess, target, step=3e-4)
+    assert np.all(np.abs(g1 - g2) <= 2e-3 * np.abs(g2)), (g1, g2)
+
+
+def test_crossing_model_smooth_in_radius_and_temperature(oracle):
+    """The crossing model is smooth in r_in and t_scale only: rays grazing the
+    plane make its image jump in spin and inclination, which is why the slab
+    is the default.  Pinned so a change of either model shows up here."""
+    import singularity_gb300 as S
+    W = S.workloads
+    base = _scene(S, 48, 32, 2)
+    form = dict(model=oracle.DIFF_MODEL_CROSSING)
+    target = oracle.diff_render(base, W.differentiation_params(W.differentiation_target()), **form)
+    guess = W.differentiation_params(W.differentiation_guess())
+    g1 = oracle.diff_fd_gradient(base, guess, target, step=1e-3, **form)
+    g2 = oracle.diff_fd_gradient(base, guess, target, step=3e-4, **form)
     for k in (2, 3):
-        assert abs(g1[k] - g2[k]) <= 0.02 * abs(g1[k]) + 1e-7, (k, g1, g2)
+        assert abs(g1[k] - g2[k]) <= 0.02 * abs(g1[k]), (k, g1, g2)

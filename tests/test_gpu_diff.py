@@ -2,9 +2,9 @@
 
 Forward: the GPU image against the oracle's image of the same form
 (oracle/diff_oracle.hpp) in the same precision.  Adjoint: the GPU's gradient
-of an image loss against central differences (step 1e-3, the oracle's FP64
-image) and the FP32 adjoint against the FP64 adjoint.  Tolerances are stated
-per test."""
+of an image loss against central differences of the oracle's FP64 image
+(steps 1e-3 and 3e-4) and the FP32 adjoint against the FP64 adjoint.
+Tolerances are stated per test."""
 
 from __future__ import annotations
 
@@ -37,46 +37,65 @@ def _loss_grad_image(img, target):
     return 2.0 * (img - target) / img.numel()
 
 
+@pytest.mark.parametrize("model", [1, 0])
 @pytest.mark.parametrize("prec", ["f32", "f64"])
-def test_forward_matches_oracle(diff, sgx, oracle, prec):
+def test_forward_matches_oracle(diff, sgx, oracle, prec, model):
     from singularity_gb300 import diff as D
     N = sgx._native
     base, tgt, guess = _setup(sgx)
-    opts = D.DiffOptions(precision=N.PRECISION_FP32 if prec == "f32" else N.PRECISION_FP64)
+    opts = D.DiffOptions(precision=N.PRECISION_FP32 if prec == "f32" else N.PRECISION_FP64, model=model)
     for p in (tgt, guess):
         img = diff.forward(base, p, opts).cpu().numpy()
-        ref = oracle.diff_render(base, p, precision=prec).astype(np.float32)
+        ref = oracle.diff_render(base, p, precision=prec, **opts.oracle_form()).astype(np.float32)
         e = np.abs(img - ref)
-        print(f"{prec} {p}: mean {e.mean():.2e} max {e.max():.2e}")
+        print(f"model {model} {prec} {p}: mean {e.mean():.2e} max {e.max():.2e}")
         if prec == "f64":
             assert e.mean() <= 1e-6 and e.max() <= 1e-4
         else:
             assert e.mean() <= 2e-5 and (e <= 1e-3).mean() >= 0.999
 
 
-def test_adjoint_matches_central_differences(diff, sgx, oracle):
+def _adjoint_and_fd(diff, sgx, oracle, model, steps=(FD_STEP,)):
     import torch
     from singularity_gb300 import diff as D
     N = sgx._native
     base, tgt, guess = _setup(sgx)
-    target = oracle.diff_render(base, tgt)
-    fd = oracle.diff_fd_gradient(base, guess, target, step=FD_STEP)
+    form = D.DiffOptions(model=model).oracle_form()
+    target = oracle.diff_render(base, tgt, **form)
+    fds = [oracle.diff_fd_gradient(base, guess, target, step=st, **form) for st in steps]
     t_dev = torch.as_tensor(target.astype(np.float32), device="cuda")
     out = {}
     for prec in (N.PRECISION_FP64, N.PRECISION_FP32):
-        img = diff.forward(base, guess, D.DiffOptions(precision=prec))
+        img = diff.forward(base, guess, D.DiffOptions(precision=prec, model=model))
         out[prec] = diff.backward(_loss_grad_image(img, t_dev))
-    g64, g32 = out[N.PRECISION_FP64], out[N.PRECISION_FP32]
-    rel64 = np.abs(g64 - fd) / np.abs(fd)
+    return fds, out[N.PRECISION_FP64], out[N.PRECISION_FP32]
+
+
+def test_adjoint_matches_central_differences(diff, sgx, oracle):
+    """Slab model: the FP64 adjoint against central differences of the FP64
+    oracle (steps 1e-3 and 3e-4), all four parameters; the FP32 adjoint
+    against the FP64 adjoint."""
+    (fd3, fd4), g64, g32 = _adjoint_and_fd(diff, sgx, oracle, 1, steps=(1e-3, 3e-4))
+    rel3 = np.abs(g64 - fd3) / np.abs(fd3)
+    rel4 = np.abs(g64 - fd4) / np.abs(fd4)
     rel32 = np.abs(g32 - g64) / np.abs(g64)
-    print("fd  ", fd)
-    print("fp64", g64, "rel vs fd", rel64)
-    print("fp32", g32, "rel vs fp64", rel32)
-    # the target image is rendered in FP32 on the device from the FP64 oracle:
-    # its rounding (1e-7) perturbs the loss gradient far below these bars
-    assert np.all(np.sign(g64) == np.sign(fd))
-    assert rel64[2] <= 1e-2 and rel64[3] <= 1e-2, rel64
-    assert np.all(rel32 <= 2e-2), rel32
+    print("fd 1e-3", fd3)
+    print("fd 3e-4", fd4)
+    print("fp64   ", g64, "rel vs fd 1e-3", rel3, "vs 3e-4", rel4)
+    print("fp32   ", g32, "rel vs fp64", rel32)
+    # FD at 1e-3 carries O(step^2) truncation and O(step) kink bias of a few
+    # 1e-4; the better of the two steps must agree to 1e-3
+    assert np.all(np.minimum(rel3, rel4) <= 1e-3), (rel3, rel4)
+    assert np.all(rel32 <= 1e-3), rel32
+
+
+def test_crossing_adjoint_smooth_parameters(diff, sgx, oracle):
+    """Crossing model: r_in and t_scale (the parameters it is smooth in)."""
+    (fd,), g64, g32 = _adjoint_and_fd(diff, sgx, oracle, 0)
+    rel = np.abs(g64 - fd) / np.abs(fd)
+    print("fd", fd, "fp64", g64, "rel", rel, "fp32", g32)
+    assert rel[2] <= 1e-3 and rel[3] <= 1e-3, rel
+    assert np.all(np.abs(g32[2:] - g64[2:]) <= 1e-3 * np.abs(g64[2:]))
 
 
 def test_backward_is_deterministic(diff, sgx):
