@@ -301,8 +301,12 @@ sgx_status sgx_render_noalloc(const sgx_uniforms* u, const sgx_render_opts* opts
  *   - w = S((r - r_in)/e) S((r_out - r)/e) softens the annulus edges (S the
  *     cubic smoothstep, e = edge_width * M); with fade_start > 0, w is also
  *     multiplied by 1 - S((psi - fade_start)/fade_width), psi the angle the ray
- *     has swept around the hole, which removes the rays near the critical
- *     curve whose images appear and vanish as parameters move;
+ *     has swept around the hole.  Rays that pass close to the photon orbit
+ *     before reaching the disc move on parameter scales below 1e-3 (their
+ *     bending grows like -log(b - b_c)), which no finite difference and no
+ *     FP32 trace resolves; they all sweep more than ~3 pi / 4, so the default
+ *     fade (5 pi / 8, pi / 8) keeps the direct image of the disc out to that
+ *     angle and drops them;
  *   - the blackbody fit is blended across its 6600 K branch switch;
  *   - rays are captured inside the prograde photon orbit radius less 0.05 M
  *     (the reference's 1.02 r_+ lets the fixed-step RK4 blow up first).
@@ -320,8 +324,8 @@ typedef struct sgx_diff_opts {
     uint32_t struct_size;
     uint32_t precision;    /* SGX_PRECISION_FP32 or SGX_PRECISION_FP64 */
     float edge_width;      /* soft annulus edge, units of M (0.1) */
-    float fade_start;      /* swept angle where images fade, rad (3 pi / 4); <= 0: no fade */
-    float fade_width;      /* fade length, rad (pi / 2) */
+    float fade_start;      /* swept angle where images fade, rad (5 pi / 8); <= 0: no fade */
+    float fade_width;      /* fade length, rad (pi / 8) */
     uint32_t model;        /* SGX_DIFF_MODEL_SLAB (default) or SGX_DIFF_MODEL_CROSSING */
     float half_thickness;  /* slab half-thickness, units of M (0.3) */
     float tau_perp;        /* slab optical depth across (4) */

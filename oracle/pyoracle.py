@@ -54,7 +54,7 @@ class DiffOpts(C.Structure):
 DIFF_MODEL_CROSSING, DIFF_MODEL_SLAB = 0, 1
 
 
-DIFF_FADE = (0.75 * math.pi, 0.5 * math.pi)  # the library's default winding fade (start, width), rad
+DIFF_FADE = (0.625 * math.pi, 0.125 * math.pi)  # the library's default winding fade (start, width), rad
 
 
 def diff_render(u, params, eps: float = 0.1, precision: str = "f64", threads: int | None = None,

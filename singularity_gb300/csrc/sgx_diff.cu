@@ -825,8 +825,8 @@ void sgx_diff_opts_default(sgx_diff_opts* o) {
     o->struct_size = sizeof(*o);
     o->precision = SGX_PRECISION_FP32;
     o->edge_width = 0.1f;
-    o->fade_start = 2.35619449019234f;  // 3 pi / 4
-    o->fade_width = 1.57079632679490f;  // pi / 2
+    o->fade_start = 1.96349540849362f;  // 5 pi / 8
+    o->fade_width = 0.39269908169872f;  // pi / 8
     o->model = SGX_DIFF_MODEL_SLAB;
     o->half_thickness = 0.3f;
     o->tau_perp = 4.0f;

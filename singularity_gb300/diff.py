@@ -35,8 +35,8 @@ class DiffOptions:
     slab half-thickness (M) and optical depth across."""
     precision: int = N.PRECISION_FP32
     edge_width: float = 0.1
-    fade_start: float = 0.75 * math.pi
-    fade_width: float = 0.5 * math.pi
+    fade_start: float = 0.625 * math.pi
+    fade_width: float = 0.125 * math.pi
     model: int = N.DIFF_MODEL_SLAB
     half_thickness: float = 0.3
     tau_perp: float = 4.0
@@ -157,9 +157,11 @@ class FitResult:
 
 def fit(dr: DiffRenderer, u: N.Uniforms, target, init: Sequence[float], steps: int = 200,
         lr: Sequence[float] = (0.01, 0.01, 0.05, 0.01), opts: Optional[DiffOptions] = None,
-        bounds: Sequence[tuple] = ((0.0, 0.998), (0.05, math.pi - 0.05), (2.0, 20.0), (0.2, 5.0))) -> FitResult:
+        bounds: Sequence[tuple] = ((0.0, 0.998), (0.05, math.pi - 0.05), (2.0, 20.0), (0.2, 5.0)),
+        cosine: bool = True) -> FitResult:
     """Adam on the mean-squared image error to `target` (a CUDA tensor of the
-    form's image), one learning rate per parameter; parameters are clamped to
+    form's image), one learning rate per parameter, decayed along a half
+    cosine to 5 % by the last step when `cosine`; parameters are clamped to
     `bounds` after every step."""
     import time
 
@@ -172,7 +174,8 @@ def fit(dr: DiffRenderer, u: N.Uniforms, target, init: Sequence[float], steps: i
     hist_p = [p.detach().clone().numpy()]
     hist_l, hist_g = [], []
     t0 = time.perf_counter()
-    for _ in range(steps):
+    for it in range(steps):
+        scale = 0.05 + 0.95 * 0.5 * (1.0 + math.cos(math.pi * it / max(1, steps))) if cosine else 1.0
         opt.zero_grad()
         img = render(p, dr, u, opts)
         loss = torch.mean((img - target) ** 2)
@@ -185,7 +188,7 @@ def fit(dr: DiffRenderer, u: N.Uniforms, target, init: Sequence[float], steps: i
             before = p.detach().clone()
         opt.step()
         with torch.no_grad():
-            p.copy_(torch.minimum(torch.maximum(before + (p - before) * lr_t, lo), hi))
+            p.copy_(torch.minimum(torch.maximum(before + (p - before) * lr_t * scale, lo), hi))
         hist_p.append(p.detach().clone().numpy())
     torch.cuda.synchronize()
     return FitResult(np.array(hist_p), np.array(hist_l), np.array(hist_g), time.perf_counter() - t0)
