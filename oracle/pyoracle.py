@@ -117,6 +117,44 @@ def schw_integrate(y8, h_base: float, rs: float, r_out: float, adaptive: bool, b
     return y, n, me.value, ml.value
 
 
+def schw_rk4_n(y8, h: float, rs: float, n: int = 1) -> np.ndarray:
+    """n FP32 Schwarzschild RK4 steps of (t, r, theta, phi, u^t, u^r, u^theta, u^phi)."""
+    y = np.ascontiguousarray(y8, dtype=np.float32).copy()
+    lib().oracle_schw_rk4_n_f32(_p(y), C.c_float(h), C.c_float(rs), C.c_int64(n))
+    return y
+
+
+def kerr_rhs(y6, c5) -> np.ndarray:
+    """FP32 Kerr Hamiltonian RHS of (t, r, theta, phi, p_r, p_theta); c5 = (E, L, Q, a, M)."""
+    y = np.ascontiguousarray(y6, dtype=np.float32)
+    c = np.ascontiguousarray(c5, dtype=np.float32)
+    d = np.zeros(6, dtype=np.float32)
+    lib().oracle_kerr_rhs_f32(_p(y), _p(c), _p(d))
+    return d
+
+
+def kerr_two_H(r, th, pr, pth, c5) -> float:
+    c = np.ascontiguousarray(c5, dtype=np.float32)
+    fn = lib().oracle_kerr_two_H_f32
+    fn.restype = C.c_float
+    return float(fn(C.c_float(r), C.c_float(th), C.c_float(pr), C.c_float(pth), _p(c)))
+
+
+def kerr_rk4_n(y6, h: float, c5, n: int = 1) -> np.ndarray:
+    """n FP32 fixed-step Kerr RK4 steps (with the pole damping)."""
+    y = np.ascontiguousarray(y6, dtype=np.float32).copy()
+    c = np.ascontiguousarray(c5, dtype=np.float32)
+    lib().oracle_kerr_rk4_n_f32(_p(y), C.c_float(h), _p(c), C.c_int64(n))
+    return y
+
+
+def crossing(th_prev: float, th_curr: float):
+    """(crossed, frac) of the equatorial-crossing test in FP32."""
+    frac = C.c_float()
+    x = lib().oracle_crossing_f32(C.c_float(th_prev), C.c_float(th_curr), C.byref(frac))
+    return bool(x), frac.value
+
+
 def build(ref: bool = True) -> None:
     """Compile the oracle (and the reference host build when its sources exist)."""
     subprocess.run(["make", "-s", "-C", str(HERE)], check=True)

@@ -645,6 +645,12 @@ template <class T> __device__ __forceinline__ bool crossed_equator(T th_prev, T 
     return x;
 }
 
+// Sign change of theta - pi/2 across a step, without the crossing fraction.
+template <class T> __device__ __forceinline__ bool crosses_plane(T th_prev, T th_curr) {
+    const T mid = DLIT(1.5707963267948966);
+    return ((th_prev - mid) * (th_curr - mid)) < DLIT(0.0);
+}
+
 // ---------------------------------------------------------------------------
 // Error-controlled Kerr integration (the adaptive extension; the CPU oracle's
 // adaptive_oracle.hpp is its specification, operation for operation).
@@ -700,12 +706,40 @@ __device__ __forceinline__ C error_norm(const KS<T>& y, const KAttempt<T>& a, fl
     return e;
 }
 
+// The same norm with one approximate reciprocal per component and a single
+// scale at the end: max_i |k4_i - k5_i| / (1 + max(|y_i|, |y4_i|)) * |h/6| / tol.
+// Equal to error_norm up to rounding (a few ulp), for the FP32 fast path.
+template <class T>
+__device__ __forceinline__ T error_norm_fast(const KS<T>& y, const KAttempt<T>& a, float tol_f) {
+    auto one = [&](T yv, T y4v, T k4v, T k5v) {
+        const T m = DM<T>::fmax_(absv(yv), absv(y4v));
+        return absv(k4v - k5v) * DM<T>::rcp_fast(DLIT(1.0) + m);
+    };
+    T e = one(y.r, a.y4.r, a.k4.r, a.k5.r);
+    e = DM<T>::fmax_(e, one(y.th, a.y4.th, a.k4.th, a.k5.th));
+    e = DM<T>::fmax_(e, one(y.ph, a.y4.ph, a.k4.ph, a.k5.ph));
+    e = DM<T>::fmax_(e, one(y.pr, a.y4.pr, a.k4.pr, a.k5.pr));
+    e = DM<T>::fmax_(e, one(y.pth, a.y4.pth, a.k4.pth, a.k5.pth));
+    e = e * (absv(a.h6) * DM<T>::rcp_fast(T(tol_f)));
+    if (!(e <= DLIT(1e30))) e = DLIT(1e30);
+    return e;
+}
+
 // h *= clamp(0.9 / err^(1/4), 0.2, 4) with IEEE sqrt and division only.
 template <class C> __device__ __forceinline__ C step_factor(C e) {
     if (e <= C(1e-30f)) return C(4.0f);
     C f = C(0.9f) / sqrt(sqrt(e));
     f = f < C(0.2f) ? C(0.2f) : f;
     f = f > C(4.0f) ? C(4.0f) : f;
+    return f;
+}
+
+// The same factor from one square root and one approximate reciprocal square root.
+__device__ __forceinline__ float step_factor_fast(float e) {
+    if (e <= 1e-30f) return 4.0f;
+    float f = 0.9f * rsqrtf(sqrtf(e));
+    f = f < 0.2f ? 0.2f : f;
+    f = f > 4.0f ? 4.0f : f;
     return f;
 }
 

@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "sgx_device.cuh"
 #include "sgx_kernels.hpp"
@@ -254,6 +255,10 @@ template <class T, int FL> struct KerrAdaptive {
             const double e = error_norm<double>(y, at, pass.tol);
             accept = e <= 1.0;
             h = T(float(double(float(h)) * step_factor<double>(e)));
+        } else if constexpr (FAST && std::is_same_v<T, float>) {
+            const T e = error_norm_fast<T>(y, at, pass.tol);
+            accept = e <= DLIT(1.0);
+            h = h * step_factor_fast(e);
         } else {
             const T e = error_norm<T>(y, at, pass.tol);
             accept = e <= DLIT(1.0);
@@ -262,8 +267,7 @@ template <class T, int FL> struct KerrAdaptive {
         if (!accept) {
             ++rej;
         } else {
-            T frac;
-            if ((v.flags & SGX_FLAG_DISC_ON) && crossed_equator(y.th, at.y4.th, frac)) {
+            if ((v.flags & SGX_FLAG_DISC_ON) && crosses_plane(y.th, at.y4.th)) {
                 const T hs = at.h6 * DLIT(6.0);
                 const T sfr = crossing_fraction(y.th, at.y4.th, k1.th, at.k5.th, hs);
                 const T r_cross = hermite(y.r, at.y4.r, k1.r, at.k5.r, hs, sfr);
