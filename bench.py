@@ -205,6 +205,11 @@ def precision_study(S, N, O, lib, r, u, d_out, stream, torch, main_opts) -> dict
         if name == "mixed":
             out["mixed_zone_step_frac"] = st.zone_steps / max(1, st.steps)
     out["fp32_over_fp64"] = out["fp32_mrays_s"] / out["fp64_mrays_s"]
+    # rhs_form 2: the same FP32 integrator with the SFU sine/cosine away from the poles
+    o = S.default_opts(integrator=N.INTEGRATOR_ADAPTIVE, sample_count=SPP_PER_STEP, rhs_form=2)
+    timed_pass(lib, N, r, u, o, d_out, stream, torch)
+    ms, st = timed_pass(lib, N, r, u, o, d_out, stream, torch)
+    out["fp32_hwtrig_mrays_s"] = rays / (ms / 1e3) / 1e6
     # reference algorithm (fixed-step RK4, h = 0.4) through the same kernels
     o = S.default_opts(sample_count=SPP_PER_STEP)
     timed_pass(lib, N, r, u, o, d_out, stream, torch)
@@ -215,8 +220,10 @@ def precision_study(S, N, O, lib, r, u, d_out, stream, torch, main_opts) -> dict
     rng = np.random.default_rng(0)
     pix = rng.choice(npix, 4096, replace=False).astype(np.uint32)
     imgs = {}
-    for name, prec in (("fp32", N.PRECISION_FP32), ("mixed", N.PRECISION_MIXED)):
-        o = S.default_opts(integrator=N.INTEGRATOR_ADAPTIVE, precision=prec, format=N.FORMAT_RGBA32F)
+    for name, prec, form in (("fp32", N.PRECISION_FP32, 0), ("mixed", N.PRECISION_MIXED, 0),
+                             ("fp32_hwtrig", N.PRECISION_FP32, 2)):
+        o = S.default_opts(integrator=N.INTEGRATOR_ADAPTIVE, precision=prec, format=N.FORMAT_RGBA32F,
+                           rhs_form=form)
         r.render(u, o)
         imgs[name] = r.capture(N.FORMAT_RGBA32F).reshape(-1, 4)[pix, :3].astype(np.float64)
     ad64 = O.adaptive_opts()

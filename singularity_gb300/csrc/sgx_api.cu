@@ -98,7 +98,7 @@ sgx_status check_opts(sgx_context* c, const sgx_render_opts& o) {
     if (o.precision > SGX_PRECISION_FP64) return fail(c, SGX_ERR_INVALID_ARGUMENT, "unknown precision");
     if (o.integrator > SGX_INTEGRATOR_ADAPTIVE) return fail(c, SGX_ERR_INVALID_ARGUMENT, "unknown integrator");
     if (o.format > SGX_FORMAT_RGBA16F_HDR) return fail(c, SGX_ERR_INVALID_ARGUMENT, "unknown format");
-    if (o.rhs_form > 1) return fail(c, SGX_ERR_INVALID_ARGUMENT, "unknown rhs_form");
+    if (o.rhs_form > 2) return fail(c, SGX_ERR_INVALID_ARGUMENT, "unknown rhs_form");
     if ((o.tile_w == 0) != (o.tile_h == 0) || o.tile_w > 4096 || o.tile_h > 4096)
         return fail(c, SGX_ERR_INVALID_ARGUMENT, "tile_w and tile_h must both be 0 or both in [1, 4096]");
     if (o.integrator == SGX_INTEGRATOR_ADAPTIVE) {
@@ -160,7 +160,7 @@ sgx_status render_impl(sgx_context* c, const sgx_uniforms* u, const sgx_render_o
         SGX_CUDA(c, cudaMemsetAsync(c->d_counters, 0, sizeof(sgxk::PassCounters), st));
         SGX_CUDA(c, cudaEventRecord(c->ev_trace0, st));
         sgxk::LaunchShape shape{int(o.block_threads), int(o.blocks_per_sm)};
-        SGX_CUDA(c, sgxk::launch_trace(int(u->metric_type), int(o.precision), int(o.integrator), o.rhs_form == 0,
+        SGX_CUDA(c, sgxk::launch_trace(int(u->metric_type), int(o.precision), int(o.integrator), int(o.rhs_form),
                                        pass, shape, st));
         SGX_CUDA(c, cudaEventRecord(c->ev_trace1, st));
         const bool first = (s0 == 0);
@@ -376,7 +376,7 @@ sgx_status sgx_trace_samples(sgx_context* c, const sgx_uniforms* u, const sgx_re
     if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_u, u, sizeof(sgx_uniforms), cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) e = sgxk::launch_setup_views(c->d_u, 1, c->d_view, int(o.precision), c->stream);
     if (e == cudaSuccess)
-        e = sgxk::launch_probe(c->d_view, int(u->metric_type), int(o.precision), int(o.integrator), o.rhs_form == 0, n, d_gx,
+        e = sgxk::launch_probe(c->d_view, int(u->metric_type), int(o.precision), int(o.integrator), int(o.rhs_form), n, d_gx,
                                d_gy, d_s, d_hdr, d_steps, d_term, o.tolerance, o.h_init_frac, o.h_max_frac,
                                o.fp64_zone, c->stream);
     if (e == cudaSuccess && hdr3) e = cudaMemcpyAsync(hdr3, d_hdr, n * 12, cudaMemcpyDeviceToHost, c->stream);

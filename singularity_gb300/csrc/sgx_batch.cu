@@ -70,7 +70,7 @@ cudaError_t enqueue(sgx_batch* b, const sgx_render_opts& o, const sgxk::ViewPlan
     cudaError_t e = cudaMemsetAsync(b->d_counters, 0, sizeof(sgxk::PassCounters), st);
     if (e == cudaSuccess) e = sgxk::launch_setup_views(b->d_u, b->n, b->d_views, int(o.precision), st);
     if (e == cudaSuccess)
-        e = sgxk::launch_trace(int(b->metric), int(o.precision), int(o.integrator), o.rhs_form == 0, pass,
+        e = sgxk::launch_trace(int(b->metric), int(o.precision), int(o.integrator), int(o.rhs_form), pass,
                                sgxk::LaunchShape{int(o.block_threads), int(o.blocks_per_sm)}, st);
     if (e == cudaSuccess)
         e = sgxk::launch_accumulate(int(o.precision), pass.vs, results, b->d_acc, true, true, b->format, b->d_out, st);

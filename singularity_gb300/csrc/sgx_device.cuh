@@ -22,6 +22,8 @@
 
 #include <cstdint>
 
+#include <type_traits>
+
 #include "sgx_uniforms.h"
 
 namespace sgxd {
@@ -482,15 +484,32 @@ __device__ __forceinline__ KS<T> kerr_rhs_fast_sc(const KS<T>& s, T st, T ct, co
     return d;
 }
 
-template <class T> __device__ __forceinline__ KS<T> kerr_rhs_fast(const KS<T>& s, const View<T>& v, const KC<T>& c) {
+// Kerr RHS forms: 0 = the reference's divisions, 1 = shared reciprocals,
+// 2 = shared reciprocals with the SFU's sine/cosine (FP32 only; CUDA's
+// __sincosf) wherever |sin(theta)| >= 1/4 — its absolute error (~4e-7) would
+// be a large relative error of the 1/sin^2 terms nearer the poles, where the
+// IEEE-accurate sincosf is kept.
+constexpr int RHS_REF = 0, RHS_SHARED = 1, RHS_SHARED_HWTRIG = 2;
+
+template <class T, int FORM> __device__ __forceinline__ void rhs_sincos(T x, T* s, T* c) {
+    if constexpr (FORM == RHS_SHARED_HWTRIG && std::is_same_v<T, float>) {
+        __sincosf(x, s, c);
+        if (fabsf(*s) < 0.25f) sincosf(x, s, c);
+    } else {
+        DM<T>::sincos_(x, s, c);
+    }
+}
+
+template <class T, int FORM = RHS_SHARED>
+__device__ __forceinline__ KS<T> kerr_rhs_fast(const KS<T>& s, const View<T>& v, const KC<T>& c) {
     T st, ct;
-    DM<T>::sincos_(s.th, &st, &ct);
+    rhs_sincos<T, FORM>(s.th, &st, &ct);
     return kerr_rhs_fast_sc(s, st, ct, v, c);
 }
 
-template <class T, bool FAST>
+template <class T, int FORM>
 __device__ __forceinline__ KS<T> kerr_rhs(const KS<T>& s, const View<T>& v, const KC<T>& c) {
-    if constexpr (FAST) return kerr_rhs_fast(s, v, c);
+    if constexpr (FORM != RHS_REF) return kerr_rhs_fast<T, FORM>(s, v, c);
     else return kerr_rhs_ref(s, v, c);
 }
 
@@ -510,22 +529,22 @@ template <class T> __device__ __forceinline__ T fixed_step_h(const View<T>& v, T
 }
 
 // Fixed-step RK4 with the reference's near-pole damping (kerr_hamilton.h:165-178).
-template <class T, bool FAST>
+template <class T, int FORM>
 __device__ __forceinline__ KS<T> kerr_rk4(const KS<T>& y, T h, const View<T>& v, const KC<T>& c) {
     // sin(theta) of the step's start serves both the pole damping and k1.
     T s0, c0;
-    DM<T>::sincos_(y.th, &s0, &c0);
+    rhs_sincos<T, FORM>(y.th, &s0, &c0);
     T st = (s0 < DLIT(0.0)) ? -s0 : s0;
     T ps = st * DLIT(5.0);
     ps = (ps > DLIT(1.0)) ? DLIT(1.0) : ((ps < DLIT(0.05)) ? DLIT(0.05) : ps);
     h = h * ps;
     const T hh = DLIT(0.5) * h;
     KS<T> k1;
-    if constexpr (FAST) k1 = kerr_rhs_fast_sc(y, s0, c0, v, c);
+    if constexpr (FORM != RHS_REF) k1 = kerr_rhs_fast_sc(y, s0, c0, v, c);
     else k1 = kerr_rhs_ref(y, v, c);
-    const KS<T> k2 = kerr_rhs<T, FAST>(ks_axpy(y, k1, hh), v, c);
-    const KS<T> k3 = kerr_rhs<T, FAST>(ks_axpy(y, k2, hh), v, c);
-    const KS<T> k4 = kerr_rhs<T, FAST>(ks_axpy(y, k3, h), v, c);
+    const KS<T> k2 = kerr_rhs<T, FORM>(ks_axpy(y, k1, hh), v, c);
+    const KS<T> k3 = kerr_rhs<T, FORM>(ks_axpy(y, k2, hh), v, c);
+    const KS<T> k4 = kerr_rhs<T, FORM>(ks_axpy(y, k3, h), v, c);
     const T h6 = h / DLIT(6.0);
     KS<T> o;
     o.r = y.r + ((k1.r + k2.r * DLIT(2.0)) + (k3.r * DLIT(2.0) + k4.r)) * h6;
@@ -661,21 +680,21 @@ template <class T> struct KAttempt {
 };
 
 // RK4 stages from y with k1 = f(y) known, plus the first-same-as-last stage.
-template <class T, bool FAST>
+template <class T, int FORM>
 __device__ __forceinline__ KAttempt<T> kerr_attempt(const KS<T>& y, const KS<T>& k1, T h, const View<T>& v,
                                                     const KC<T>& c) {
     KAttempt<T> at;
     const T hh = DLIT(0.5) * h;
-    const KS<T> k2 = kerr_rhs<T, FAST>(ks_axpy(y, k1, hh), v, c);
-    const KS<T> k3 = kerr_rhs<T, FAST>(ks_axpy(y, k2, hh), v, c);
-    at.k4 = kerr_rhs<T, FAST>(ks_axpy(y, k3, h), v, c);
+    const KS<T> k2 = kerr_rhs<T, FORM>(ks_axpy(y, k1, hh), v, c);
+    const KS<T> k3 = kerr_rhs<T, FORM>(ks_axpy(y, k2, hh), v, c);
+    at.k4 = kerr_rhs<T, FORM>(ks_axpy(y, k3, h), v, c);
     at.h6 = h / DLIT(6.0);
     at.y4.r = y.r + ((k1.r + k2.r * DLIT(2.0)) + (k3.r * DLIT(2.0) + at.k4.r)) * at.h6;
     at.y4.th = y.th + ((k1.th + k2.th * DLIT(2.0)) + (k3.th * DLIT(2.0) + at.k4.th)) * at.h6;
     at.y4.ph = y.ph + ((k1.ph + k2.ph * DLIT(2.0)) + (k3.ph * DLIT(2.0) + at.k4.ph)) * at.h6;
     at.y4.pr = y.pr + ((k1.pr + k2.pr * DLIT(2.0)) + (k3.pr * DLIT(2.0) + at.k4.pr)) * at.h6;
     at.y4.pth = y.pth + ((k1.pth + k2.pth * DLIT(2.0)) + (k3.pth * DLIT(2.0) + at.k4.pth)) * at.h6;
-    at.k5 = kerr_rhs<T, FAST>(at.y4, v, c);
+    at.k5 = kerr_rhs<T, FORM>(at.y4, v, c);
     return at;
 }
 

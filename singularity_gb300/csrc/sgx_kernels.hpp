@@ -81,11 +81,11 @@ cudaError_t launch_setup_views(const sgx_uniforms* d_u, std::uint32_t n, void* d
                                cudaStream_t st);
 
 // Persistent tracer over a ViewSet.  precision: sgx_precision; integrator: sgx_integrator.
-cudaError_t launch_trace(int metric, int precision, int integrator, bool fast_math, const PassDesc& pass,
+cudaError_t launch_trace(int metric, int precision, int integrator, int rhs_form, const PassDesc& pass,
                          LaunchShape shape, cudaStream_t st);
 
 // Per-sample probe (parity tests) of a single view: n samples, device arrays.
-cudaError_t launch_probe(const void* d_view, int metric, int precision, int integrator, bool fast_math,
+cudaError_t launch_probe(const void* d_view, int metric, int precision, int integrator, int rhs_form,
                          std::uint64_t n, const std::uint32_t* gx, const std::uint32_t* gy, const std::uint32_t* s,
                          float* hdr3, std::uint32_t* steps, std::uint32_t* term, float tol, float h_init_frac,
                          float h_max_frac, float zone, cudaStream_t st);

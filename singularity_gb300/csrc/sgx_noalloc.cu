@@ -111,7 +111,7 @@ extern "C" sgx_status sgx_render_noalloc(const sgx_uniforms* u, const sgx_render
         set_err(err, err_len, "sgx_render_noalloc: precision must be FP32 or FP64 with the fixed-step integrator");
         return SGX_ERR_INVALID_ARGUMENT;
     }
-    if (o.integrator != SGX_INTEGRATOR_FIXED || o.rhs_form > 1 ||
+    if (o.integrator != SGX_INTEGRATOR_FIXED || o.rhs_form > 2 ||
         (format != SGX_FORMAT_RGBA8_SRGB && format != SGX_FORMAT_RGBA32F)) {
         set_err(err, err_len, "sgx_render_noalloc: fixed-step integrator and RGBA8/RGBA32F output only");
         return SGX_ERR_INVALID_ARGUMENT;
@@ -174,7 +174,7 @@ extern "C" sgx_status sgx_render_noalloc(const sgx_uniforms* u, const sgx_render
     if (e == cudaSuccess) e = cudaMemsetAsync(counters, 0, sizeof(sgxk::PassCounters), st);
     if (e == cudaSuccess) e = sgxk::launch_setup_views(d_u, 1, d_view, int(o.precision), st);
     if (e == cudaSuccess)
-        e = sgxk::launch_trace(int(u->metric_type), int(o.precision), int(o.integrator), o.rhs_form == 0, pass,
+        e = sgxk::launch_trace(int(u->metric_type), int(o.precision), int(o.integrator), int(o.rhs_form), pass,
                                shape, st);
     if (e == cudaSuccess)
         e = sgxk::launch_accumulate(int(o.precision), pass.vs, results, acc, true, true, format, d_out, st);

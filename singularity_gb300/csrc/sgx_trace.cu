@@ -59,12 +59,14 @@ __device__ __forceinline__ std::uint32_t pack_meta(std::uint32_t term, std::uint
 }
 
 // Policy flags: bit 0 = shared-reciprocal Kerr RHS, bit 1 = mixed precision.
-constexpr int FL_FAST = 1;
+constexpr int FL_FAST = 1;    // shared-reciprocal Kerr RHS
+constexpr int FL_HWTRIG = 4;  // ... with the SFU sine/cosine (FP32)
 constexpr int FL_MIXED = 2;
 
 // Kerr, fixed step (geodesic_kernel.cu:303-403).
 template <class T, int FL> struct KerrFixed {
     static constexpr bool FAST = (FL & FL_FAST) != 0;
+    static constexpr int FORM = FAST ? ((FL & FL_HWTRIG) ? RHS_SHARED_HWTRIG : RHS_SHARED) : RHS_REF;
     KS<T> y;
     KC<T> c;
     T prev_th, prev_r;
@@ -115,7 +117,7 @@ template <class T, int FL> struct KerrFixed {
         }
         prev_th = y.th;
         prev_r = y.r;
-        y = kerr_rk4<T, FAST>(y, fixed_step_h(v, y.r), v, c);
+        y = kerr_rk4<T, FORM>(y, fixed_step_h(v, y.r), v, c);
         if (++steps >= v.max_steps) {
             term = TERM_BUDGET;
             return true;
@@ -191,6 +193,7 @@ template <class T, int FL> struct SchwFixed {
 // step() is one attempt; max_steps bounds the attempts.
 template <class T, int FL> struct KerrAdaptive {
     static constexpr bool FAST = (FL & FL_FAST) != 0;
+    static constexpr int FORM = FAST ? ((FL & FL_HWTRIG) ? RHS_SHARED_HWTRIG : RHS_SHARED) : RHS_REF;
     static constexpr bool MIXED = (FL & FL_MIXED) != 0;
     KS<T> y, k1;
     KC<T> c;
@@ -221,7 +224,7 @@ template <class T, int FL> struct KerrAdaptive {
         }
         c = make_kc(v, E, L);
         h = T(pass.h_init_frac) * y.r;
-        k1 = kerr_rhs<T, FAST>(y, v, c);
+        k1 = kerr_rhs<T, FORM>(y, v, c);
         if (v.max_steps == 0u) {
             term = TERM_BUDGET;
             return false;
@@ -242,7 +245,7 @@ template <class T, int FL> struct KerrAdaptive {
         }
         const T hmax = T(pass.h_max_frac) * y.r;
         h = h > hmax ? hmax : h;
-        const KAttempt<T> at = kerr_attempt<T, FAST>(y, k1, h, v, c);
+        const KAttempt<T> at = kerr_attempt<T, FORM>(y, k1, h, v, c);
         ++steps;
         bool accept;
         bool in_zone = false;
@@ -630,25 +633,31 @@ cudaError_t run_probe(const void* d_view, std::uint64_t n, const std::uint32_t* 
 
 // One call site per (metric, precision, integrator, RHS form): F is invoked
 // with the chosen <T, Policy, FL> as a generic lambda's template arguments.
+// rhs_form: 0 shared reciprocals, 1 the reference's divisions, 2 shared
+// reciprocals with the SFU sine/cosine (FP32; FP64 runs form 0).
 template <class F>
-cudaError_t dispatch(int metric, int precision, int integrator, bool fast, F&& f) {
+cudaError_t dispatch(int metric, int precision, int integrator, int rhs_form, F&& f) {
     const bool adaptive = integrator == SGX_INTEGRATOR_ADAPTIVE;
+    const bool ref = rhs_form == 1, hw = rhs_form == 2;
     if (metric == SGX_METRIC_KERR && adaptive) {
         if (precision == SGX_PRECISION_FP64)
-            return fast ? f.template operator()<double, KerrAdaptive, FL_FAST>()
-                        : f.template operator()<double, KerrAdaptive, 0>();
+            return ref ? f.template operator()<double, KerrAdaptive, 0>()
+                       : f.template operator()<double, KerrAdaptive, FL_FAST>();
         if (precision == SGX_PRECISION_MIXED)
-            return fast ? f.template operator()<float, KerrAdaptive, FL_FAST | FL_MIXED>()
-                        : f.template operator()<float, KerrAdaptive, FL_MIXED>();
-        return fast ? f.template operator()<float, KerrAdaptive, FL_FAST>()
-                    : f.template operator()<float, KerrAdaptive, 0>();
+            return ref  ? f.template operator()<float, KerrAdaptive, FL_MIXED>()
+                   : hw ? f.template operator()<float, KerrAdaptive, FL_FAST | FL_MIXED | FL_HWTRIG>()
+                        : f.template operator()<float, KerrAdaptive, FL_FAST | FL_MIXED>();
+        return ref  ? f.template operator()<float, KerrAdaptive, 0>()
+               : hw ? f.template operator()<float, KerrAdaptive, FL_FAST | FL_HWTRIG>()
+                    : f.template operator()<float, KerrAdaptive, FL_FAST>();
     }
     if (metric == SGX_METRIC_KERR) {
         if (precision == SGX_PRECISION_FP64)
-            return fast ? f.template operator()<double, KerrFixed, FL_FAST>()
-                        : f.template operator()<double, KerrFixed, 0>();
-        return fast ? f.template operator()<float, KerrFixed, FL_FAST>()
-                    : f.template operator()<float, KerrFixed, 0>();
+            return ref ? f.template operator()<double, KerrFixed, 0>()
+                       : f.template operator()<double, KerrFixed, FL_FAST>();
+        return ref  ? f.template operator()<float, KerrFixed, 0>()
+               : hw ? f.template operator()<float, KerrFixed, FL_FAST | FL_HWTRIG>()
+                    : f.template operator()<float, KerrFixed, FL_FAST>();
     }
     // Schwarzschild: the reference's fixed-step integrator for every form.
     if (precision == SGX_PRECISION_FP64) return f.template operator()<double, SchwFixed, 0>();
@@ -739,15 +748,15 @@ cudaError_t launch_setup_views(const sgx_uniforms* d_u, std::uint32_t n, void* d
     return cudaGetLastError();
 }
 
-cudaError_t launch_trace(int metric, int precision, int integrator, bool fast_math, const PassDesc& pass,
+cudaError_t launch_trace(int metric, int precision, int integrator, int rhs_form, const PassDesc& pass,
                          LaunchShape shape, cudaStream_t st) {
-    return dispatch(metric, precision, integrator, fast_math,
+    return dispatch(metric, precision, integrator, rhs_form,
                     [&]<class T, template <class, int> class Policy, int FL>() {
                         return run_persistent<T, Policy, FL>(pass, shape, st);
                     });
 }
 
-cudaError_t launch_probe(const void* d_view, int metric, int precision, int integrator, bool fast_math,
+cudaError_t launch_probe(const void* d_view, int metric, int precision, int integrator, int rhs_form,
                          std::uint64_t n, const std::uint32_t* gx, const std::uint32_t* gy, const std::uint32_t* s,
                          float* hdr3, std::uint32_t* steps, std::uint32_t* term, float tol, float h_init_frac,
                          float h_max_frac, float zone, cudaStream_t st) {
@@ -756,7 +765,7 @@ cudaError_t launch_probe(const void* d_view, int metric, int precision, int inte
     pass.h_init_frac = h_init_frac;
     pass.h_max_frac = h_max_frac;
     pass.zone = zone;
-    return dispatch(metric, precision, integrator, fast_math,
+    return dispatch(metric, precision, integrator, rhs_form,
                     [&]<class T, template <class, int> class Policy, int FL>() {
                         return run_probe<T, Policy, FL>(d_view, n, gx, gy, s, hdr3, steps, term, pass, st);
                     });

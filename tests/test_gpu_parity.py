@@ -43,7 +43,7 @@ def test_probe_matches_reference_host_vectors(renderer, oracle, host_vectors):
         assert ok.mean() >= SAMPLE_FRAC, name
 
 
-@pytest.mark.parametrize("rhs_form", [0, 1])
+@pytest.mark.parametrize("rhs_form", [0, 1, 2])
 def test_render_matches_oracle(renderer, oracle, host_vectors, sgx, rhs_form):
     z, names = host_vectors
     opts = sgx.default_opts(rhs_form=rhs_form)
