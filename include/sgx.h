@@ -322,6 +322,11 @@ typedef struct sgx_diff_params {
 } sgx_diff_params;
 #define SGX_DIFF_MODEL_CROSSING 0u
 #define SGX_DIFF_MODEL_SLAB 1u
+/* How the backward pass multiplies by a step's Jacobian: the hand-derived
+ * reverse pass (default), or the Jacobian built with 9-lane dual numbers
+ * (slower; kept as the cross-check of the first). */
+#define SGX_DIFF_ADJOINT_REVERSE 0u
+#define SGX_DIFF_ADJOINT_DUAL 1u
 typedef struct sgx_diff_opts {
     uint32_t struct_size;
     uint32_t precision;    /* SGX_PRECISION_FP32 or SGX_PRECISION_FP64 */
@@ -331,6 +336,8 @@ typedef struct sgx_diff_opts {
     uint32_t model;        /* SGX_DIFF_MODEL_SLAB (default) or SGX_DIFF_MODEL_CROSSING */
     float half_thickness;  /* slab half-thickness, units of M (0.3) */
     float tau_perp;        /* slab optical depth across (4) */
+    uint32_t adjoint_form; /* SGX_DIFF_ADJOINT_REVERSE (default) or SGX_DIFF_ADJOINT_DUAL */
+    uint32_t reserved;
 } sgx_diff_opts;
 void sgx_diff_opts_default(sgx_diff_opts* opts);
 /* Forward pass: renders the form for `params` with size, samples, distance

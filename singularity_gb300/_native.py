@@ -132,10 +132,12 @@ class DiffParams(C.Structure):
 class DiffOpts(C.Structure):
     _fields_ = [("struct_size", C.c_uint32), ("precision", C.c_uint32), ("edge_width", C.c_float),
                 ("fade_start", C.c_float), ("fade_width", C.c_float), ("model", C.c_uint32),
-                ("half_thickness", C.c_float), ("tau_perp", C.c_float)]
+                ("half_thickness", C.c_float), ("tau_perp", C.c_float), ("adjoint_form", C.c_uint32),
+                ("reserved", C.c_uint32)]
 
 
 DIFF_MODEL_CROSSING, DIFF_MODEL_SLAB = 0, 1
+DIFF_ADJOINT_REVERSE, DIFF_ADJOINT_DUAL = 0, 1
 
 
 _P = C.c_void_p

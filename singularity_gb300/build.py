@@ -26,7 +26,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++20", "-Xcompiler", "-fPIC", "-Xcompil
               f"-I{INCLUDE}", f"-I{CSRC}"]
 CXX_FLAGS = ["-O2", "-std=c++20", "-fPIC", "-Wall", f"-I{INCLUDE}", f"-I{CSRC}"]
 
-CUDA_UNITS = ["sgx_trace.cu", "sgx_api.cu", "sgx_batch.cu", "sgx_post.cu", "sgx_probe.cu", "sgx_noalloc.cu", "sgx_diff.cu"]
+CUDA_UNITS = ["sgx_trace.cu", "sgx_api.cu", "sgx_batch.cu", "sgx_post.cu", "sgx_probe.cu", "sgx_noalloc.cu", "sgx_diff.cu", "sgx_diff64.cu"]
 HOST_UNITS = ["sgx_host.cpp"]
 
 

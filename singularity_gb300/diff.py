@@ -40,6 +40,7 @@ class DiffOptions:
     model: int = N.DIFF_MODEL_SLAB
     half_thickness: float = 0.3
     tau_perp: float = 4.0
+    adjoint_form: int = N.DIFF_ADJOINT_REVERSE
 
     def to_c(self) -> N.DiffOpts:
         o = N.DiffOpts()
@@ -51,6 +52,7 @@ class DiffOptions:
         o.model = self.model
         o.half_thickness = self.half_thickness
         o.tau_perp = self.tau_perp
+        o.adjoint_form = self.adjoint_form
         return o
 
     def oracle_form(self) -> dict:

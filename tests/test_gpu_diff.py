@@ -98,6 +98,25 @@ def test_crossing_adjoint_smooth_parameters(diff, sgx, oracle):
     assert np.all(np.abs(g32[2:] - g64[2:]) <= 1e-3 * np.abs(g64[2:]))
 
 
+@pytest.mark.parametrize("model", [1, 0])
+@pytest.mark.parametrize("prec", [0, 2])
+def test_reverse_pass_matches_dual_jacobians(diff, sgx, prec, model):
+    """The hand-derived reverse pass of a step against the step Jacobian built
+    with dual numbers: the same gradient to rounding."""
+    import torch
+    from singularity_gb300 import diff as D
+    base, tgt, guess = _setup(sgx, 48, 32, 2)
+    target = diff.forward(base, tgt, D.DiffOptions(precision=prec, model=model)).clone()
+    out = []
+    for form in (sgx._native.DIFF_ADJOINT_REVERSE, sgx._native.DIFF_ADJOINT_DUAL):
+        o = D.DiffOptions(precision=prec, model=model, adjoint_form=form)
+        img = diff.forward(base, guess, o)
+        out.append(diff.backward(_loss_grad_image(img, target)))
+    rel = np.abs(out[0] - out[1]) / np.abs(out[1])
+    print(f"prec {prec} model {model}: reverse {out[0]} dual {out[1]} rel {rel}")
+    assert np.all(rel <= (1e-9 if prec == 2 else 1e-4)), rel
+
+
 def test_backward_is_deterministic(diff, sgx):
     import torch
     base, tgt, guess = _setup(sgx, 40, 30, 2)
