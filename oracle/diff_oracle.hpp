@@ -32,7 +32,8 @@
 //     in temperature (identical outside that band);
 //   * the disc temperature scale multiplies the peak temperature.
 //   * a ray is captured inside the prograde photon orbit radius less 0.05 M
-//     instead of at 1.02 r_+ (see diff_trace).
+//     instead of at 1.02 r_+ (see diff_trace), and ends once it moves outward
+//     beyond r_out (escaped rays are black here).
 // Integration is the reference's fixed-step Kerr RK4 with its pole damping
 // (kerr_hamilton.h:165-178), checks and escape as geodesic_kernel.cu:351-401.
 
@@ -246,6 +247,10 @@ inline DiffOut<T> diff_trace(const sgx_uniforms& ub, const DiffParams& dp, const
                 }
             }
         }
+        // outgoing beyond the disc (after this step's emission or crossing): no
+        // turning point is left (no bound photon orbits outside the photon
+        // region) and nothing emits out there
+        if (y.p_r > OLIT(0.0) && y.r > u.r_out) break;
         prev = y;
         y = kerr_rk4(y, u.h_step, c);
         if (fade) {

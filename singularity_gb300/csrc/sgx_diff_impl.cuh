@@ -389,6 +389,10 @@ __global__ void __launch_bounds__(128) diff_forward_kernel(DiffConst<T> k, DiffP
                         }
                     }
                 }
+                // outgoing beyond the disc, after this step's emission or crossing: a
+                // photon outside the photon region moving out has no turning point
+                // left, and nothing emits there (starfield off)
+                if (y[3] > T(0) && y[0] > k.r_out) break;
 #pragma unroll
                 for (int i = 0; i < NS; ++i) prev[i] = y[i];
                 step_g<T, T>(prev, E, L, a, k.M, k.h, k.fade != 0u, y);
