@@ -381,6 +381,7 @@ def main() -> None:
     ap.add_argument("--no-precision-study", action="store_true")
     ap.add_argument("--no-batch-study", action="store_true")
     ap.add_argument("--no-diff-study", action="store_true")
+    ap.add_argument("--adam-steps", type=int, default=200)
     ap.add_argument("--rhs-form", type=int, default=0)
     ap.add_argument("--integrator", choices=["adaptive", "fixed"], default="adaptive")
     ap.add_argument("--precision", choices=["fp32", "mixed", "fp64"], default="fp32")
@@ -538,7 +539,7 @@ def main() -> None:
         batch = batch_study(S, N, r, torch)
     diff = None
     if not args.no_diff_study and args.precision == "fp32" and integ == N.INTEGRATOR_ADAPTIVE:
-        diff = diff_study(S, N, r, torch)
+        diff = diff_study(S, N, r, torch, adam_steps=args.adam_steps)
     cpu = None if args.no_cpu_baseline else cpu_baseline(S, O, u)
     clocks = clk.summary()
     wl = (f"kerr_a0.94_r40_i75_fov30_isco-30M_T1e4_{WIDTH}x{HEIGHT}_256spp_"
