@@ -17,8 +17,13 @@
 
 #if defined(__CUDACC__)
 #define SGX_HD __host__ __device__ __forceinline__
+// The right-hand side and its reverse pass are called four times per step;
+// one out-of-line copy each keeps the adjoint kernel inside the
+// instruction cache.
+#define SGX_HD_CALL __host__ __device__ __noinline__
 #else
 #define SGX_HD inline
+#define SGX_HD_CALL inline
 #endif
 
 namespace sgxa {
@@ -35,7 +40,7 @@ SGX_HD double hsqrt(double x) { return sqrt(x); }
 
 // The right-hand side in the shared-reciprocal algebra.
 template <class T>
-SGX_HD void rhs(const T* y, T E, T L, T a, T M, T* d) {
+SGX_HD_CALL void rhs(const T* y, T E, T L, T a, T M, T* d) {
     const T st = hsin(y[1]), ct = hcos(y[1]);
     const T r = y[0], pr = y[3], pth = y[4];
     const T a2 = a * a, s2 = st * st, c2 = ct * ct, r2 = r * r;
@@ -73,7 +78,7 @@ SGX_HD void rhs(const T* y, T E, T L, T a, T M, T* d) {
 // gy[0..4] receives the state part (gy[2] = 0: the right-hand side does not
 // depend on phi); gc[0..2] += the constants' part.
 template <class T>
-SGX_HD void rhs_vjp(const T* y, T E, T L, T a, T M, const T* w, T* gy, T* gc) {
+SGX_HD_CALL void rhs_vjp(const T* y, T E, T L, T a, T M, const T* w, T* gy, T* gc) {
     // forward intermediates
     const T th = y[1];
     const T st = hsin(th), ct = hcos(th);

@@ -483,7 +483,7 @@ __device__ __forceinline__ void step_adjoint(const T* yp, T E, T L, T a, const D
 // Adjoint: one thread per ray, a reverse sweep from the ray's last emitting
 // step to the camera, one checkpoint segment at a time.
 template <class T, bool SLAB, bool DUALJ>
-__global__ void __launch_bounds__(128) diff_backward_kernel(DiffConst<T> k, DiffParamsT<T> p, DiffBufs<T> b,
+__global__ void __launch_bounds__(128, 4) diff_backward_kernel(DiffConst<T> k, DiffParamsT<T> p, DiffBufs<T> b,
                                                             const float* __restrict__ gimg) {
     const std::uint64_t id = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (id >= b.n) return;
