@@ -44,7 +44,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 WIDTH, HEIGHT, SPP, SPP_PER_STEP = 3840, 2160, 256, 16
-# Headline integrator (BASELINE configs 2-3): error-controlled RK4, tolerance 1e-6.
+# Headline integrator: the error-controlled RK4 at tolerance 1e-6.
 METRIC = "Kerr geodesic Mrays/s at 4K x 256spp"
 # `--workload small`: the same scene at 1280x720 (profiling captures only).
 SMALL = (1280, 720)
@@ -189,7 +189,7 @@ def timed_pass(lib, N, r, u, opts, d_out, stream, torch) -> tuple[float, object]
 
 
 def precision_study(S, N, O, lib, r, u, d_out, stream, torch, main_opts) -> dict:
-    """BASELINE precision form: FP32 vs FP64 GPU forms at equal tolerance, and
+    """Precision forms: FP32 vs FP64 GPU forms at equal tolerance, and
     errors against the FP64 CPU oracle on 4096 pixels drawn with
     numpy.random.default_rng(0).choice(W*H, 4096, replace=False)."""
     out = {}
@@ -248,7 +248,7 @@ def precision_study(S, N, O, lib, r, u, d_out, stream, torch, main_opts) -> dict
 
 
 def batch_study(S, N, r, torch, launches: int = 3) -> dict:
-    """Config 4: the 64 views of workloads.batch_64_views(0) in one persistent
+    """Batched views: the 64 views of workloads.batch_64_views(0) in one persistent
     launch per batch, replayed from a CUDA graph, launch shape from the
     autotuner (timed on the views with samples capped at 4)."""
     views = S.workloads.batch_64_views(0)
@@ -276,7 +276,7 @@ def batch_study(S, N, r, torch, launches: int = 3) -> dict:
 
 
 def hdr_bloom_study(S, N, r, torch, reps: int = 3) -> dict:
-    """Config 2: Kerr a=0.94 1920x1080, 16 spp, adaptive tol 1e-6, half-float HDR,
+    """HDR + bloom: Kerr a=0.94 1920x1080, 16 spp, adaptive tol 1e-6, half-float HDR,
     bloom sigma 8 px, ACES -> RGBA8; device time of render + post-process."""
     u = S.workloads.kerr_1080p_16spp()
     opts = S.default_opts(integrator=N.INTEGRATOR_ADAPTIVE, format=N.FORMAT_RGBA16F_HDR)
@@ -304,7 +304,7 @@ def hdr_bloom_study(S, N, r, torch, reps: int = 3) -> dict:
 
 
 def diff_study(S, N, r, torch, adam_steps: int = 200, fd_eps: float = 1e-3) -> dict:
-    """Config 5: the differentiable form (emitting-slab disc, soft edges,
+    """Parameter recovery: the differentiable form (emitting-slab disc, soft edges,
     winding fade) at 512x512x4 = 1,048,576 rays; target a = 0.7, i = 60 deg,
     r_in = ISCO(0.7), T-scale 1; guess a = 0.5, i = 50 deg, r_in = 1.2 ISCO(0.5),
     T-scale 0.8; loss = mean squared image error to the FP64 target image.

@@ -24,7 +24,7 @@ def _kerr(spin, r_obs, incl_deg, fov_deg, w, h, spp, peak_T=1e4, r_out=30.0, r_i
 
 
 def schwarzschild_256():
-    """Config 1: a = 0, 256x256, 1 spp at pixel centres, fixed step h = 0.05, 4000 steps,
+    """Schwarzschild (a = 0), 256x256, 1 spp at pixel centres, fixed step h = 0.05, 4000 steps,
     r_obs = 30 M, inclination 80 deg, FOV 40 deg, disc 6-20 M, Doppler and redshift on."""
     sc = B.Scene(metric=B.MetricType.Schwarzschild, spin_a_over_M=0.0, disc_inner_M=6.0, disc_outer_M=20.0,
                  render_supersample=1, h_step=0.05, max_steps=4000)
@@ -33,17 +33,17 @@ def schwarzschild_256():
 
 
 def kerr_1080p_16spp():
-    """Config 2 scene: a = 0.94, 1920x1080, 16 spp, r_obs 40 M, i = 75 deg, FOV 30, disc ISCO-30 M, 1e4 K."""
+    """Kerr a = 0.94, 1920x1080, 16 spp, r_obs 40 M, i = 75 deg, FOV 30, disc ISCO-30 M, 1e4 K."""
     return _kerr(0.94, 40.0, 75.0, 30.0, 1920, 1080, 16)
 
 
 def kerr_4k_256spp():
-    """Config 3: config 2's scene at 3840x2160 and 256 spp."""
+    """The 1080p Kerr a = 0.94 scene at 3840x2160 and 256 spp."""
     return _kerr(0.94, 40.0, 75.0, 30.0, 3840, 2160, 256)
 
 
 def batch_64_views(seed: int = 0):
-    """Config 4: 64 square views drawn with numpy.random.default_rng(seed), per view in the
+    """64 square views drawn with numpy.random.default_rng(seed), per view in the
     order side in {128, 192, ..., 1024}, spin U[0, 0.998], inclination U[10, 89] deg,
     r_obs U[20, 60] M, spp in {1..64}; disc ISCO(a)-30 M; FOV 30 deg.
     seed 0 gives 31,272,960 pixels and 1,039,998,976 rays."""
@@ -60,12 +60,12 @@ def batch_64_views(seed: int = 0):
 
 
 def differentiation_target(w=512, h=512, spp=4):
-    """Config 5 target: a = 0.7, i = 60 deg, disc inner radius ISCO(0.7), temperature scale 1.0."""
+    """Parameter-recovery target: a = 0.7, i = 60 deg, disc inner radius ISCO(0.7), temperature scale 1.0."""
     return dict(spin=0.7, incl_deg=60.0, r_in=B.kerr_isco_prograde(1.0, 0.7), t_scale=1.0, w=w, h=h, spp=spp)
 
 
 def differentiation_guess(w=512, h=512, spp=4):
-    """Config 5 initial guess: a = 0.5, i = 50 deg, r_in = 1.2 ISCO(0.5), temperature scale 0.8."""
+    """Parameter-recovery initial guess: a = 0.5, i = 50 deg, r_in = 1.2 ISCO(0.5), temperature scale 0.8."""
     return dict(spin=0.5, incl_deg=50.0, r_in=1.2 * B.kerr_isco_prograde(1.0, 0.5), t_scale=0.8, w=w, h=h, spp=spp)
 
 

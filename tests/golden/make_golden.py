@@ -112,7 +112,7 @@ def host_cases():
     # Schwarzschild metric proper (spin 0 scene), disc 6-20, h 0.05, 4000 steps, fov 40, r 30, i 80 deg.
     sc = S.Scene(metric=S.MetricType.Schwarzschild, spin_a_over_M=0.0, disc_inner_M=6.0, disc_outer_M=20.0,
                  max_steps=4000, h_step=0.05)
-    cases.append(("schw_cfg1_small", S.pack_uniforms(sc, S.build_orbital_camera(30.0, 0.174533, 0.0, 40.0), 40, 40)))
+    cases.append(("schw_a0_fov40_small", S.pack_uniforms(sc, S.build_orbital_camera(30.0, 0.174533, 0.0, 40.0), 40, 40)))
     # Kerr 0.94, 4 spp Halton, r 40, i 75, fov 30, disc ISCO..30, T 1e4.
     isco = S.kerr_isco_prograde(1.0, 0.94)
     sc = S.Scene(spin_a_over_M=0.94, disc_inner_M=isco, disc_outer_M=30.0, disc_peak_T_K=1e4, render_supersample=4)

@@ -3,7 +3,7 @@ against its CPU specification (oracle/adaptive_oracle.hpp), through the C ABI.
 
 Tolerances: per-sample — same termination and |rel| <= 1e-3 for >= 97 % of
 samples; images — mean per-channel error <= 2e-3 of full scale.  The
-the benchmark spec precision target (FP32 vs FP64 mean per-channel error <= 1e-3) is
+precision target (FP32 vs FP64 mean per-channel error <= 1e-3) is
 checked GPU-against-GPU and GPU-against-FP64-oracle.
 """
 
