@@ -138,15 +138,16 @@ template <class T> struct DiffOut {
 // One sample of the differentiable form.  u supplies size, spp, distance
 // (|cam_pos|), FOV, aspect, mass, r_out, peak T, h, max_steps, escape radius,
 // exposure, turbulence, time and the Doppler/redshift flags.
+// The parameters enter as T, so a dual-number T carries their derivatives
+// through the whole trace (diff_pixel_grad).
 template <class T>
-inline DiffOut<T> diff_trace(const sgx_uniforms& ub, const DiffParams& dp, const DiffOpts& o, std::uint32_t gx,
-                             std::uint32_t gy, std::uint32_t s) {
+inline DiffOut<T> diff_trace_p(const sgx_uniforms& ub, T spin, T incl, T r_in_M, T t_scale, const DiffOpts& o,
+                               std::uint32_t gx, std::uint32_t gy, std::uint32_t s) {
     const Params<T> u = promote<T>(ub);
     const T Mm = u.mass_M;
-    const T a = T(dp.spin) * Mm;
-    const T incl = T(dp.incl);
-    const T r_in = T(dp.r_in) * Mm;
-    const T peak_T = u.peak_T * T(dp.t_scale);
+    const T a = spin * Mm;
+    const T r_in = r_in_M * Mm;
+    const T peak_T = u.peak_T * t_scale;
     const T eps = T(o.eps) * Mm;
     const T dcam = M<T>::sqrt(T(ub.cam_pos.x) * T(ub.cam_pos.x) + T(ub.cam_pos.y) * T(ub.cam_pos.y) +
                               T(ub.cam_pos.z) * T(ub.cam_pos.z));
@@ -263,6 +264,12 @@ inline DiffOut<T> diff_trace(const sgx_uniforms& ub, const DiffParams& dp, const
     return out;
 }
 
+template <class T>
+inline DiffOut<T> diff_trace(const sgx_uniforms& ub, const DiffParams& dp, const DiffOpts& o, std::uint32_t gx,
+                             std::uint32_t gy, std::uint32_t s) {
+    return diff_trace_p<T>(ub, T(dp.spin), T(dp.incl), T(dp.r_in), T(dp.t_scale), o, gx, gy, s);
+}
+
 // Image of the form: per pixel the mean over samples of ACES(hdr * exposure),
 // samples summed in order (geodesic_kernel.cu:482-503).
 template <class T>
@@ -276,6 +283,109 @@ inline V3<T> diff_pixel(const sgx_uniforms& ub, const DiffParams& dp, const Diff
         ldr = vadd(ldr, aces(vmul(t.hdr, exposure)));
     }
     return vmul(ldr, OLIT(1.0) / T(float(spp)));
+}
+
+// ---------------------------------------------------------------------------
+// Forward-mode dual numbers (a double and its derivatives with respect to the
+// four parameters) and their scalar traits: evaluating the form on Dual4
+// yields d(image)/d(spin, incl, r_in, t_scale) of this very code, an FP64
+// gradient independent of the GPU's adjoint sweep.
+// ---------------------------------------------------------------------------
+struct Dual4 {
+    double v;
+    double d[4];
+    Dual4() = default;
+    Dual4(double x) : v(x), d{0.0, 0.0, 0.0, 0.0} {}
+    static Dual4 var(double x, int k) {
+        Dual4 r(x);
+        r.d[k] = 1.0;
+        return r;
+    }
+    explicit operator double() const { return v; }
+};
+inline Dual4 operator+(const Dual4& a, const Dual4& b) {
+    Dual4 r(a.v + b.v);
+    for (int i = 0; i < 4; ++i) r.d[i] = a.d[i] + b.d[i];
+    return r;
+}
+inline Dual4 operator-(const Dual4& a, const Dual4& b) {
+    Dual4 r(a.v - b.v);
+    for (int i = 0; i < 4; ++i) r.d[i] = a.d[i] - b.d[i];
+    return r;
+}
+inline Dual4 operator-(const Dual4& a) {
+    Dual4 r(-a.v);
+    for (int i = 0; i < 4; ++i) r.d[i] = -a.d[i];
+    return r;
+}
+inline Dual4 operator*(const Dual4& a, const Dual4& b) {
+    Dual4 r(a.v * b.v);
+    for (int i = 0; i < 4; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+    return r;
+}
+inline Dual4 operator/(const Dual4& a, const Dual4& b) {
+    Dual4 r(a.v / b.v);
+    for (int i = 0; i < 4; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) / b.v;
+    return r;
+}
+inline bool operator<(const Dual4& a, const Dual4& b) { return a.v < b.v; }
+inline bool operator>(const Dual4& a, const Dual4& b) { return a.v > b.v; }
+inline bool operator<=(const Dual4& a, const Dual4& b) { return a.v <= b.v; }
+inline bool operator>=(const Dual4& a, const Dual4& b) { return a.v >= b.v; }
+inline Dual4 dchain(const Dual4& x, double f, double df) {
+    Dual4 r(f);
+    for (int i = 0; i < 4; ++i) r.d[i] = df * x.d[i];
+    return r;
+}
+template <> struct M<Dual4> {
+    using D = Dual4;
+    static D sqrt(const D& x) {
+        const double s = std::sqrt(x.v);
+        return dchain(x, s, s > 0.0 ? 0.5 / s : 0.0);
+    }
+    static D exp(const D& x) {
+        const double e = std::exp(x.v);
+        return dchain(x, e, e);
+    }
+    static D sin(const D& x) { return dchain(x, std::sin(x.v), std::cos(x.v)); }
+    static D cos(const D& x) { return dchain(x, std::cos(x.v), -std::sin(x.v)); }
+    static D acos(const D& x) {
+        const double q = 1.0 - x.v * x.v;
+        return dchain(x, std::acos(x.v), q > 0.0 ? -1.0 / std::sqrt(q) : 0.0);
+    }
+    static D log(const D& x) { return dchain(x, std::log(x.v), 1.0 / x.v); }
+    // x^y: d = y x^(y-1) dx + x^y log(x) dy
+    static D pow(const D& x, const D& y) {
+        const double p = std::pow(x.v, y.v);
+        D r(p);
+        for (int i = 0; i < 4; ++i)
+            r.d[i] = (x.v != 0.0 ? y.v * p / x.v : 0.0) * x.d[i] + (x.v > 0.0 ? p * std::log(x.v) : 0.0) * y.d[i];
+        return r;
+    }
+    static D fmin(const D& a, const D& b) { return b.v < a.v ? b : a; }
+    static D fmax(const D& a, const D& b) { return b.v > a.v ? b : a; }
+    static bool isfinite(const D& x) { return std::isfinite(x.v); }
+    static D lit(float, double d) { return D(d); }
+};
+
+// Pixel (gx, gy): its LDR mean and d(LDR)/d(spin, incl, r_in, t_scale).
+inline void diff_pixel_grad(const sgx_uniforms& ub, const DiffParams& dp, const DiffOpts& o, std::uint32_t gx,
+                            std::uint32_t gy, double ldr[3], double dldr[3][4]) {
+    const std::uint32_t spp = ub.supersample < 1u ? 1u : (ub.supersample > 1024u ? 1024u : ub.supersample);
+    using T = Dual4;
+    const T exposure = T(double(ub.exposure));
+    V3<T> acc = v3(T(0.0), T(0.0), T(0.0));
+    for (std::uint32_t s = 0; s < spp; ++s) {
+        const DiffOut<T> t = diff_trace_p<T>(ub, T::var(dp.spin, 0), T::var(dp.incl, 1), T::var(dp.r_in, 2),
+                                             T::var(dp.t_scale, 3), o, gx, gy, s);
+        acc = vadd(acc, aces(vmul(t.hdr, exposure)));
+    }
+    const V3<T> mean = vmul(acc, T(1.0) / T(double(float(spp))));
+    const T c[3] = {mean.x, mean.y, mean.z};
+    for (int k = 0; k < 3; ++k) {
+        ldr[k] = c[k].v;
+        for (int q = 0; q < 4; ++q) dldr[k][q] = c[k].d[q];
+    }
 }
 
 }  // namespace oracle

@@ -301,4 +301,29 @@ int oracle_diff_trace_f64(const sgx_uniforms* u, const oracle::DiffParams* p, co
     return 0;
 }
 
+// Gradient of sum_px dL/dI . I with respect to (spin, incl, r_in, t_scale),
+// I the form's LDR image, by forward-mode dual numbers over diff_trace
+// (FP64).  dLdI is H*W*3; per-pixel terms are summed in pixel order.
+int oracle_diff_grad_f64(const sgx_uniforms* u, const oracle::DiffParams* p, const oracle::DiffOpts* o,
+                         const double* dLdI, double* grad4, double* ldr3, int threads) {
+    if (u == nullptr || p == nullptr || o == nullptr || dLdI == nullptr || grad4 == nullptr) return 1;
+    const std::int64_t npix = std::int64_t(u->width) * u->height;
+    std::vector<double> part(std::size_t(npix) * 4, 0.0);
+    parallel_for(npix, threads, [&](std::int64_t i) {
+        double l[3], dl[3][4];
+        oracle::diff_pixel_grad(*u, *p, *o, std::uint32_t(i % u->width), std::uint32_t(i / u->width), l, dl);
+        for (int q = 0; q < 4; ++q)
+            part[std::size_t(i) * 4 + q] = dLdI[3 * i] * dl[0][q] + dLdI[3 * i + 1] * dl[1][q] + dLdI[3 * i + 2] * dl[2][q];
+        if (ldr3) {
+            ldr3[3 * i] = l[0];
+            ldr3[3 * i + 1] = l[1];
+            ldr3[3 * i + 2] = l[2];
+        }
+    });
+    for (int q = 0; q < 4; ++q) grad4[q] = 0.0;
+    for (std::int64_t i = 0; i < npix; ++i)
+        for (int q = 0; q < 4; ++q) grad4[q] += part[std::size_t(i) * 4 + q];
+    return 0;
+}
+
 }  // extern "C"

@@ -93,6 +93,23 @@ def diff_trace(u, params, gx, gy, s, eps: float = 0.1, fade=DIFF_FADE, model: in
     return hdr, steps, events
 
 
+def diff_grad(u, params, dLdI: np.ndarray, eps: float = 0.1, fade=DIFF_FADE, model: int = 1,
+              half_thickness: float = 0.3, tau_perp: float = 4.0, threads: int | None = None):
+    """FP64 gradient of sum(dLdI * I) w.r.t. (spin, incl, r_in, t_scale) by forward-mode dual
+    numbers through the oracle's form, and the FP64 image I."""
+    threads = threads or default_threads()
+    p = DiffParams(*[float(x) for x in params])
+    o = DiffOpts(eps, fade[0], fade[1], model, half_thickness, tau_perp, 0.0, 0.0)
+    g = np.ascontiguousarray(dLdI, dtype=np.float64)
+    assert g.shape == (u.height, u.width, 3)
+    out = np.zeros(4, dtype=np.float64)
+    img = np.zeros((u.height, u.width, 3), dtype=np.float64)
+    rc = lib().oracle_diff_grad_f64(_u(u), C.byref(p), C.byref(o), _p(g), _p(out), _p(img), C.c_int(threads))
+    if rc != 0:
+        raise RuntimeError("oracle diff grad failed")
+    return out, img
+
+
 def diff_fd_gradient(u, params, target: np.ndarray, step: float = 1e-3, eps: float = 0.1,
                      precision: str = "f64", fade=DIFF_FADE, **form) -> np.ndarray:
     """Central finite differences (step in each parameter) of mean((I - target)^2)."""

@@ -73,3 +73,21 @@ def test_crossing_model_smooth_in_radius_and_temperature(oracle):
     g2 = oracle.diff_fd_gradient(base, guess, target, step=3e-4, **form)
     for k in (2, 3):
         assert abs(g1[k] - g2[k]) <= 0.02 * abs(g1[k]), (k, g1, g2)
+
+
+def test_dual_gradient_matches_central_differences(oracle):
+    """The oracle's forward-mode gradient against its own central differences
+    (the two independent ways the oracle differentiates the form).  The bar
+    is the differences' own error: the clamps of ACES and the blackbody fit
+    are kinks, which bias a central difference by O(step) (2.4e-3 on the
+    temperature scale at this size and step)."""
+    import singularity_gb300 as S
+    W = S.workloads
+    base = _scene(S, 48, 32, 2)
+    target = oracle.diff_render(base, W.differentiation_params(W.differentiation_target()))
+    guess = W.differentiation_params(W.differentiation_guess())
+    img = oracle.diff_render(base, guess)
+    g, img2 = oracle.diff_grad(base, guess, 2.0 * (img - target) / img.size)
+    np.testing.assert_array_equal(img2, img)
+    fd = oracle.diff_fd_gradient(base, guess, target, step=3e-4)
+    assert np.all(np.abs(g - fd) <= 3e-3 * np.abs(fd)), (g, fd)
