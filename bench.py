@@ -247,17 +247,24 @@ def precision_study(S, N, O, lib, r, u, d_out, stream, torch, main_opts) -> dict
     return out
 
 
-def batch_study(S, N, r, torch, launches: int = 3) -> dict:
+def batch_study(S, N, r, torch, launches: int = 3, rank: int = 0, world: int = 1) -> dict:
     """Batched views: the 64 views of workloads.batch_64_views(0) in one persistent
     launch per batch, replayed from a CUDA graph, launch shape from the
-    autotuner (timed on the views with samples capped at 4)."""
-    views = S.workloads.batch_64_views(0)
+    autotuner (timed on the views with samples capped at 4).  Under N ranks
+    the views are split by cost (singularity_gb300.dist.split_by_cost) and the
+    rate is all ranks' rays over the slowest rank's time."""
+    from singularity_gb300 import dist as D
+    views_all = S.workloads.batch_64_views(0)
+    parts = D.split_by_cost([D.view_cost(v.width, v.height, v.supersample) for v in views_all], world)
+    views = [views_all[i] for i in parts[rank]]
     rays = sum(v.width * v.height * v.supersample for v in views)
     base = S.default_opts(integrator=N.INTEGRATOR_ADAPTIVE)
     t0 = time.perf_counter()
     best, tune_ms = S.autotune(r, views, base, sample_cap=4)
     tune_s = time.perf_counter() - t0
-    out = {"views": len(views), "pixels": sum(v.width * v.height for v in views), "rays": rays,
+    out = {"views": len(views_all), "views_this_rank": len(views),
+           "pixels": sum(v.width * v.height for v in views_all),
+           "rays": sum(v.width * v.height * v.supersample for v in views_all),
            "autotune": {"block_threads": best.block_threads, "refill_interval": best.refill_interval,
                         "tile": [best.tile_w, best.tile_h], "probe_ms": tune_ms, "wall_s": tune_s}}
     for name, opts in (("autotuned", best), ("default", base)):
@@ -269,8 +276,8 @@ def batch_study(S, N, r, torch, launches: int = 3) -> dict:
             b.launch()
             ms.append(b.wait().total_ms)
         b.close()
-        out[f"{name}_ms_per_batch"] = float(np.median(ms))
-        out[f"{name}_mrays_s"] = rays / (np.median(ms) / 1e3) / 1e6
+        out[f"{name}_ms_per_batch"] = D.max_over_ranks(float(np.median(ms)), "cuda")
+        out[f"{name}_mrays_s"] = D.whole_job_rate(rays, float(np.median(ms)) / 1e3, "cuda") / 1e6
     out["note"] = "one graph replay renders all 64 views (every sample); adaptive FP32, tol 1e-6; device time"
     return out
 
@@ -412,7 +419,8 @@ def main() -> None:
     lib = N.load()
     # Weak scaling: each rank renders its own view (camera azimuth offset per rank).
     isco = S.kerr_isco_prograde(1.0, 0.94)
-    cam = S.build_orbital_camera(40.0, 0.261799, 2 * np.pi * rank / world, 30.0)
+    from singularity_gb300 import dist as D
+    cam = S.build_orbital_camera(40.0, 0.261799, D.view_azimuth(rank, world), 30.0)
     u = S.pack_uniforms(S.Scene(spin_a_over_M=0.94, disc_inner_M=isco, disc_outer_M=30.0, disc_peak_T_K=1e4,
                                 render_supersample=SPP), cam, WIDTH, HEIGHT, 0.0)
     npix = u.width * u.height
@@ -458,12 +466,8 @@ def main() -> None:
         torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
-    ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    rays_total = stats_acc["rays"] * world
+    ms = D.max_over_ranks(ev0.elapsed_time(ev1), "cuda")
+    rays_total = D.sum_over_ranks(stats_acc["rays"], "cuda")
     value = rays_total / (ms / 1e3) / 1e6
 
     # --- e2e through the public API with host buffers ---
@@ -487,15 +491,16 @@ def main() -> None:
         t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
             e2e_step()
-        dt = time.perf_counter() - t0
-        if world > 1:
-            t = torch.tensor([dt], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            dt = float(t.item())
+        dt = D.max_over_ranks(time.perf_counter() - t0, "cuda")
         e2e = {"value": npix * SPP_PER_STEP * args.e2e_steps * world / dt / 1e6, "unit": "Mrays/s",
                "h2d_bytes_per_step": C.sizeof(N.Uniforms), "d2h_bytes_per_step": npix * 4,
                "note": "per step sgx_render (a full 16-spp frame) + sgx_capture RGBA8 into pinned host memory, "
                        "wall clock"}
+
+    # the batch shards its views across ranks: every rank takes part
+    batch = None
+    if not args.no_batch_study and args.precision == "fp32" and integ == N.INTEGRATOR_ADAPTIVE:
+        batch = batch_study(S, N, r, torch, rank=rank, world=world)
 
     if rank != 0:
         if world > 1:
@@ -528,19 +533,20 @@ def main() -> None:
             "cpu_oracle_steps_per_ray": mean_steps_cpu,
             "ops_rule": "reference formulas, add/sub/mul/div/sqrt/min/max/transcendental = 1 each"}
 
+    # single-GPU properties (precision forms, HDR post-process, adjoint, CPU
+    # baseline) are measured at N = 1 only; under N ranks only the sharded
+    # batch runs, so the timed work stays short while N GPUs are held
+    single = world == 1
     study = None
-    if not args.no_precision_study and args.precision == "fp32" and integ == N.INTEGRATOR_ADAPTIVE:
+    if single and not args.no_precision_study and args.precision == "fp32" and integ == N.INTEGRATOR_ADAPTIVE:
         study = precision_study(S, N, O, lib, r, u, d_out, stream, torch, opts)
     hdr = None
-    if not args.no_batch_study and args.precision == "fp32" and integ == N.INTEGRATOR_ADAPTIVE:
+    if single and not args.no_batch_study and args.precision == "fp32" and integ == N.INTEGRATOR_ADAPTIVE:
         hdr = hdr_bloom_study(S, N, r, torch)
-    batch = None
-    if not args.no_batch_study and args.precision == "fp32" and integ == N.INTEGRATOR_ADAPTIVE:
-        batch = batch_study(S, N, r, torch)
     diff = None
-    if not args.no_diff_study and args.precision == "fp32" and integ == N.INTEGRATOR_ADAPTIVE:
+    if single and not args.no_diff_study and args.precision == "fp32" and integ == N.INTEGRATOR_ADAPTIVE:
         diff = diff_study(S, N, r, torch, adam_steps=args.adam_steps)
-    cpu = None if args.no_cpu_baseline else cpu_baseline(S, O, u)
+    cpu = None if (args.no_cpu_baseline or rank != 0 or not single) else cpu_baseline(S, O, u)
     clocks = clk.summary()
     wl = (f"kerr_a0.94_r40_i75_fov30_isco-30M_T1e4_{WIDTH}x{HEIGHT}_256spp_"
           + ("adaptive_tol1e-6" if integ == N.INTEGRATOR_ADAPTIVE else "fixed_h0.4_max2500") + f"_{args.precision}")
