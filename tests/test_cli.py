@@ -126,3 +126,20 @@ def test_cli_extensions(cli, tmp_path):
     srgb = np.where(f <= 0.0031308, 12.92 * f, 1.055 * np.power(np.clip(f, 0, 1), 1 / 2.4) - 0.055)
     u8 = np.clip(srgb * 255 + 0.5, 0, 255).astype(np.uint8)
     assert np.abs(u8.astype(int) - img[..., :3].astype(int)).max() <= 1
+
+
+@pytest.mark.gpu
+def test_cli_adaptive_step_flag(cli, tmp_path, sgx, oracle):
+    """--adaptive-step packs SGX_FLAG_ADAPTIVE_STEP (the radius-adaptive step of
+    geodesic_math.h:91-96); the CLI's image matches the oracle with that flag."""
+    scene = tmp_path / "s.scene"
+    scene.write_text("mass = 1.0\nspin = 0.0\ndisc_r_inner = 6.0\ndisc_r_outer = 20.0\n")
+    r = run(cli, "--output", tmp_path / "a.png", "--res", "64x48", "--scene", scene, "--adaptive-step")
+    assert r.returncode == 0, r.stderr
+    img = read_png(tmp_path / "a.png")
+    sc = sgx.Scene(metric=sgx.MetricType.Schwarzschild, spin_a_over_M=0.0, disc_inner_M=6.0, disc_outer_M=20.0,
+                   adaptive_step_on=True)
+    u = sgx.pack_uniforms(sc, sgx.build_orbital_camera(30.0, 0.15, 0.0, 60.0), 64, 48)
+    ref, _ = oracle.render(u)
+    d = np.abs(img[..., :3].astype(int) - ref[..., :3].astype(int))
+    assert d.mean() <= 0.5 and (d.max(axis=-1) <= 1).mean() >= 0.97
