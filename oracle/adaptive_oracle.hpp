@@ -67,20 +67,23 @@ struct RayDiag {
 
 // Radius of the unstable spherical photon orbit whose xi = L/E equals the
 // ray's (Bardeen 1973; Teo 2003: xi(r) = [r^2 (3M - r) - a^2 (r + M)] / [a (r - M)]),
-// by 24 bisections in T inside [r_ph,prograde, r_ph,retrograde]; 3M for a = 0;
+// by 12 bisections in T inside [r_ph,prograde, r_ph,retrograde]; 3M for a = 0;
 // NaN when xi is outside the photon region's range.
 template <class T> inline T photon_orbit_radius(T a, T Mm, T xi) {
     if (!(a > OLIT(1e-7)) && !(a < OLIT(-1e-7))) return OLIT(3.0) * Mm;
-    auto xi_of = [&](T r) { return (r * r * (OLIT(3.0) * Mm - r) - a * a * (r + Mm)) / (a * (r - Mm)); };
+    // sign of xi(r) - xi, xi(r) = (r^2 (3M - r) - a^2 (r + M)) / (a (r - M)), without
+    // the division by a (r - M) (> 0 for a > 0, r > M; the sign flips for a < 0)
+    const T sg = a > OLIT(0.0) ? OLIT(1.0) : OLIT(-1.0);
+    auto g = [&](T r) { return sg * ((r * r * (OLIT(3.0) * Mm - r) - a * a * (r + Mm)) - xi * a * (r - Mm)); };
     T lo = OLIT(2.0) * Mm * (OLIT(1.0) + M<T>::cos(OLIT(2.0) / OLIT(3.0) * M<T>::acos(-a / Mm)));
     T hi = OLIT(2.0) * Mm * (OLIT(1.0) + M<T>::cos(OLIT(2.0) / OLIT(3.0) * M<T>::acos(a / Mm)));
-    const T flo = xi_of(lo) - xi, fhi = xi_of(hi) - xi;
+    const T flo = g(lo), fhi = g(hi);
     if (!(flo * fhi <= OLIT(0.0))) return T(NAN);
     const bool lo_neg = flo <= OLIT(0.0);
-    for (int i = 0; i < 24; ++i) {
+    // 12 halvings of [r_pro, r_ret] (< 3M): r_c to 1e-3 M, ample for a 0.05 M band
+    for (int i = 0; i < 12; ++i) {
         const T mid = OLIT(0.5) * (lo + hi);
-        const T fm = xi_of(mid) - xi;
-        if ((fm <= OLIT(0.0)) == lo_neg) lo = mid;
+        if ((g(mid) <= OLIT(0.0)) == lo_neg) lo = mid;
         else hi = mid;
     }
     return OLIT(0.5) * (lo + hi);
@@ -262,9 +265,10 @@ inline TraceOut<T> trace_kerr_adaptive(const CamRay<T>& cam, const Params<T>& u,
         bool accept;
         if (in_zone) {
             ++zone_steps;
+            // the error measured in FP64, the step factor (a heuristic) in T
             const double e = error_norm<double>(y, at, o.tol);
             accept = e <= 1.0;
-            h = T(float(double(float(h)) * step_factor<double>(e)));
+            h = h * step_factor<T>(T(float(e)));
         } else {
             const T e = error_norm<T>(y, at, o.tol);
             accept = e <= OLIT(1.0);

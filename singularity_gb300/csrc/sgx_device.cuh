@@ -111,6 +111,9 @@ template <class T> struct View {
     T r_ph_pro, r_ph_ret; // equatorial prograde / retrograde photon orbits
     // Kerr metric at the camera (geodesic_kernel.cu:310-319)
     T g_tt, g_tp, g_rr, g_thth, g_pp, s2_c;
+    // the same in FP64 (from the T camera values) for the mixed form's FP64
+    // constants of motion, and 1 / (2 g_tt)
+    double g_tt_d, g_tp_d, g_rr_d, g_thth_d, g_pp_d, inv_2gtt_d;
     std::uint32_t width, height, flags, max_steps, spp, metric;
 };
 
@@ -166,6 +169,16 @@ template <class T> __device__ inline View<T> make_view(const sgx_uniforms& u) {
     v.g_rr = Sigma_c / Delta_c;
     v.g_thth = Sigma_c;
     v.g_pp = v.s2_c * ((r * r + a * a) * (r * r + a * a) - a * a * Delta_c * v.s2_c) / Sigma_c;
+    {
+        const double Md = v.M, ad = v.a, rd = v.cam_r, ct = v.cos_th, st = v.sin_th;
+        const double Sg = rd * rd + ad * ad * ct * ct, Dl = rd * rd - 2.0 * Md * rd + ad * ad, s2 = st * st;
+        v.g_tt_d = -(1.0 - 2.0 * Md * rd / Sg);
+        v.g_tp_d = -2.0 * Md * rd * ad * s2 / Sg;
+        v.g_rr_d = Sg / Dl;
+        v.g_thth_d = Sg;
+        v.g_pp_d = s2 * ((rd * rd + ad * ad) * (rd * rd + ad * ad) - ad * ad * Dl * s2) / Sg;
+        v.inv_2gtt_d = 1.0 / (2.0 * v.g_tt_d);
+    }
     if (v.metric == SGX_METRIC_KERR) {
         v.hcut = DLIT(1.02) * (Mm + DM<T>::sqrt_(DM<T>::fmax_(Mm * Mm - a * a, DLIT(0.0))));
     } else {
@@ -578,21 +591,16 @@ __device__ __forceinline__ bool kerr_init(const View<T>& v, const CamDir<T>& cd,
 // FP64 constants of motion from the FP32 camera direction (mixed form).
 __device__ __forceinline__ bool kerr_init_fp64_constants(const View<float>& v, const CamDir<float>& cd, double& E,
                                                          double& L, double& pr, double& pth) {
-    const double Mm = v.M, a = v.a, r = v.cam_r, ct = v.cos_th, st = v.sin_th;
-    const double Sigma = r * r + a * a * ct * ct, Delta = r * r - 2.0 * Mm * r + a * a, s2 = st * st;
-    const double g_tt = -(1.0 - 2.0 * Mm * r / Sigma);
-    const double g_tp = -2.0 * Mm * r * a * s2 / Sigma;
-    const double g_rr = Sigma / Delta, g_thth = Sigma;
-    const double g_pp = s2 * ((r * r + a * a) * (r * r + a * a) - a * a * Delta * s2) / Sigma;
+    // the metric at the camera is per view (View::*_d); per ray one FP64 sqrt
     const double ur = cd.ur, uth = cd.utheta, uph = cd.uphi;
-    const double B = 2.0 * g_tp * uph, C = g_rr * ur * ur + g_thth * uth * uth + g_pp * uph * uph;
-    const double disc = B * B - 4.0 * g_tt * C;
+    const double B = 2.0 * v.g_tp_d * uph, C = v.g_rr_d * ur * ur + v.g_thth_d * uth * uth + v.g_pp_d * uph * uph;
+    const double disc = B * B - 4.0 * v.g_tt_d * C;
     if (disc < 0.0) return false;
-    const double ut = (-B - sqrt(disc)) / (2.0 * g_tt);
-    E = -(g_tt * ut + g_tp * uph);
-    L = g_tp * ut + g_pp * uph;
-    pr = g_rr * ur;
-    pth = g_thth * uth;
+    const double ut = (-B - sqrt(disc)) * v.inv_2gtt_d;
+    E = -(v.g_tt_d * ut + v.g_tp_d * uph);
+    L = v.g_tp_d * ut + v.g_pp_d * uph;
+    pr = v.g_rr_d * ur;
+    pth = v.g_thth_d * uth;
     return true;
 }
 
@@ -797,23 +805,51 @@ template <class T> __device__ __forceinline__ T crossing_fraction(T th0, T th1, 
 }
 
 // Spherical photon orbit with the ray's xi = L/E (Bardeen 1973, Teo 2003):
-// 24 bisections inside [r_ph,pro, r_ph,ret]; 3M for a = 0; NaN outside.
+// 12 bisections inside [r_ph,pro, r_ph,ret]; 3M for a = 0; NaN outside.
 template <class T> __device__ __forceinline__ T photon_orbit_radius(const View<T>& v, T xi) {
     const T a = v.a, Mm = v.M;
     if (!(a > DLIT(1e-7)) && !(a < DLIT(-1e-7))) return DLIT(3.0) * Mm;
-    auto xi_of = [&](T r) { return (r * r * (DLIT(3.0) * Mm - r) - a * a * (r + Mm)) / (a * (r - Mm)); };
+    // sign of xi(r) - xi without the division by a (r - M) > 0 (a > 0; flipped for a < 0)
+    const T sg = a > DLIT(0.0) ? DLIT(1.0) : DLIT(-1.0);
+    auto g = [&](T r) { return sg * ((r * r * (DLIT(3.0) * Mm - r) - a * a * (r + Mm)) - xi * a * (r - Mm)); };
     T lo = v.r_ph_pro, hi = v.r_ph_ret;
-    const T flo = xi_of(lo) - xi, fhi = xi_of(hi) - xi;
+    const T flo = g(lo), fhi = g(hi);
     if (!(flo * fhi <= DLIT(0.0))) return T(NAN);
     const bool lo_neg = flo <= DLIT(0.0);
 #pragma unroll 1
-    for (int i = 0; i < 24; ++i) {
+    for (int i = 0; i < 12; ++i) {
         const T mid = DLIT(0.5) * (lo + hi);
-        const T fm = xi_of(mid) - xi;
-        if ((fm <= DLIT(0.0)) == lo_neg) lo = mid;
+        if ((g(mid) <= DLIT(0.0)) == lo_neg) lo = mid;
         else hi = mid;
     }
     return DLIT(0.5) * (lo + hi);
+}
+
+// The mixed form's FP64 error norm with a single division: the component of
+// largest |h/6 (k4 - k5)| / (tol (1 + max(|y|, |y4|))) is found by
+// cross-multiplied comparisons, then divided once (the value equals the max
+// of the ratios up to the choice among ratios equal to rounding).
+template <class T>
+__device__ __forceinline__ double error_norm_fp64_1div(const KS<T>& y, const KAttempt<T>& a, float tol_f) {
+    const double tol = tol_f, h6 = a.h6;
+    double num = 0.0, den = 1.0;
+    auto one = [&](T yv, T y4v, T k4v, T k5v) {
+        const double ya = fabs(double(yv)), yb = fabs(double(y4v));
+        const double sc = tol * (1.0 + (ya > yb ? ya : yb));
+        const double n = fabs(h6 * (double(k4v) - double(k5v)));
+        if (n * den > num * sc) {
+            num = n;
+            den = sc;
+        }
+    };
+    one(y.r, a.y4.r, a.k4.r, a.k5.r);
+    one(y.th, a.y4.th, a.k4.th, a.k5.th);
+    one(y.ph, a.y4.ph, a.k4.ph, a.k5.ph);
+    one(y.pr, a.y4.pr, a.k4.pr, a.k5.pr);
+    one(y.pth, a.y4.pth, a.k4.pth, a.k5.pth);
+    double e = num / den;
+    if (!(e <= 1e30)) e = 1e30;
+    return e;
 }
 
 }  // namespace sgxd

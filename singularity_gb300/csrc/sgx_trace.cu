@@ -255,9 +255,9 @@ template <class T, int FL> struct KerrAdaptive {
         }
         if (in_zone) {
             ++zone;
-            const double e = error_norm<double>(y, at, pass.tol);
+            const double e = error_norm_fp64_1div(y, at, pass.tol);
             accept = e <= 1.0;
-            h = T(float(double(float(h)) * step_factor<double>(e)));
+            h = h * step_factor_fast(float(e));
         } else if constexpr (FAST && std::is_same_v<T, float>) {
             const T e = error_norm_fast<T>(y, at, pass.tol);
             accept = e <= DLIT(1.0);

@@ -84,7 +84,9 @@ def test_fewer_steps_than_reference_fixed_step(oracle, sgx):
 
 
 def test_photon_orbit_radius_known_answers(oracle):
-    """xi(r) round trip and the a = 0 limit (3M); prograde/retrograde ends."""
+    """xi(r) round trip and the a = 0 limit (3M); prograde/retrograde ends.
+    12 halvings of [r_pro, r_ret] (< 3M wide) resolve r_c to 3.7e-4 M, well
+    inside the 0.05 M band the mixed form needs."""
     import ctypes as C
     L = oracle.lib()
     L.oracle_photon_orbit_radius.restype = C.c_double
@@ -93,7 +95,7 @@ def test_photon_orbit_radius_known_answers(oracle):
     a = 0.94
     for r in (1.6, 2.0, 2.8, 3.5):
         xi = (r * r * (3 - r) - a * a * (r + 1)) / (a * (r - 1))
-        assert L.oracle_photon_orbit_radius(a, 1.0, xi) == pytest.approx(r, abs=1e-5)
+        assert L.oracle_photon_orbit_radius(a, 1.0, xi) == pytest.approx(r, abs=4e-4)
     assert np.isnan(L.oracle_photon_orbit_radius(a, 1.0, 100.0))
 
 
