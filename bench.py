@@ -241,9 +241,13 @@ def precision_study(S, N, O, lib, r, u, d_out, stream, torch, main_opts) -> dict
         dq = np.array([abs(x.Q_end - x.Q0) / x.norm_Q for x in d])[ok]
         out[f"carter_drift_{key}"] = {"median": float(np.median(dq)), "mean": float(dq.mean()),
                                       "p99": float(np.percentile(dq, 99)), "max": float(dq.max())}
+        dh = np.array([abs(x.H2_end) / max(1e-30, x.E * x.E) for x in d])[ok]
+        out[f"null_condition_drift_{key}"] = {"median": float(np.median(dh)), "mean": float(dh.mean()),
+                                              "p99": float(np.percentile(dh, 99)), "max": float(dh.max())}
     out["note"] = ("speeds: one 16-spp 4K pass each; errors: full 256-spp frame, RGBA32F LDR mean, units of "
-                   "full scale; Carter drift |Q_end-Q0|/(|Q0|+L^2+a^2E^2) from the CPU oracle of the same "
-                   "integrator")
+                   "full scale; Carter drift |Q_end-Q0|/(|Q0|+L^2+a^2E^2) and null-condition drift |2H_end|/E^2 "
+                   "from the CPU oracle of the same integrator; E and L_z are constants of the Hamiltonian form "
+                   "(held exactly, zero drift by construction)")
     return out
 
 
