@@ -4,9 +4,17 @@ Workload (the headline of the reference's own benchmarks, and the scene of
 its 4K x 256 spp Kerr claim): Kerr a/M = 0.94, 3840x2160, 256 samples per
 pixel with Halton(2,3) jitter, observer at r = 40 M, inclination 75 deg
 (elevation 0.261799 rad), vertical FOV 30 deg, disc from the prograde ISCO to
-30 M, peak temperature 1e4 K, reference defaults otherwise.  One bench step is
-one progressive pass of 16 samples per pixel over the full frame
-(132,710,400 rays); 16 steps make the 256-spp frame.
+30 M, peak temperature 1e4 K, reference defaults otherwise.  Integrated in
+the precision form: the error-controlled Kerr RK4 at tolerance 1e-6 in FP32,
+with the constants of motion and the step control within 0.05 M of the
+photon orbit or the horizon in FP64 (`--precision fp32 | fp64` for the other
+forms).  One bench step is one progressive pass of 16 samples per pixel over
+the full frame (132,710,400 rays); 16 steps make the 256-spp frame.
+
+Studies in the same line (N = 1): precision forms (FP32 / mixed / FP64 speed,
+errors against the FP64 CPU oracle, Carter and null-condition drift), 64
+batched views in a CUDA graph, 1080p HDR + bloom, and the adjoint at
+512x512x4 (grad/s, central differences, FP64 gradient, 200 Adam steps).
 
   value   Mrays/s, device time (CUDA events on the launching stream) over the
           K timed steps, inputs resident; max over ranks.
@@ -401,7 +409,9 @@ def main() -> None:
     ap.add_argument("--adam-steps", type=int, default=200)
     ap.add_argument("--rhs-form", type=int, default=0)
     ap.add_argument("--integrator", choices=["adaptive", "fixed"], default="adaptive")
-    ap.add_argument("--precision", choices=["fp32", "mixed", "fp64"], default="fp32")
+    # the precision form: FP32 bulk with FP64 constants of motion and FP64 step
+    # control within 0.05 M of the photon orbit or the horizon
+    ap.add_argument("--precision", choices=["fp32", "mixed", "fp64"], default="mixed")
     ap.add_argument("--workload", choices=["4k", "small"], default="4k")
     args = ap.parse_args()
     if args.workload == "small":
@@ -509,7 +519,7 @@ def main() -> None:
 
     # the batch shards its views across ranks: every rank takes part
     batch = None
-    if not args.no_batch_study and args.precision == "fp32" and integ == N.INTEGRATOR_ADAPTIVE:
+    if not args.no_batch_study and args.precision != "fp64" and integ == N.INTEGRATOR_ADAPTIVE:
         batch = batch_study(S, N, r, torch, rank=rank, world=world)
 
     if rank != 0:
@@ -521,6 +531,8 @@ def main() -> None:
     from oracle import pyoracle as O
     O.build(ref=False)
     ad = O.adaptive_opts() if integ == N.INTEGRATOR_ADAPTIVE else None
+    if ad is not None and args.precision == "mixed":
+        ad = O.adaptive_opts(mixed=True)
     ops_step, mean_steps_cpu = ops_per_step(S, O, u, adaptive=ad)
     trace_ms = np.array(stats_acc["trace_ms"])
     per_launch_ms = float(trace_ms.mean())
@@ -549,13 +561,13 @@ def main() -> None:
     # batch runs, so the timed work stays short while N GPUs are held
     single = world == 1
     study = None
-    if single and not args.no_precision_study and args.precision == "fp32" and integ == N.INTEGRATOR_ADAPTIVE:
+    if single and not args.no_precision_study and args.precision != "fp64" and integ == N.INTEGRATOR_ADAPTIVE:
         study = precision_study(S, N, O, lib, r, u, d_out, stream, torch, opts)
     hdr = None
-    if single and not args.no_batch_study and args.precision == "fp32" and integ == N.INTEGRATOR_ADAPTIVE:
+    if single and not args.no_batch_study and args.precision != "fp64" and integ == N.INTEGRATOR_ADAPTIVE:
         hdr = hdr_bloom_study(S, N, r, torch)
     diff = None
-    if single and not args.no_diff_study and args.precision == "fp32" and integ == N.INTEGRATOR_ADAPTIVE:
+    if single and not args.no_diff_study and args.precision != "fp64" and integ == N.INTEGRATOR_ADAPTIVE:
         diff = diff_study(S, N, r, torch, adam_steps=args.adam_steps)
     cpu = None if (args.no_cpu_baseline or rank != 0 or not single) else cpu_baseline(S, O, u)
     clocks = clk.summary()
