@@ -401,9 +401,15 @@ enum : int { MODE_IDLE = 0, MODE_ACTIVE = 1, MODE_DONE = 2 };
 // The persistent tracer over a set of views.  Ray ids enumerate, view by
 // view, tiles of tile_w x tile_h pixels (padded to whole tiles), the pixels
 // of a tile row-major, and a pixel's samples innermost; ids that land in the
-// padding carry no work.
+// padding carry no work.  FP32 variants are held to 64 registers (4 blocks of
+// 256 per SM): the precision form would otherwise take 80 and 3 blocks for
+// its few FP64 temporaries (1.5 % faster capped); FP64 variants keep their
+// registers (capped they spill up to 1.4 KB).
+template <class T> struct TraceMinBlocks {
+    static constexpr int value = sizeof(T) == 4 ? 4 : 1;
+};
 template <class T, class Ray>
-__global__ void __launch_bounds__(256) trace_persistent(PassDesc pass) {
+__global__ void __launch_bounds__(256, TraceMinBlocks<T>::value) trace_persistent(PassDesc pass) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const ViewSet& vs = pass.vs;
     const SmemSet<T> m = carve<T>(smem_raw, vs.n, vs.max_S);
