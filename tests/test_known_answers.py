@@ -11,12 +11,17 @@ thresholds:
   orbit, equatorial symmetry, photon sphere, bounded non-equatorial orbit,
   20000-step stress, 2H along a long geodesic, analytic partials vs finite
   differences at 5e-3, repulsive polar barrier);
-* equatorial crossing, tests/test_disc_intersection.cpp:20-95.
+* equatorial crossing, tests/test_disc_intersection.cpp:20-95;
+* Kerr geometry on the path, verification/test_kerr_geometry.py:95-228 (the
+  prograde ISCO as the circular-orbit energy minimum, the equatorial photon
+  orbits, the mixed form's spherical photon orbit radius).
 """
 
 from __future__ import annotations
 
 import math
+
+import pytest
 
 import numpy as np
 
@@ -250,3 +255,51 @@ def test_crossing_detection_and_fraction(oracle):
     x, f = oracle.crossing(hp - F(0.15), hp + F(0.05))
     r_cross = F(12.4) + F(f) * (F(11.9) - F(12.4))
     assert x and 11.9 <= r_cross <= 12.4 and abs(r_cross - 12.025) <= 1e-5
+
+
+# --- Kerr geometry used on the path (verification/test_kerr_geometry.py:95-228):
+#     the prograde ISCO (disc inner edge), the equatorial photon orbits (the
+#     mixed form's band, the differentiable form's capture radius) ----------
+
+def _circular_energy(r, a, M=1.0):
+    # specific energy of a prograde circular equatorial orbit (Bardeen, Press & Teukolsky 1972)
+    v = math.sqrt(M / r)
+    return (1 - 2 * v * v + a * v ** 3) / math.sqrt(1 - 3 * v * v + 2 * a * v ** 3)
+
+
+def test_isco_is_the_circular_orbit_energy_minimum():
+    from scipy.optimize import brentq
+    import singularity_gb300 as S
+    for a in (0.0, 0.5, 0.94, 0.998):
+        dE = lambda r: (_circular_energy(r + 1e-6, a) - _circular_energy(r - 1e-6, a)) / 2e-6
+        r_pro = 2 * (1 + math.cos(2 / 3 * math.acos(-a)))  # circular orbits exist outside it
+        r_min = brentq(dE, r_pro + 1e-3, 9.0)
+        got = S.kerr_isco_prograde(1.0, a)
+        assert got == pytest.approx(r_min, rel=3e-4), (a, got, r_min)
+    assert S.kerr_isco_prograde(1.0, 0.0) == pytest.approx(6.0, rel=3e-4)
+
+
+def test_equatorial_photon_orbits_close():
+    """The prograde / retrograde circular photon orbit radii 2M(1 + cos(2/3 acos(-+a/M)))
+    satisfy r^(3/2) - 3M r^(1/2) +- 2 a M^(1/2) = 0; a = 0 gives 3M."""
+    for a in (0.0, 0.5, 0.94, 0.998):
+        r_pro = 2 * (1 + math.cos(2 / 3 * math.acos(-a)))
+        r_ret = 2 * (1 + math.cos(2 / 3 * math.acos(a)))
+        assert abs(r_pro ** 1.5 - 3 * r_pro ** 0.5 + 2 * a) < 1e-9
+        assert abs(r_ret ** 1.5 - 3 * r_ret ** 0.5 - 2 * a) < 1e-9
+    assert 2 * (1 + math.cos(2 / 3 * math.acos(0.0))) == pytest.approx(3.0)
+
+
+def test_photon_orbit_radius_spans_the_photon_region(oracle):
+    """The mixed form's r_c(xi): across the photon region it returns the
+    spherical orbit of that xi (the equatorial orbits bound the region)."""
+    import ctypes as C
+    L = oracle.lib()
+    L.oracle_photon_orbit_radius.restype = C.c_double
+    L.oracle_photon_orbit_radius.argtypes = [C.c_double, C.c_double, C.c_double]
+    a = 0.5
+    xi = lambda r: (r * r * (3 - r) - a * a * (r + 1)) / (a * (r - 1))
+    r_pro = 2 * (1 + math.cos(2 / 3 * math.acos(-a)))
+    r_ret = 2 * (1 + math.cos(2 / 3 * math.acos(a)))
+    for r in np.linspace(r_pro, r_ret, 9)[1:-1]:
+        assert L.oracle_photon_orbit_radius(a, 1.0, xi(r)) == pytest.approx(r, abs=4e-4)
