@@ -1,0 +1,85 @@
+"""Our kernels against the reference's own CUDA kernel on the same GB300.
+
+The reference kernel (render/cuda/kernels/geodesic_kernel.cu, compiled to PTX
+from the reference tree by `make -C oracle ref`) is launched the way
+CudaBackend::render_frame launches it (oracle/ref_gpu.py).  Parity: the same
+RGBA8 frame on the pinned scenes, within the bar of test_gpu_parity.py (both
+are FP32 CUDA; the few differing pixels are photon-ring rays where the two
+compilations' FMA contractions diverge).  Speed: the reference's
+one-thread-per-pixel fixed-step kernel against our fixed-step kernel and our
+precision form on the same scene, printed (and ours required faster)."""
+
+from __future__ import annotations
+
+import time
+
+import numpy as np
+import pytest
+
+from conftest import uniforms_from_bytes
+from imgmetrics import channel_error
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def refk(sgx, renderer):
+    from oracle import ref_gpu
+    if not ref_gpu.available():
+        pytest.skip("reference kernel PTX not built (make -C oracle ref needs the reference tree)")
+    import torch
+    torch.zeros(1, device="cuda")  # the primary context current on this thread
+    k = ref_gpu.RefKernel()
+    yield k
+    k.close()
+
+
+def _ref_frame(refk, u):
+    import torch
+    out = torch.zeros(u.width * u.height * 4, dtype=torch.uint8, device="cuda")
+    refk.launch(out.data_ptr(), u)
+    torch.cuda.synchronize()
+    return out.cpu().numpy().reshape(u.height, u.width, 4)
+
+
+@pytest.mark.parametrize("rhs_form", [0, 1])
+def test_matches_reference_cuda_kernel(renderer, sgx, host_vectors, refk, rhs_form):
+    z, names = host_vectors
+    for name in names:
+        u = uniforms_from_bytes(z[f"{name}_uniforms"])
+        ref = _ref_frame(refk, u)
+        img = renderer.render_image(u, sgx.default_opts(rhs_form=rhs_form))
+        e = channel_error(img, ref)
+        exact = float((img == ref).all(axis=-1).mean())
+        print(f"{name} rhs_form={rhs_form}: exact pixels {exact:.4f} {e}")
+        assert e["mean"] <= 2e-3 and e["le1_frac"] >= 0.97, (name, e)
+        np.testing.assert_array_equal(ref, _ref_frame(refk, u))  # the reference kernel is deterministic
+
+
+def test_faster_than_reference_cuda_kernel(renderer, sgx, refk):
+    import torch
+    N = sgx._native
+    u = sgx.workloads.kerr_1080p_16spp()
+    rays = u.width * u.height * u.supersample
+    out = torch.zeros(u.width * u.height * 4, dtype=torch.uint8, device="cuda")
+    refk.launch(out.data_ptr(), u)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(2):
+        refk.launch(out.data_ptr(), u)
+    torch.cuda.synchronize()
+    t_ref = (time.perf_counter() - t0) / 2
+    res = {}
+    for name, opts in (("fixed", sgx.default_opts()),
+                       ("precision_form", sgx.default_opts(integrator=N.INTEGRATOR_ADAPTIVE,
+                                                           precision=N.PRECISION_MIXED))):
+        renderer.render(u, opts)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(2):
+            renderer.render(u, opts)
+        torch.cuda.synchronize()
+        res[name] = (time.perf_counter() - t0) / 2
+    print(f"1080p x 16 spp: reference CUDA kernel {rays / t_ref / 1e6:.1f} Mrays/s, ours fixed step "
+          f"{rays / res['fixed'] / 1e6:.1f}, ours precision form {rays / res['precision_form'] / 1e6:.1f}")
+    assert res["fixed"] < t_ref
