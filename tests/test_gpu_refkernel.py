@@ -3,9 +3,9 @@
 The reference kernel (render/cuda/kernels/geodesic_kernel.cu, compiled to PTX
 from the reference tree by `make -C oracle ref`) is launched the way
 CudaBackend::render_frame launches it (oracle/ref_gpu.py).  Parity: the same
-RGBA8 frame on the pinned scenes, within the bar of test_gpu_parity.py (both
-are FP32 CUDA; the few differing pixels are photon-ring rays where the two
-compilations' FMA contractions diverge).  Speed: the reference's
+RGBA8 frame on the pinned scenes — at least 99.5 % identical pixels and none
+off by more than one level (both are FP32 CUDA; the few differing pixels are
+near-polar rays where the two compilations' FMA contractions diverge).  Speed: the reference's
 one-thread-per-pixel fixed-step kernel against our fixed-step kernel and our
 precision form on the same scene, printed (and ours required faster)."""
 
@@ -52,7 +52,9 @@ def test_matches_reference_cuda_kernel(renderer, sgx, host_vectors, refk, rhs_fo
         e = channel_error(img, ref)
         exact = float((img == ref).all(axis=-1).mean())
         print(f"{name} rhs_form={rhs_form}: exact pixels {exact:.4f} {e}")
-        assert e["mean"] <= 2e-3 and e["le1_frac"] >= 0.97, (name, e)
+        # measured: identical frames on 8 of the 9 scenes, 99.8 % identical
+        # pixels (others one level off) on the near-polar one
+        assert exact >= 0.995 and e["max"] <= 1, (name, e)
         np.testing.assert_array_equal(ref, _ref_frame(refk, u))  # the reference kernel is deterministic
 
 
