@@ -85,3 +85,31 @@ def test_faster_than_reference_cuda_kernel(renderer, sgx, refk):
     print(f"1080p x 16 spp: reference CUDA kernel {rays / t_ref / 1e6:.1f} Mrays/s, ours fixed step "
           f"{rays / res['fixed'] / 1e6:.1f}, ours precision form {rays / res['precision_form'] / 1e6:.1f}")
     assert res["fixed"] < t_ref
+
+
+def test_random_scenes_match_reference_cuda_kernel(renderer, sgx, refk):
+    """Seeded random scenes (metric, spin, camera, FOV, flags, disc, spp, step,
+    budget) through both kernels."""
+    N = sgx._native
+    rng = np.random.default_rng(11)
+    exact_all = []
+    for i in range(24):
+        kerr = bool(rng.integers(0, 2))
+        spin = float(rng.uniform(0.0, 0.998)) if kerr else 0.0
+        sc = sgx.Scene(metric=sgx.MetricType.Kerr if kerr else sgx.MetricType.Schwarzschild, spin_a_over_M=spin,
+                       disc_inner_M=float(rng.uniform(1.5, 8.0)), disc_outer_M=float(rng.uniform(12.0, 40.0)),
+                       disc_peak_T_K=float(rng.uniform(3000.0, 20000.0)), render_supersample=int(rng.integers(1, 5)),
+                       h_step=float(rng.choice([0.2, 0.4])), max_steps=int(rng.choice([500, 2500])),
+                       disc_doppler_on=bool(rng.integers(0, 2)), disc_redshift_on=bool(rng.integers(0, 2)))
+        cam = sgx.build_orbital_camera(float(rng.uniform(15.0, 60.0)), float(rng.uniform(-1.4, 1.4)),
+                                       float(rng.uniform(0.0, 6.28)), float(rng.uniform(20.0, 70.0)))
+        u = sgx.pack_uniforms(sc, cam, int(rng.integers(8, 80)), int(rng.integers(8, 60)), float(rng.uniform(0, 2)))
+        ref = _ref_frame(refk, u)
+        img = renderer.render_image(u)
+        e = channel_error(img, ref)
+        exact = float((img == ref).all(axis=-1).mean())
+        exact_all.append(exact)
+        print(f"scene {i} kerr={kerr} a={spin:.3f} {u.width}x{u.height}x{u.supersample}: exact {exact:.4f} max {e['max']}")
+        assert e["mean"] <= 2e-3 and e["le1_frac"] >= 0.97, (i, e)
+    print(f"mean identical pixels {np.mean(exact_all):.4f}")
+    assert np.mean(exact_all) >= 0.99
