@@ -4,7 +4,8 @@ Workload (the headline of the reference's own benchmarks, and the scene of
 its 4K x 256 spp Kerr claim): Kerr a/M = 0.94, 3840x2160, 256 samples per
 pixel with Halton(2,3) jitter, observer at r = 40 M, inclination 75 deg
 (elevation 0.261799 rad), vertical FOV 30 deg, disc from the prograde ISCO to
-30 M, peak temperature 1e4 K, reference defaults otherwise.  Integrated in
+30 M, peak temperature 1e4 K, disc-band phase of turbulence seed 7 (time
+7/30 s), reference defaults otherwise.  Integrated in
 the precision form: the error-controlled Kerr RK4 at tolerance 1e-6 in FP32,
 with the constants of motion and the step control within 0.05 M of the
 photon orbit or the horizon in FP64 (`--precision fp32 | fp64` for the other
@@ -63,7 +64,7 @@ def workload_uniforms(S, spp=SPP):
     scene = S.Scene(spin_a_over_M=0.94, disc_inner_M=isco, disc_outer_M=30.0, disc_peak_T_K=1e4,
                     render_supersample=spp)
     cam = S.build_orbital_camera(40.0, 0.261799, 0.0, 30.0)
-    return S.pack_uniforms(scene, cam, WIDTH, HEIGHT, 0.0)
+    return S.pack_uniforms(scene, cam, WIDTH, HEIGHT, S.workloads.turbulence_time())
 
 
 class ClockSampler:
@@ -442,7 +443,7 @@ def main() -> None:
     from singularity_gb300 import dist as D
     cam = S.build_orbital_camera(40.0, 0.261799, D.view_azimuth(rank, world), 30.0)
     u = S.pack_uniforms(S.Scene(spin_a_over_M=0.94, disc_inner_M=isco, disc_outer_M=30.0, disc_peak_T_K=1e4,
-                                render_supersample=SPP), cam, WIDTH, HEIGHT, 0.0)
+                                render_supersample=SPP), cam, WIDTH, HEIGHT, S.workloads.turbulence_time())
     npix = u.width * u.height
     r = S.Renderer(local)
     stream = torch.cuda.Stream()

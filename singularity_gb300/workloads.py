@@ -15,12 +15,22 @@ import numpy as np
 from . import backend as B
 
 
-def _kerr(spin, r_obs, incl_deg, fov_deg, w, h, spp, peak_T=1e4, r_out=30.0, r_in=None, max_steps=0):
+# Band-phase seed of the disc turbulence (the reference has no seed): seed s
+# renders the bands at time s / 30 s, the phase the reference's 1/30 s frame
+# clock reaches at frame s (cuda_backend.cu:149-151).
+TURBULENCE_SEED = 7
+
+
+def turbulence_time(seed: int = TURBULENCE_SEED) -> float:
+    return seed / 30.0
+
+
+def _kerr(spin, r_obs, incl_deg, fov_deg, w, h, spp, peak_T=1e4, r_out=30.0, r_in=None, max_steps=0, time_sec=0.0):
     isco = B.kerr_isco_prograde(1.0, spin)
     sc = B.Scene(spin_a_over_M=spin, disc_inner_M=isco if r_in is None else r_in, disc_outer_M=r_out,
                  disc_peak_T_K=peak_T, render_supersample=spp, max_steps=max_steps)
     cam = B.build_orbital_camera(r_obs, math.pi / 2 - math.radians(incl_deg), 0.0, fov_deg)
-    return B.pack_uniforms(sc, cam, w, h, 0.0)
+    return B.pack_uniforms(sc, cam, w, h, time_sec)
 
 
 def schwarzschild_256():
@@ -32,14 +42,15 @@ def schwarzschild_256():
     return B.pack_uniforms(sc, cam, 256, 256, 0.0)
 
 
-def kerr_1080p_16spp():
-    """Kerr a = 0.94, 1920x1080, 16 spp, r_obs 40 M, i = 75 deg, FOV 30, disc ISCO-30 M, 1e4 K."""
-    return _kerr(0.94, 40.0, 75.0, 30.0, 1920, 1080, 16)
+def kerr_1080p_16spp(seed: int = TURBULENCE_SEED):
+    """Kerr a = 0.94, 1920x1080, 16 spp, r_obs 40 M, i = 75 deg, FOV 30, disc ISCO-30 M, 1e4 K,
+    turbulence band phase of seed 7."""
+    return _kerr(0.94, 40.0, 75.0, 30.0, 1920, 1080, 16, time_sec=turbulence_time(seed))
 
 
-def kerr_4k_256spp():
+def kerr_4k_256spp(seed: int = TURBULENCE_SEED):
     """The 1080p Kerr a = 0.94 scene at 3840x2160 and 256 spp."""
-    return _kerr(0.94, 40.0, 75.0, 30.0, 3840, 2160, 256)
+    return _kerr(0.94, 40.0, 75.0, 30.0, 3840, 2160, 256, time_sec=turbulence_time(seed))
 
 
 def batch_64_views(seed: int = 0):
