@@ -113,3 +113,21 @@ def test_random_scenes_match_reference_cuda_kernel(renderer, sgx, refk):
         assert e["mean"] <= 2e-3 and e["le1_frac"] >= 0.97, (i, e)
     print(f"mean identical pixels {np.mean(exact_all):.4f}")
     assert np.mean(exact_all) >= 0.99
+
+
+def test_schwarzschild_256_workload(renderer, sgx, oracle, refk):
+    """The plain Schwarzschild workload (256x256, 1 spp at pixel centres, h = 0.05 M,
+    4000 steps, r 30 M, i 80 deg, FOV 40, disc 6-20 M, FP32 RGBA float output):
+    RGBA8 against the reference CUDA kernel, RGBA32F against the FP32 oracle."""
+    N = sgx._native
+    u = sgx.workloads.schwarzschild_256()
+    ref = _ref_frame(refk, u)
+    img = renderer.render_image(u)
+    exact = float((img == ref).all(axis=-1).mean())
+    f32 = renderer.capture(N.FORMAT_RGBA32F)[..., :3]
+    _, ldr = oracle.render(u)
+    d = np.abs(f32 - ldr.reshape(u.height, u.width, 3))
+    print(f"schwarzschild_256: identical RGBA8 pixels vs reference kernel {exact:.4f}; "
+          f"RGBA32F vs oracle mean {d.mean():.2e} max {d.max():.2e}")
+    assert exact >= 0.995
+    assert d.mean() <= 1e-5
