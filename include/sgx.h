@@ -75,7 +75,7 @@ typedef struct sgx_render_opts {
     uint32_t sample_count;   /* samples in this pass; 0 = all remaining (default 0) */
     uint32_t block_threads;  /* launch shape: threads per block; 0 = tuned default */
     uint32_t blocks_per_sm;  /* launch shape: resident blocks per SM; 0 = occupancy limit */
-    uint32_t refill_interval;/* steps between warp refills of finished rays; 0 = tuned */
+    uint32_t refill_interval;/* steps between warp refills of finished rays; 0 = 32 */
     uint32_t rhs_form;       /* Kerr right-hand side: 0 = shared-reciprocal form (default),
                                 1 = the reference's division-for-division form,
                                 2 = form 0 with the SFU's sine/cosine where |sin(theta)| >= 1/4

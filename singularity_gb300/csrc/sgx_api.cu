@@ -149,7 +149,7 @@ sgx_status render_impl(sgx_context* c, const sgx_uniforms* u, const sgx_render_o
         SGX_CUDA(c, cudaMemcpyAsync(c->d_words, plan.words, plan.word_count * 8, cudaMemcpyHostToDevice, st));
         sgxk::PassDesc pass{};
         pass.vs = sgxk::make_view_set(plan, c->d_view, c->d_words);
-        pass.refill = o.refill_interval == 0 ? 16u : o.refill_interval;
+        pass.refill = o.refill_interval == 0 ? sgxk::kDefaultRefill : o.refill_interval;
         pass.results = c->d_results;
         pass.counters = c->d_counters;
         pass.tol = o.tolerance;

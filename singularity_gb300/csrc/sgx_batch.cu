@@ -60,7 +60,7 @@ cudaError_t enqueue(sgx_batch* b, const sgx_render_opts& o, const sgxk::ViewPlan
                     cudaStream_t st) {
     sgxk::PassDesc pass{};
     pass.vs = sgxk::make_view_set(plan, b->d_views, b->d_words);
-    pass.refill = o.refill_interval == 0 ? 16u : o.refill_interval;
+    pass.refill = o.refill_interval == 0 ? sgxk::kDefaultRefill : o.refill_interval;
     pass.results = results;
     pass.counters = b->d_counters;
     pass.tol = o.tolerance;

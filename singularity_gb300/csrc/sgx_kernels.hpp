@@ -44,6 +44,9 @@ struct ViewSet {
     std::uint64_t total_pix;
 };
 
+// Steps between warp refills when the caller leaves it to the library: the
+// 4K Kerr pass runs 1.6 % faster at 32 than at 16 (64: within 1 %; 8: 4 % slower).
+constexpr std::uint32_t kDefaultRefill = 32;
 constexpr std::uint32_t kMaxLaunchViews = 128;
 constexpr std::uint32_t kMaxPassSamplesHost = 1024;
 

@@ -160,7 +160,7 @@ extern "C" sgx_status sgx_render_noalloc(const sgx_uniforms* u, const sgx_render
     }
     sgxk::PassDesc pass{};
     pass.vs = sgxk::make_view_set(plan, d_view, d_words);
-    pass.refill = o.refill_interval == 0 ? 16u : o.refill_interval;
+    pass.refill = o.refill_interval == 0 ? sgxk::kDefaultRefill : o.refill_interval;
     pass.results = results;
     pass.counters = counters;
     pass.tol = o.tolerance;
