@@ -67,6 +67,9 @@ void print_help() {
         "  --turbulence X                disc band amplitude (default 0.5)\n"
         "  --h-step H / --max-steps N    integrator step and budget (default 0.4 / 2500)\n"
         "  --adaptive-step               radius-adaptive fixed step h * clamp(r / 6M, 1, 40)\n"
+        "  --turbulence-seed N           disc band phase of seed N (first frame at time N/30 s)\n"
+        "  --bloom                       bloom + blit post-process (half-float HDR, the 7-tap kernel)\n"
+        "  --bloom-sigma PX              ... with a Gaussian of PX pixels instead\n"
         "  --disc-inner-isco             disc inner edge at the prograde ISCO of the spin\n"
         "  --use-scene-camera            take camera_distance/elevation/fov from the scene file\n"
         "  --use-scene-integrator        take h_step/max_steps from the scene file\n"
@@ -175,6 +178,9 @@ int main(int argc, char** argv) {
     sgx_render_opts opts;
     sgx_render_opts_default(&opts);
     bool have_opts = false, isco_inner = false, scene_camera = false, scene_integrator = false, pfm = false, adaptive_step = false;
+    bool bloom = false, have_seed = false;
+    float bloom_sigma = 0.0f;
+    long turbulence_seed = 0;
     float peak_temp = -1.0f, exposure = -1.0f, turbulence = -1.0f, h_step = 0.0f;
     std::uint32_t max_steps = 0;
 
@@ -268,6 +274,14 @@ int main(int argc, char** argv) {
             max_steps = static_cast<std::uint32_t>(std::strtoul(argv[++i], nullptr, 10));
         } else if (a == "--adaptive-step") {
             adaptive_step = true;
+        } else if (a == "--turbulence-seed" && has_val) {
+            turbulence_seed = std::strtol(argv[++i], nullptr, 10);
+            have_seed = true;
+        } else if (a == "--bloom") {
+            bloom = true;
+        } else if (a == "--bloom-sigma" && has_val) {
+            bloom = true;
+            bloom_sigma = std::strtof(argv[++i], nullptr);
         } else if (a == "--disc-inner-isco") {
             isco_inner = true;
         } else if (a == "--use-scene-camera") {
@@ -324,6 +338,10 @@ int main(int argc, char** argv) {
     if (adaptive_step) scene.adaptive_step_on = true;
     if (max_steps > 0) scene.max_steps = max_steps;
 
+    if (bloom && !(bloom_sigma >= 0.0f && bloom_sigma <= 64.0f)) {
+        std::fprintf(stderr, "singularity_cuda_cli: --bloom-sigma must be in [0, 64]\n");
+        return 2;
+    }
     if (frames > 1 && output_pattern.empty()) {
         std::fprintf(stderr,
                      "singularity_cuda_cli: --frames > 1 requires --output-pattern with a "
@@ -352,6 +370,8 @@ int main(int argc, char** argv) {
         return 1;
     }
     if (have_opts) backend.set_render_options(opts);
+    if (bloom) backend.set_bloom(bloom_sigma);
+    if (have_seed) backend.set_frame_time(float(turbulence_seed) / 30.0f);
 
     constexpr float kTwoPi = 6.28318530717958647693f;
     std::future<bool> pending;

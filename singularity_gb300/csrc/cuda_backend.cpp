@@ -54,7 +54,11 @@ void CudaBackend::resize(std::uint32_t width, std::uint32_t height) {
 void CudaBackend::render_frame(const Scene& scene, const CameraState& camera) {
     if (ctx_ == nullptr) return;
     const sgx_uniforms u = sgx::pack_uniforms(scene, camera, width_, height_, frame_time_sec_);
-    const sgx_status s = sgx_render(ctx_, &u, have_opts_ ? &opts_ : nullptr);
+    sgx_render_opts o;
+    if (have_opts_) o = opts_;
+    else sgx_render_opts_default(&o);
+    if (bloom_) o.format = SGX_FORMAT_RGBA16F_HDR;
+    const sgx_status s = sgx_render(ctx_, &u, &o);
     if (s != SGX_OK) {
         std::fprintf(stderr, "singularity CUDA backend: render failed: %s\n", sgx_last_error(ctx_));
     } else {
@@ -63,11 +67,26 @@ void CudaBackend::render_frame(const Scene& scene, const CameraState& camera) {
     frame_time_sec_ += 1.0f / 30.0f;
 }
 
+bool CudaBackend::post_(std::uint32_t format) {
+    if (!bloom_) return true;
+    sgx_bloom_opts b{};
+    b.struct_size = sizeof(b);
+    b.sigma_px = bloom_sigma_;
+    b.threshold = bloom_threshold_;
+    b.strength = bloom_strength_;
+    b.format = format;
+    if (sgx_bloom(ctx_, &b) != SGX_OK) {
+        std::fprintf(stderr, "singularity CUDA backend: bloom failed: %s\n", sgx_last_error(ctx_));
+        return false;
+    }
+    return true;
+}
+
 ImageData CudaBackend::capture_frame() {
     ImageData out;
     out.width = width_;
     out.height = height_;
-    if (ctx_ == nullptr || !rendered_) return out;
+    if (ctx_ == nullptr || !rendered_ || !post_(SGX_FORMAT_RGBA8_SRGB)) return out;
     out.pixels_rgba.resize(std::size_t(width_) * height_ * 4u);
     if (sgx_capture(ctx_, out.pixels_rgba.data(), out.pixels_rgba.size(), SGX_FORMAT_RGBA8_SRGB) != SGX_OK) {
         std::fprintf(stderr, "singularity CUDA backend: capture failed: %s\n", sgx_last_error(ctx_));
@@ -78,7 +97,7 @@ ImageData CudaBackend::capture_frame() {
 
 std::vector<float> CudaBackend::capture_frame_float() {
     std::vector<float> out;
-    if (ctx_ == nullptr || !rendered_) return out;
+    if (ctx_ == nullptr || !rendered_ || !post_(SGX_FORMAT_RGBA32F)) return out;
     out.resize(std::size_t(width_) * height_ * 4u);
     if (sgx_capture(ctx_, out.data(), out.size() * sizeof(float), SGX_FORMAT_RGBA32F) != SGX_OK) out.clear();
     return out;

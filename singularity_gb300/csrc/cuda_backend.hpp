@@ -74,6 +74,17 @@ public:
     void set_render_options(const sgx_render_opts& opts) { opts_ = opts; have_opts_ = true; }
     // Extension: the last frame as RGBA32F (tone-mapped mean before sRGB).
     std::vector<float> capture_frame_float();
+    // Extension: the bloom + blit post-process of the desktop backends on every
+    // later frame (frames render to the half-float HDR target; captures return
+    // the composite). sigma_px 0 = the reference's 7-tap kernel.
+    void set_bloom(float sigma_px, float threshold = -1.0f, float strength = -1.0f) {
+        bloom_ = true;
+        bloom_sigma_ = sigma_px;
+        bloom_threshold_ = threshold;
+        bloom_strength_ = strength;
+    }
+    // Extension: the virtual clock of the next frame (the disc bands' phase).
+    void set_frame_time(float seconds) { frame_time_sec_ = seconds; }
 
 private:
     std::uint32_t width_{0};
@@ -83,6 +94,9 @@ private:
     float frame_time_sec_{0.0f};
     sgx_render_opts opts_{};
     bool have_opts_{false};
+    bool bloom_{false};
+    float bloom_sigma_{0.0f}, bloom_threshold_{-1.0f}, bloom_strength_{-1.0f};
+    bool post_(std::uint32_t format);
 };
 
 }  // namespace singularity

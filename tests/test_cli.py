@@ -47,6 +47,7 @@ def test_help(cli):
     (["--frames", "3", "--output-pattern", "frame.png"], "--output-pattern must contain a printf placeholder"),
     (["--encode-mp4", "x.mp4"], "--encode-mp4 requires --frames > 1"),
     (["--integrator", "euler"], "--integrator must be fixed or adaptive"),
+    (["--bloom-sigma", "100"], "--bloom-sigma must be in [0, 64]"),
 ])
 def test_usage_errors_exit_2(cli, args, msg):
     r = run(cli, *args)
@@ -143,3 +144,24 @@ def test_cli_adaptive_step_flag(cli, tmp_path, sgx, oracle):
     ref, _ = oracle.render(u)
     d = np.abs(img[..., :3].astype(int) - ref[..., :3].astype(int))
     assert d.mean() <= 0.5 and (d.max(axis=-1) <= 1).mean() >= 0.97
+
+
+@pytest.mark.gpu
+def test_cli_bloom_and_seed(cli, tmp_path, sgx, renderer):
+    """--bloom-sigma renders the half-float HDR frame and writes the bloom +
+    ACES composite; --turbulence-seed sets the first frame's band phase. The
+    PNG equals the library's HDR render + sgx_bloom of the same scene."""
+    N = sgx._native
+    r = run(cli, "--output", tmp_path / "b.png", "--res", "96x54", "--samples-per-pixel", "2",
+            "--bloom-sigma", "8", "--turbulence-seed", "7")
+    assert r.returncode == 0, r.stderr
+    img = read_png(tmp_path / "b.png")
+    sc = sgx.Scene(render_supersample=2)
+    u = sgx.pack_uniforms(sc, sgx.build_orbital_camera(30.0, 0.15, 0.0, 60.0), 96, 54, 7.0 / 30.0)
+    renderer.render(u, sgx.default_opts(format=N.FORMAT_RGBA16F_HDR))
+    ref = renderer.bloom(sigma_px=8.0, fmt=N.FORMAT_RGBA8_SRGB)
+    np.testing.assert_array_equal(img, ref)
+    plain = run(cli, "--output", tmp_path / "p.png", "--res", "96x54", "--samples-per-pixel", "2",
+                "--turbulence-seed", "7")
+    assert plain.returncode == 0
+    assert not np.array_equal(read_png(tmp_path / "p.png"), img)
