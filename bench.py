@@ -396,6 +396,44 @@ def diff_study(S, N, r, torch, adam_steps: int = 200, fd_eps: float = 1e-3) -> d
     return out
 
 
+# The scene of the reference's published CUDA timing (scenes/kerr_a094.scene:
+# a/M = 0.94, disc 1.7-30 M, Doppler and redshift on), CLI defaults otherwise.
+KERR_A094_SCENE = ("mass = 1.0\nspin = 0.94\ndisc_r_inner = 1.7\ndisc_r_outer = 30.0\n"
+                   "disc_doppler_on = 1\ndisc_redshift_on = 1\n")
+
+
+def cli_study(reps: int = 1) -> dict:
+    """The reference's headline command end to end: `singularity_cuda_cli --res
+    3840x2160 --samples-per-pixel 256 --scene kerr_a094.scene --output x.png`
+    (4K Kerr a/M = 0.94 at 256 spp; the reference quotes about 2:42 on an RTX
+    3090, README.md:39,130), wall clock of the process including CUDA start-up
+    and the PNG write; once with the reference's fixed-step integrator (the
+    defaults) and once with --integrator adaptive --precision mixed."""
+    import tempfile
+    cli = ROOT / "singularity_gb300" / "_build" / "singularity_cuda_cli"
+    if not cli.exists():
+        return {"unavailable": "CLI not built"}
+    out = {"command": "singularity_cuda_cli --res 3840x2160 --samples-per-pixel 256 --scene kerr_a094.scene "
+                      "--output <png>", "reference_published_s": 162.0}
+    with tempfile.TemporaryDirectory() as td:
+        scene = Path(td) / "kerr_a094.scene"
+        scene.write_text(KERR_A094_SCENE)
+        for name, extra in (("fixed_step", []), ("adaptive_mixed", ["--integrator", "adaptive", "--precision",
+                                                                     "mixed"])):
+            ts = []
+            for _ in range(reps):
+                t0 = time.perf_counter()
+                r = subprocess.run([str(cli), "--res", "3840x2160", "--samples-per-pixel", "256", "--scene",
+                                    str(scene), "--output", str(Path(td) / "x.png"), *extra],
+                                   capture_output=True, text=True, timeout=600)
+                ts.append(time.perf_counter() - t0)
+                if r.returncode != 0:
+                    return {"unavailable": f"CLI exit {r.returncode}: {r.stderr[-200:]}"}
+            out[f"{name}_s"] = float(min(ts))
+            out[f"{name}_vs_published"] = 162.0 / float(min(ts))
+    return out
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -407,6 +445,7 @@ def main() -> None:
     ap.add_argument("--no-precision-study", action="store_true")
     ap.add_argument("--no-batch-study", action="store_true")
     ap.add_argument("--no-diff-study", action="store_true")
+    ap.add_argument("--no-cli-study", action="store_true")
     ap.add_argument("--adam-steps", type=int, default=200)
     ap.add_argument("--rhs-form", type=int, default=0)
     ap.add_argument("--integrator", choices=["adaptive", "fixed"], default="adaptive")
@@ -570,6 +609,9 @@ def main() -> None:
     diff = None
     if single and not args.no_diff_study and args.precision != "fp64" and integ == N.INTEGRATOR_ADAPTIVE:
         diff = diff_study(S, N, r, torch, adam_steps=args.adam_steps)
+    cli = None
+    if single and not args.no_cli_study and args.workload == "4k":
+        cli = cli_study()
     cpu = None if (args.no_cpu_baseline or rank != 0 or not single) else cpu_baseline(S, O, u)
     clocks = clk.summary()
     wl = (f"kerr_a0.94_r40_i75_fov30_isco-30M_T1e4_{WIDTH}x{HEIGHT}_256spp_"
@@ -592,6 +634,7 @@ def main() -> None:
         "batched_views": batch,
         "hdr_bloom_1080p": hdr,
         "adjoint_512x512x4": diff,
+        "cli_4k_256spp": cli,
     }
     print(json.dumps(line), flush=True)
     if world > 1:
