@@ -18,7 +18,7 @@
 //     the next step's k1 (a rejected attempt costs the same four evaluations);
 //   * the max-norm over (r, theta, phi, p_r, p_theta) of that estimate scaled
 //     by tol * (1 + max(|y|, |y_new|)); accept when <= 1;
-//   * the step update h *= clamp(0.9 / sqrt(sqrt(err)), 0.2, 4) and the ceiling
+//   * the step update h *= clamp(0.85 / sqrt(sqrt(err)), 0.2, 4) and the ceiling
 //     h <= h_max_frac * r — written with IEEE sqrt and division only, so a CPU
 //     and a GPU controller round identically;
 //   * equatorial crossings located on the cubic Hermite interpolant of the
@@ -139,17 +139,20 @@ inline C error_norm(const KState<T>& y, const Attempt<T>& a, float tol_f) {
     return e;
 }
 
-// h *= clamp(0.9 / err^(1/4), 0.2, 4), computed in C.
+// h *= clamp(0.85 / err^(1/4), 0.2, 4), computed in C.  Safety factor 0.85:
+// on the 4K Kerr a = 0.94 scene 0.9 rejects 14 % of the attempts; 0.85 takes
+// 10 % fewer attempts per ray (40.4 against 45.0) for the same error against
+// an FP64 solution at tolerance 1e-10 (0.8 and 0.75 take more).
 template <class C> inline C step_factor(C e) {
     if (e <= C(1e-30f)) return C(4.0f);
-    C f = C(0.9f) / std::sqrt(std::sqrt(e));
+    C f = C(0.85f) / std::sqrt(std::sqrt(e));
     f = f < C(0.2f) ? C(0.2f) : f;
     f = f > C(4.0f) ? C(4.0f) : f;
     return f;
 }
 template <> inline Counted step_factor<Counted>(Counted e) {
     if (e <= Counted(1e-30f)) return Counted(4.0f);
-    Counted f = Counted(0.9f) / M<Counted>::sqrt(M<Counted>::sqrt(e));
+    Counted f = Counted(0.85f) / M<Counted>::sqrt(M<Counted>::sqrt(e));
     f = f < Counted(0.2f) ? Counted(0.2f) : f;
     f = f > Counted(4.0f) ? Counted(4.0f) : f;
     return f;

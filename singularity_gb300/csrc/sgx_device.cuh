@@ -752,10 +752,10 @@ __device__ __forceinline__ T error_norm_fast(const KS<T>& y, const KAttempt<T>& 
     return e;
 }
 
-// h *= clamp(0.9 / err^(1/4), 0.2, 4) with IEEE sqrt and division only.
+// h *= clamp(0.85 / err^(1/4), 0.2, 4) with IEEE sqrt and division only.
 template <class C> __device__ __forceinline__ C step_factor(C e) {
     if (e <= C(1e-30f)) return C(4.0f);
-    C f = C(0.9f) / sqrt(sqrt(e));
+    C f = C(0.85f) / sqrt(sqrt(e));
     f = f < C(0.2f) ? C(0.2f) : f;
     f = f > C(4.0f) ? C(4.0f) : f;
     return f;
@@ -764,7 +764,7 @@ template <class C> __device__ __forceinline__ C step_factor(C e) {
 // The same factor from one square root and one approximate reciprocal square root.
 __device__ __forceinline__ float step_factor_fast(float e) {
     if (e <= 1e-30f) return 4.0f;
-    float f = 0.9f * rsqrtf(sqrtf(e));
+    float f = 0.85f * rsqrtf(sqrtf(e));
     f = f < 0.2f ? 0.2f : f;
     f = f > 4.0f ? 4.0f : f;
     return f;
