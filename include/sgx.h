@@ -76,10 +76,11 @@ typedef struct sgx_render_opts {
     uint32_t block_threads;  /* launch shape: threads per block; 0 = tuned default */
     uint32_t blocks_per_sm;  /* launch shape: resident blocks per SM; 0 = occupancy limit */
     uint32_t refill_interval;/* steps between warp refills of finished rays; 0 = 32 */
-    uint32_t rhs_form;       /* Kerr right-hand side: 0 = shared-reciprocal form (default),
+    uint32_t rhs_form;       /* Kerr right-hand side: 0 = the same Hamiltonian in Carter's
+                                    separated form, three reciprocals (default),
                                 1 = the reference's division-for-division form,
                                 2 = form 0 with the SFU's sine/cosine where |sin(theta)| >= 1/4
-                                    (FP32; about 10 % faster, FP32-vs-FP64 image error 1.6x) */
+                                    (FP32; faster, FP32-vs-FP64 image error ~1.2x) */
     uint32_t tile_w;         /* ray order: tiles of tile_w x tile_h pixels, samples innermost;  */
     uint32_t tile_h;         /*   0 = whole rows (tile_w = width, tile_h = 1)                  */
 } sgx_render_opts;

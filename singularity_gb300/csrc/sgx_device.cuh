@@ -392,23 +392,21 @@ template <class T> struct KS {
     T r, th, ph, pr, pth;
 };
 
-// Per-ray constants of motion and the products the FAST form folds.
+// Per-ray constants of motion and the products the separated form folds.
 template <class T> struct KC {
     T E, L;
-    T E2, L2, cEL, aL2;  // E^2, L^2, 4 M a E L, a^2 L^2
-    T twoMaE, twoMaL;    // 2 M a E, 2 M a L
+    T aE, aL;          // a E, a L
+    T twoaE, fourE;    // 2 a E, 4 E
 };
 
 template <class T> __device__ __forceinline__ KC<T> make_kc(const View<T>& v, T E, T L) {
     KC<T> c;
     c.E = E;
     c.L = L;
-    c.E2 = E * E;
-    c.L2 = L * L;
-    c.cEL = DLIT(4.0) * v.M * v.a * E * L;
-    c.aL2 = v.a2 * c.L2;
-    c.twoMaE = DLIT(2.0) * v.M * v.a * E;
-    c.twoMaL = DLIT(2.0) * v.M * v.a * L;
+    c.aE = v.a * E;
+    c.aL = v.a * L;
+    c.twoaE = DLIT(2.0) * c.aE;
+    c.fourE = DLIT(4.0) * E;
     return c;
 }
 
@@ -450,62 +448,60 @@ template <class T> __device__ __forceinline__ KS<T> kerr_rhs_ref(const KS<T>& s,
     return d;
 }
 
-// Same function, three reciprocals and folded constants.
-//   dphi   = (2Mra E s2 + (Delta - a2 s2) L) / (Sigma Delta s2)
-//   dr     = Delta p_r / Sigma,     dth = p_th / Sigma
-//   -2 dp_r  = B_r/(SD) - B (2r Delta + Sigma Del_r)/(SD)^2 - 2r L^2/(Sigma^2 s2)
-//              + Del_r p_r^2 / Sigma - 2r Dp2 / Sigma^2
-//   -2 dp_th = B_t/(SD) - B Sig_t/(Sigma^2 Delta)
-//              - L^2 (Sig_t s2 + Sigma sin2t)/(Sigma^2 s2^2) - Dp2 Sig_t / Sigma^2
+// The same Hamiltonian in Carter's separated form (Carter 1968), with three
+// reciprocals.  With s2 = sin^2(theta), P = (r^2 + a^2) E - a L and
+// W = L - a E s2,
+//   2 Sigma H = N = Delta p_r^2 + p_th^2 - P^2 / Delta + W^2 / s2,
+// which equals the reference's grouping identically: -P^2/Delta + W^2/s2 =
+// B/Delta + L^2/s2 with B = -A E^2 + 4 M a r E L - a^2 L^2 (expand and use
+// r^2 + a^2 - Delta = 2 M r).  With Q = P/Delta and U = W/s2:
+//   dr = Delta p_r / Sigma,   dth = p_th / Sigma,   dphi = (a Q + U) / Sigma
+//   dp_r  = -(N_r  - N Sigma_r  / Sigma) / (2 Sigma),  N_r  = Delta' (p_r^2 + Q^2) - 4 r E Q
+//   dp_th = -(N_th - N Sigma_th / Sigma) / (2 Sigma),  N_th = -sin2t U (2 a E + U),
+//   Sigma_r = 2 r,  Sigma_th = -a^2 sin2t,  Delta' = 2 (r - M).
+// About 45 operations against the reference grouping's ~75; the 1/sin^2
+// guard (1e-10) applies to U as it does to the reference's L^2/s2 terms.
 template <class T>
-__device__ __forceinline__ KS<T> kerr_rhs_fast_sc(const KS<T>& s, T st, T ct, const View<T>& v, const KC<T>& c) {
+__device__ __forceinline__ KS<T> kerr_rhs_sep_sc(const KS<T>& s, T st, T ct, const View<T>& v, const KC<T>& c) {
     const T r = s.r;
     const T a2 = v.a2;
     const T s2 = st * st;
     const T safe_s2 = DM<T>::fmax_(s2, DLIT(1e-10));
-    const T c2 = ct * ct;
     const T r2 = r * r;
-    const T r2a2 = r2 + a2;
-    const T Sigma = r2 + a2 * c2;
-    const T Del_r = DLIT(2.0) * (r - v.M);
+    const T Sigma = r2 + a2 * (ct * ct);
     const T Delta = r * (r - DLIT(2.0) * v.M) + a2;
-    const T a2s2 = a2 * s2;
-    const T A = r2a2 * r2a2 - a2s2 * Delta;
+    const T Del_r = DLIT(2.0) * r - DLIT(2.0) * v.M;
+    const T P = (r2 + a2) * c.E - c.aL;
+    const T W = c.L - c.aE * s2;
     const T iS = DM<T>::rcp_fast(Sigma);
     const T iD = DM<T>::rcp_fast(Delta);
     const T is2 = DM<T>::rcp_fast(safe_s2);
-    const T iSD = iS * iD;
-    const T iS2 = iS * iS;
+    const T Q = P * iD;
+    const T U = W * is2;
     KS<T> d;
-    d.ph = (c.twoMaE * r * s2 + (Delta - a2s2) * c.L) * iSD * is2;
     d.r = Delta * s.pr * iS;
     d.th = s.pth * iS;
-    const T B = (c.cEL * r - A * c.E2) - c.aL2;
-    const T A_r = DLIT(4.0) * r * r2a2 - a2s2 * Del_r;
-    const T B_r = c.cEL - A_r * c.E2;
-    const T sin2t = DLIT(2.0) * st * ct;
-    const T Sig_t = -a2 * sin2t;
+    d.ph = (v.a * Q + U) * iS;
     const T pr2 = s.pr * s.pr;
-    const T Dp2 = Delta * pr2 + s.pth * s.pth;
-    const T two_r = DLIT(2.0) * r;
-    const T dH_dr = iSD * (B_r - B * (two_r * Delta + Sigma * Del_r) * iSD) + Del_r * pr2 * iS
-                    - two_r * iS2 * (c.L2 * is2 + Dp2);
-    const T dH_dth = iSD * (a2 * Delta * sin2t * c.E2) - B * Sig_t * iS2 * iD
-                     - iS2 * (c.L2 * is2 * (Sig_t + Sigma * sin2t * is2) + Dp2 * Sig_t);
-    d.pr = DLIT(-0.5) * dH_dr;
-    d.pth = DLIT(-0.5) * dH_dth;
+    const T N = ((Delta * pr2 + s.pth * s.pth) - P * Q) + W * U;
+    const T N_r = Del_r * (Q * Q + pr2) - (c.fourE * r) * Q;
+    const T NiS = N * iS;
+    const T m = DLIT(-0.5) * iS;
+    d.pr = m * (N_r - (DLIT(2.0) * r) * NiS);
+    const T sin2t = DLIT(2.0) * st * ct;
+    d.pth = m * (sin2t * (a2 * NiS - U * (c.twoaE + U)));
     return d;
 }
 
-// Kerr RHS forms: 0 = the reference's divisions, 1 = shared reciprocals,
-// 2 = shared reciprocals with the SFU's sine/cosine (FP32 only; CUDA's
+// Kerr RHS forms: 0 = the reference's divisions, 1 = the separated form,
+// 2 = the separated form with the SFU's sine/cosine (FP32 only; CUDA's
 // __sincosf) wherever |sin(theta)| >= 1/4 — its absolute error (~4e-7) would
 // be a large relative error of the 1/sin^2 terms nearer the poles, where the
 // IEEE-accurate sincosf is kept.
-constexpr int RHS_REF = 0, RHS_SHARED = 1, RHS_SHARED_HWTRIG = 2;
+constexpr int RHS_REF = 0, RHS_SEP = 1, RHS_SEP_HWTRIG = 2;
 
 template <class T, int FORM> __device__ __forceinline__ void rhs_sincos(T x, T* s, T* c) {
-    if constexpr (FORM == RHS_SHARED_HWTRIG && std::is_same_v<T, float>) {
+    if constexpr (FORM == RHS_SEP_HWTRIG && std::is_same_v<T, float>) {
         __sincosf(x, s, c);
         if (fabsf(*s) < 0.25f) sincosf(x, s, c);
     } else {
@@ -513,11 +509,11 @@ template <class T, int FORM> __device__ __forceinline__ void rhs_sincos(T x, T* 
     }
 }
 
-template <class T, int FORM = RHS_SHARED>
+template <class T, int FORM = RHS_SEP>
 __device__ __forceinline__ KS<T> kerr_rhs_fast(const KS<T>& s, const View<T>& v, const KC<T>& c) {
     T st, ct;
     rhs_sincos<T, FORM>(s.th, &st, &ct);
-    return kerr_rhs_fast_sc(s, st, ct, v, c);
+    return kerr_rhs_sep_sc(s, st, ct, v, c);
 }
 
 template <class T, int FORM>
@@ -553,7 +549,7 @@ __device__ __forceinline__ KS<T> kerr_rk4(const KS<T>& y, T h, const View<T>& v,
     h = h * ps;
     const T hh = DLIT(0.5) * h;
     KS<T> k1;
-    if constexpr (FORM != RHS_REF) k1 = kerr_rhs_fast_sc(y, s0, c0, v, c);
+    if constexpr (FORM != RHS_REF) k1 = kerr_rhs_sep_sc(y, s0, c0, v, c);
     else k1 = kerr_rhs_ref(y, v, c);
     const KS<T> k2 = kerr_rhs<T, FORM>(ks_axpy(y, k1, hh), v, c);
     const KS<T> k3 = kerr_rhs<T, FORM>(ks_axpy(y, k2, hh), v, c);

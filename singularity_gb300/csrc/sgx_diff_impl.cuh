@@ -66,8 +66,8 @@ template <class S> __device__ __forceinline__ S smooth01(const S& x) {
     return x * x * (S(T(3)) - S(T(2)) * x);
 }
 
-// Kerr Hamiltonian right-hand side (kerr_hamilton.h:97-155), the
-// shared-reciprocal algebra of sgx_device.cuh, generic in the scalar.
+// Kerr Hamiltonian right-hand side (kerr_hamilton.h:97-155): the reference's
+// grouping with three shared reciprocals, generic in the scalar.
 template <class S, class T>
 __device__ __forceinline__ void rhs_g(const S* y, const S& E, const S& L, const S& a, T M, S* d) {
     S st, ct;

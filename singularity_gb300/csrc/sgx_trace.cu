@@ -58,15 +58,15 @@ __device__ __forceinline__ std::uint32_t pack_meta(std::uint32_t term, std::uint
     return term | ((steps < 0x1FFFFFFFu ? steps : 0x1FFFFFFFu) << 3);
 }
 
-// Policy flags: bit 0 = shared-reciprocal Kerr RHS, bit 1 = mixed precision.
-constexpr int FL_FAST = 1;    // shared-reciprocal Kerr RHS
+// Policy flags: bit 0 = separated-form Kerr RHS, bit 1 = mixed precision.
+constexpr int FL_FAST = 1;    // separated-form Kerr RHS
 constexpr int FL_HWTRIG = 4;  // ... with the SFU sine/cosine (FP32)
 constexpr int FL_MIXED = 2;
 
 // Kerr, fixed step (geodesic_kernel.cu:303-403).
 template <class T, int FL> struct KerrFixed {
     static constexpr bool FAST = (FL & FL_FAST) != 0;
-    static constexpr int FORM = FAST ? ((FL & FL_HWTRIG) ? RHS_SHARED_HWTRIG : RHS_SHARED) : RHS_REF;
+    static constexpr int FORM = FAST ? ((FL & FL_HWTRIG) ? RHS_SEP_HWTRIG : RHS_SEP) : RHS_REF;
     KS<T> y;
     KC<T> c;
     T prev_th, prev_r;
@@ -193,7 +193,7 @@ template <class T, int FL> struct SchwFixed {
 // step() is one attempt; max_steps bounds the attempts.
 template <class T, int FL> struct KerrAdaptive {
     static constexpr bool FAST = (FL & FL_FAST) != 0;
-    static constexpr int FORM = FAST ? ((FL & FL_HWTRIG) ? RHS_SHARED_HWTRIG : RHS_SHARED) : RHS_REF;
+    static constexpr int FORM = FAST ? ((FL & FL_HWTRIG) ? RHS_SEP_HWTRIG : RHS_SEP) : RHS_REF;
     static constexpr bool MIXED = (FL & FL_MIXED) != 0;
     KS<T> y, k1;
     KC<T> c;
@@ -639,8 +639,8 @@ cudaError_t run_probe(const void* d_view, std::uint64_t n, const std::uint32_t* 
 
 // One call site per (metric, precision, integrator, RHS form): F is invoked
 // with the chosen <T, Policy, FL> as a generic lambda's template arguments.
-// rhs_form: 0 shared reciprocals, 1 the reference's divisions, 2 shared
-// reciprocals with the SFU sine/cosine (FP32; FP64 runs form 0).
+// rhs_form: 0 the separated form, 1 the reference's divisions, 2 the
+// separated form with the SFU sine/cosine (FP32; FP64 runs form 0).
 template <class F>
 cudaError_t dispatch(int metric, int precision, int integrator, int rhs_form, F&& f) {
     const bool adaptive = integrator == SGX_INTEGRATOR_ADAPTIVE;
