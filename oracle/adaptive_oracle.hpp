@@ -10,20 +10,28 @@
 // shared_shader/geodesic_math.h:91-96).  This file is the specification of the
 // adaptive form the GPU kernels implement, operation for operation:
 //
-//   * the reference's Hamiltonian right-hand side (kerr_rhs in
-//     geodesic_oracle.hpp) and the classical RK4 stages;
+//   * the reference's Hamiltonian right-hand side (kerr_rhs_sc in
+//     geodesic_oracle.hpp) and the classical RK4 stages, with theta carried
+//     as the pair (sin theta, cos theta): the state is (r, s, c, phi, p_r,
+//     p_theta) and the theta equation becomes ds = c dtheta, dc = -s dtheta
+//     (dtheta = p_theta / Sigma), so no stage evaluates a sine or cosine;
+//     after each accepted step the pair is brought back to the unit circle by
+//     one Newton step of 1/sqrt(x) at x = 1, n = 3/2 - (s^2 + c^2)/2;
 //   * a fifth, first-same-as-last stage k5 = f(y_{n+1}) giving the embedded
 //     third-order solution with weights (1/6, 1/3, 1/3, 0, 1/6); the local
 //     error estimate is (h/6)(k4 - k5), free on accepted steps because k5 is
 //     the next step's k1 (a rejected attempt costs the same four evaluations);
-//   * the max-norm over (r, theta, phi, p_r, p_theta) of that estimate scaled
+//   * the max-norm over (r, s, c, phi, p_r, p_theta) of that estimate scaled
 //     by tol * (1 + max(|y|, |y_new|)); accept when <= 1;
 //   * the step update h *= clamp(0.85 / sqrt(sqrt(err)), 0.2, 4) and the ceiling
 //     h <= h_max_frac * r — written with IEEE sqrt and division only, so a CPU
 //     and a GPU controller round identically;
-//   * equatorial crossings located on the cubic Hermite interpolant of the
-//     accepted step (values and derivatives at both ends, three Newton steps),
-//     so long steps keep the crossing radius to fourth order;
+//   * equatorial crossings: a sign change of cos(theta) with sin(theta) > 0
+//     (the reference's theta = pi/2 crossing for theta in (0, pi)), located on
+//     the cubic Hermite interpolant of cos(theta) over the accepted step
+//     (values and derivatives at both ends, three Newton steps), so long steps
+//     keep the crossing radius to fourth order; an escaped ray's sky
+//     direction is (s cos phi, s sin phi, c);
 //   * precision forms: FP32 (T = float); FP64 (T = double); and the mixed form
 //     (T = float with the constants of motion E, L_z, Q and the initial momenta
 //     computed in double from the camera ray, and — for a ray within `zone` M
@@ -97,31 +105,46 @@ inline double carter_Q(double theta, double p_theta, double E, double L, double 
 
 template <class T> inline T abs_(T x) { return x < OLIT(0.0) ? -x : x; }
 
+// State of the error-controlled form: theta carried as (sin theta, cos theta).
+template <class T> struct SCState {
+    T r, s, c, phi, p_r, p_theta;
+};
+
+template <class T> inline SCState<T> sc_add_scaled(const SCState<T>& y, const SCState<T>& k, T f) {
+    return {y.r + k.r * f, y.s + k.s * f, y.c + k.c * f, y.phi + k.phi * f, y.p_r + k.p_r * f, y.p_theta + k.p_theta * f};
+}
+
+template <class T> inline SCState<T> sc_rhs(const SCState<T>& y, const KConst<T>& c) {
+    const KState<T> k{OLIT(0.0), y.r, OLIT(0.0), y.phi, y.p_r, y.p_theta};
+    const KState<T> d = kerr_rhs_sc<T, false>(k, y.s, y.c, c);
+    return {d.r, y.c * d.theta, -(y.s * d.theta), d.phi, d.p_r, d.p_theta};
+}
+
 template <class T> struct Attempt {
-    KState<T> y4, k4, k5;
+    SCState<T> y4, k4, k5;
     T h6;
 };
 
 // RK4 stages from y with k1 = f(y) already known, and the FSAL stage.
-template <class T> inline Attempt<T> rk4_attempt(const KState<T>& y, const KState<T>& k1, T h, const KConst<T>& c) {
+template <class T> inline Attempt<T> rk4_attempt(const SCState<T>& y, const SCState<T>& k1, T h, const KConst<T>& c) {
     Attempt<T> a;
-    const KState<T> k2 = kerr_rhs(k_add_scaled(y, k1, OLIT(0.5) * h), c);
-    const KState<T> k3 = kerr_rhs(k_add_scaled(y, k2, OLIT(0.5) * h), c);
-    a.k4 = kerr_rhs(k_add_scaled(y, k3, h), c);
+    const SCState<T> k2 = sc_rhs(sc_add_scaled(y, k1, OLIT(0.5) * h), c);
+    const SCState<T> k3 = sc_rhs(sc_add_scaled(y, k2, OLIT(0.5) * h), c);
+    a.k4 = sc_rhs(sc_add_scaled(y, k3, h), c);
     a.h6 = h / OLIT(6.0);
-    a.y4.t = rk4_combine(y.t, k1.t, k2.t, k3.t, a.k4.t, a.h6);
     a.y4.r = rk4_combine(y.r, k1.r, k2.r, k3.r, a.k4.r, a.h6);
-    a.y4.theta = rk4_combine(y.theta, k1.theta, k2.theta, k3.theta, a.k4.theta, a.h6);
+    a.y4.s = rk4_combine(y.s, k1.s, k2.s, k3.s, a.k4.s, a.h6);
+    a.y4.c = rk4_combine(y.c, k1.c, k2.c, k3.c, a.k4.c, a.h6);
     a.y4.phi = rk4_combine(y.phi, k1.phi, k2.phi, k3.phi, a.k4.phi, a.h6);
     a.y4.p_r = rk4_combine(y.p_r, k1.p_r, k2.p_r, k3.p_r, a.k4.p_r, a.h6);
     a.y4.p_theta = rk4_combine(y.p_theta, k1.p_theta, k2.p_theta, k3.p_theta, a.k4.p_theta, a.h6);
-    a.k5 = kerr_rhs(a.y4, c);
+    a.k5 = sc_rhs(a.y4, c);
     return a;
 }
 
 // Scaled max-norm of the embedded estimate, evaluated in C (T or double).
 template <class C, class T>
-inline C error_norm(const KState<T>& y, const Attempt<T>& a, float tol_f) {
+inline C error_norm(const SCState<T>& y, const Attempt<T>& a, float tol_f) {
     const C tol = C(tol_f);
     const C h6 = C(a.h6);
     auto one = [&](T yv, T y4v, T k4v, T k5v) {
@@ -131,7 +154,8 @@ inline C error_norm(const KState<T>& y, const Attempt<T>& a, float tol_f) {
     };
     C e = one(y.r, a.y4.r, a.k4.r, a.k5.r);
     C t;
-    t = one(y.theta, a.y4.theta, a.k4.theta, a.k5.theta); e = t > e ? t : e;
+    t = one(y.s, a.y4.s, a.k4.s, a.k5.s); e = t > e ? t : e;
+    t = one(y.c, a.y4.c, a.k4.c, a.k5.c); e = t > e ? t : e;
     t = one(y.phi, a.y4.phi, a.k4.phi, a.k5.phi); e = t > e ? t : e;
     t = one(y.p_r, a.y4.p_r, a.k4.p_r, a.k5.p_r); e = t > e ? t : e;
     t = one(y.p_theta, a.y4.p_theta, a.k4.p_theta, a.k5.p_theta); e = t > e ? t : e;
@@ -176,15 +200,14 @@ template <class T> inline T hermite_d(T y0, T y1, T d0, T d1, T h, T s) {
     return h00 * y0 + h10 * h * d0 + h01 * y1 + h11 * h * d1;
 }
 
-// theta = pi/2 inside an accepted step: Newton on the Hermite interpolant from
-// the linear estimate, kept inside [0, 1].
+// cos(theta) = 0 inside an accepted step: Newton on the Hermite interpolant
+// from the linear estimate, kept inside [0, 1].
 template <class T>
-inline T crossing_fraction(T th0, T th1, T d0, T d1, T h) {
-    const T mid = OLIT(1.5707963267948966);
-    T s = (mid - th0) / (th1 - th0);
+inline T crossing_fraction(T c0, T c1, T d0, T d1, T h) {
+    T s = c0 / (c0 - c1);
     for (int it = 0; it < 3; ++it) {
-        const T f = hermite(th0, th1, d0, d1, h, s) - mid;
-        const T fp = hermite_d(th0, th1, d0, d1, h, s);
+        const T f = hermite(c0, c1, d0, d1, h, s);
+        const T fp = hermite_d(c0, c1, d0, d1, h, s);
         if (!(abs_(fp) > OLIT(1e-30))) break;
         T sn = s - f / fp;
         sn = sn < OLIT(0.0) ? OLIT(0.0) : (sn > OLIT(1.0) ? OLIT(1.0) : sn);
@@ -226,17 +249,18 @@ inline TraceOut<T> trace_kerr_adaptive(const CamRay<T>& cam, const Params<T>& u,
     constexpr bool is_double = std::is_same<T, double>::value;
     const V3<T> black = v3(OLIT(0.0), OLIT(0.0), OLIT(0.0));
     const bool mixed = (o.mixed != 0u) && !is_double;
-    KState<T> y;
+    KState<T> y0;
     KConst<T> c;
-    if (!kerr_init(cam, u, y, c)) return {black, 0u, TERM_NO_ROOT};
+    if (!kerr_init(cam, u, y0, c)) return {black, 0u, TERM_NO_ROOT};
     double Ed = double(c.E), Ld = double(c.L), Qd = double(c.Q), prd = 0, pthd = 0;
     if (mixed) {
         if (!kerr_init_double(cam, u, Ed, Ld, Qd, prd, pthd)) return {black, 0u, TERM_NO_ROOT};
         c.E = T(float(Ed));
         c.L = T(float(Ld));
-        y.p_r = T(float(prd));
-        y.p_theta = T(float(pthd));
+        y0.p_r = T(float(prd));
+        y0.p_theta = T(float(pthd));
     }
+    SCState<T> y{y0.r, cam.sin_th, M<T>::cos(cam.cam_theta), y0.phi, y0.p_r, y0.p_theta};
     const std::uint32_t max_steps = o.max_steps != 0u ? o.max_steps : u.max_steps;
     const T hcut = kerr_horizon_cut(u.mass_M, u.spin_a);
     const T r_plus = u.mass_M + M<T>::sqrt(M<T>::fmax(u.mass_M * u.mass_M - u.spin_a * u.spin_a, OLIT(0.0)));
@@ -244,7 +268,7 @@ inline TraceOut<T> trace_kerr_adaptive(const CamRay<T>& cam, const Params<T>& u,
     const T zone = T(o.zone);
 
     T h = T(o.h_init_frac) * y.r;
-    KState<T> k1 = kerr_rhs(y, c);
+    SCState<T> k1 = sc_rhs(y, c);
     std::uint32_t accepted = 0, rejected = 0, zone_steps = 0, steps = 0;
     TraceOut<T> out{black, max_steps, TERM_BUDGET};
     for (;;) {
@@ -257,7 +281,7 @@ inline TraceOut<T> trace_kerr_adaptive(const CamRay<T>& cam, const Params<T>& u,
             break;
         }
         if (y.r > u.escape_r) {
-            out = {(u.flags & SGX_FLAG_STARFIELD_ON) ? sky_color(y.theta, y.phi) : black, steps, TERM_ESCAPE};
+            out = {(u.flags & SGX_FLAG_STARFIELD_ON) ? sky_color_sc(y.s, y.c, y.phi) : black, steps, TERM_ESCAPE};
             break;
         }
         const T hmax = T(o.h_max_frac) * y.r;
@@ -282,10 +306,9 @@ inline TraceOut<T> trace_kerr_adaptive(const CamRay<T>& cam, const Params<T>& u,
             continue;
         }
         ++accepted;
-        const Crossing<T> x = equatorial_crossing(y.theta, at.y4.theta);
-        if ((u.flags & SGX_FLAG_DISC_ON) && x.crossed) {
+        if ((u.flags & SGX_FLAG_DISC_ON) && (y.c * at.y4.c < OLIT(0.0)) && at.y4.s > OLIT(0.0)) {
             const T hs = at.h6 * OLIT(6.0);
-            const T sfr = crossing_fraction(y.theta, at.y4.theta, k1.theta, at.k5.theta, hs);
+            const T sfr = crossing_fraction(y.c, at.y4.c, k1.c, at.k5.c, hs);
             const T r_cross = hermite(y.r, at.y4.r, k1.r, at.k5.r, hs, sfr);
             if (in_annulus(r_cross, u.r_in, u.r_out)) {
                 const T T_local = disc_temperature(r_cross, u.r_in, u.peak_T);
@@ -300,6 +323,9 @@ inline TraceOut<T> trace_kerr_adaptive(const CamRay<T>& cam, const Params<T>& u,
             }
         }
         y = at.y4;
+        const T n = OLIT(1.5) - OLIT(0.5) * (y.s * y.s + y.c * y.c);
+        y.s = y.s * n;
+        y.c = y.c * n;
         k1 = at.k5;
     }
     if (diag != nullptr) {
@@ -307,7 +333,9 @@ inline TraceOut<T> trace_kerr_adaptive(const CamRay<T>& cam, const Params<T>& u,
         diag->E = Ed;
         diag->L = Ld;
         diag->Q0 = Qd;
-        const double th = is_double ? double(y.theta) : double(float(y.theta));
+        const double sv = is_double ? double(y.s) : double(float(y.s));
+        const double cv = is_double ? double(y.c) : double(float(y.c));
+        const double th = std::atan2(sv, cv);
         const double pth = is_double ? double(y.p_theta) : double(float(y.p_theta));
         const double rr = is_double ? double(y.r) : double(float(y.r));
         const double pr = is_double ? double(y.p_r) : double(float(y.p_r));

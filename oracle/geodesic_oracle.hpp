@@ -228,11 +228,13 @@ template <class T> inline V3<T> starfield_color(V3<T> dir) {
     return vmul(v3(r, g, b), OLIT(0.6));
 }
 
+template <class T> inline V3<T> sky_color_sc(T sin_theta, T cos_theta, T phi) {
+    const T sx = sin_theta * M<T>::cos(phi);
+    const T sy = sin_theta * M<T>::sin(phi);
+    return starfield_color(v3(sx, sy, cos_theta));
+}
 template <class T> inline V3<T> sky_color(T theta, T phi) {
-    const T sx = M<T>::sin(theta) * M<T>::cos(phi);
-    const T sy = M<T>::sin(theta) * M<T>::sin(phi);
-    const T sz = M<T>::cos(theta);
-    return starfield_color(v3(sx, sy, sz));
+    return sky_color_sc(M<T>::sin(theta), M<T>::cos(theta), phi);
 }
 
 // ---------------------------------------------------------------------------
@@ -533,13 +535,14 @@ template <class T> inline T kerr_two_H(T r, T theta, T p_r, T p_theta, const KCo
     return t_tt + t_tp + t_pp + t_rr + t_th;
 }
 
-// Hamilton's equations with the analytic partials (kerr_hamilton.h:97-155).
-template <class T> inline KState<T> kerr_rhs(const KState<T>& s, const KConst<T>& c) {
+// Hamilton's equations with the analytic partials (kerr_hamilton.h:97-155),
+// with sin(theta) and cos(theta) given (the theta slot of s is not read).
+// WITH_T = false leaves dt/dlambda out (the error-controlled form drops t).
+template <class T, bool WITH_T = true>
+inline KState<T> kerr_rhs_sc(const KState<T>& s, T st, T ct, const KConst<T>& c) {
     const T r = s.r;
-    const T st = M<T>::sin(s.theta);
     const T s2 = st * st;
     const T safe_s2 = (s2 < OLIT(1e-10)) ? OLIT(1e-10) : s2;
-    const T ct = M<T>::cos(s.theta);
     const T c2 = ct * ct;
     const T r2 = r * r;
     const T a = c.a;
@@ -550,7 +553,8 @@ template <class T> inline KState<T> kerr_rhs(const KState<T>& s, const KConst<T>
     const T A = (r2 + a2) * (r2 + a2) - a2 * Delta * s2;
     const T SD = Sigma * Delta;
     KState<T> d;
-    d.t = (A * c.E - OLIT(2.0) * Mm * r * a * c.L) / SD;
+    if constexpr (WITH_T) d.t = (A * c.E - OLIT(2.0) * Mm * r * a * c.L) / SD;
+    else d.t = OLIT(0.0);
     d.phi = (OLIT(2.0) * Mm * r * a * c.E * s2 + (Delta - a2 * s2) * c.L) / (SD * safe_s2);
     d.r = Delta * s.p_r / Sigma;
     d.theta = s.p_theta / Sigma;
@@ -576,6 +580,12 @@ template <class T> inline KState<T> kerr_rhs(const KState<T>& s, const KConst<T>
     d.p_r = OLIT(-0.5) * dH_dr;
     d.p_theta = OLIT(-0.5) * dH_dth;
     return d;
+}
+
+template <class T> inline KState<T> kerr_rhs(const KState<T>& s, const KConst<T>& c) {
+    const T st = M<T>::sin(s.theta);
+    const T ct = M<T>::cos(s.theta);
+    return kerr_rhs_sc(s, st, ct, c);
 }
 
 // Near-pole step damping: h * clamp(5|sin theta|, 0.05, 1) (kerr_hamilton.h:165-170).

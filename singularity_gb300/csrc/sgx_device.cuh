@@ -295,10 +295,9 @@ __device__ __forceinline__ std::uint32_t star_hash(std::uint32_t ix, std::uint32
     return x;
 }
 
-// Sky colour for an escaped ray at (theta, phi): the starfield of
-// geodesic_kernel.cu:135-171 applied to the direction at the last state.
-template <class T> __device__ inline V3<T> sky_color(T theta, T phi) {
-    const T st = DM<T>::sin_(theta), ct = DM<T>::cos_(theta);
+// Sky colour for an escaped ray with (sin theta, cos theta, phi) at its last
+// state: the starfield of geodesic_kernel.cu:135-171 in that direction.
+template <class T> __device__ inline V3<T> sky_color_sc(T st, T ct, T phi) {
     const V3<T> dir = mk3(st * DM<T>::cos_(phi), st * DM<T>::sin_(phi), ct);
     const T len = DM<T>::sqrt_(dot3(dir, dir));
     if (len < DLIT(1e-6)) return mk3(DLIT(0.0), DLIT(0.0), DLIT(0.005));
@@ -410,10 +409,10 @@ template <class T> __device__ __forceinline__ KC<T> make_kc(const View<T>& v, T 
     return c;
 }
 
-// The reference's expression, division for division.
-template <class T> __device__ __forceinline__ KS<T> kerr_rhs_ref(const KS<T>& s, const View<T>& v, const KC<T>& c) {
-    T st, ct;
-    DM<T>::sincos_(s.th, &st, &ct);
+// The reference's expression, division for division, with sin(theta) and
+// cos(theta) given.
+template <class T>
+__device__ __forceinline__ KS<T> kerr_rhs_ref_sc(const KS<T>& s, T st, T ct, const View<T>& v, const KC<T>& c) {
     const T r = s.r;
     const T s2 = st * st;
     const T safe_s2 = (s2 < DLIT(1e-10)) ? DLIT(1e-10) : s2;
@@ -446,6 +445,12 @@ template <class T> __device__ __forceinline__ KS<T> kerr_rhs_ref(const KS<T>& s,
     d.pr = DLIT(-0.5) * dH_dr;
     d.pth = DLIT(-0.5) * dH_dth;
     return d;
+}
+
+template <class T> __device__ __forceinline__ KS<T> kerr_rhs_ref(const KS<T>& s, const View<T>& v, const KC<T>& c) {
+    T st, ct;
+    DM<T>::sincos_(s.th, &st, &ct);
+    return kerr_rhs_ref_sc(s, st, ct, v, c);
 }
 
 // The same Hamiltonian in Carter's separated form (Carter 1968), with three
@@ -668,46 +673,71 @@ template <class T> __device__ __forceinline__ bool crossed_equator(T th_prev, T 
     return x;
 }
 
-// Sign change of theta - pi/2 across a step, without the crossing fraction.
-template <class T> __device__ __forceinline__ bool crosses_plane(T th_prev, T th_curr) {
-    const T mid = DLIT(1.5707963267948966);
-    return ((th_prev - mid) * (th_curr - mid)) < DLIT(0.0);
-}
-
 // ---------------------------------------------------------------------------
 // Error-controlled Kerr integration (the adaptive extension; the CPU oracle's
-// adaptive_oracle.hpp is its specification, operation for operation).
+// adaptive_oracle.hpp is its specification, operation for operation).  theta
+// is carried as (sin theta, cos theta): ds = c dtheta, dc = -s dtheta, so no
+// stage evaluates a sine or cosine.
 // ---------------------------------------------------------------------------
+template <class T> struct KSC {
+    T r, s, c, ph, pr, pth;
+};
+
+template <class T> __device__ __forceinline__ KSC<T> ksc_axpy(const KSC<T>& y, const KSC<T>& k, T f) {
+    return KSC<T>{y.r + k.r * f, y.s + k.s * f, y.c + k.c * f, y.ph + k.ph * f, y.pr + k.pr * f, y.pth + k.pth * f};
+}
+
+template <class T, int FORM>
+__device__ __forceinline__ KSC<T> kerr_rhs_scs(const KSC<T>& y, const View<T>& v, const KC<T>& c) {
+    const KS<T> k{y.r, DLIT(0.0), y.ph, y.pr, y.pth};
+    KS<T> d;
+    if constexpr (FORM != RHS_REF) d = kerr_rhs_sep_sc(k, y.s, y.c, v, c);
+    else d = kerr_rhs_ref_sc(k, y.s, y.c, v, c);
+    return KSC<T>{d.r, y.c * d.th, -(y.s * d.th), d.ph, d.pr, d.pth};
+}
+
+// (s, c) back to the unit circle after an accepted step: one Newton step of
+// 1/sqrt(x) at x = 1 (s^2 + c^2 stays within ~1e-6 of 1 between steps).
+template <class T> __device__ __forceinline__ void renormalise(KSC<T>& y) {
+    const T n = DLIT(1.5) - DLIT(0.5) * (y.s * y.s + y.c * y.c);
+    y.s = y.s * n;
+    y.c = y.c * n;
+}
+
 template <class T> struct KAttempt {
-    KS<T> y4, k4, k5;
+    KSC<T> y4, k4, k5;
     T h6;
 };
 
 // RK4 stages from y with k1 = f(y) known, plus the first-same-as-last stage.
 template <class T, int FORM>
-__device__ __forceinline__ KAttempt<T> kerr_attempt(const KS<T>& y, const KS<T>& k1, T h, const View<T>& v,
+__device__ __forceinline__ KAttempt<T> kerr_attempt(const KSC<T>& y, const KSC<T>& k1, T h, const View<T>& v,
                                                     const KC<T>& c) {
     KAttempt<T> at;
     const T hh = DLIT(0.5) * h;
-    const KS<T> k2 = kerr_rhs<T, FORM>(ks_axpy(y, k1, hh), v, c);
-    const KS<T> k3 = kerr_rhs<T, FORM>(ks_axpy(y, k2, hh), v, c);
-    at.k4 = kerr_rhs<T, FORM>(ks_axpy(y, k3, h), v, c);
+    const KSC<T> k2 = kerr_rhs_scs<T, FORM>(ksc_axpy(y, k1, hh), v, c);
+    const KSC<T> k3 = kerr_rhs_scs<T, FORM>(ksc_axpy(y, k2, hh), v, c);
+    at.k4 = kerr_rhs_scs<T, FORM>(ksc_axpy(y, k3, h), v, c);
     at.h6 = h / DLIT(6.0);
-    at.y4.r = y.r + ((k1.r + k2.r * DLIT(2.0)) + (k3.r * DLIT(2.0) + at.k4.r)) * at.h6;
-    at.y4.th = y.th + ((k1.th + k2.th * DLIT(2.0)) + (k3.th * DLIT(2.0) + at.k4.th)) * at.h6;
-    at.y4.ph = y.ph + ((k1.ph + k2.ph * DLIT(2.0)) + (k3.ph * DLIT(2.0) + at.k4.ph)) * at.h6;
-    at.y4.pr = y.pr + ((k1.pr + k2.pr * DLIT(2.0)) + (k3.pr * DLIT(2.0) + at.k4.pr)) * at.h6;
-    at.y4.pth = y.pth + ((k1.pth + k2.pth * DLIT(2.0)) + (k3.pth * DLIT(2.0) + at.k4.pth)) * at.h6;
-    at.k5 = kerr_rhs<T, FORM>(at.y4, v, c);
+    auto comb = [&](T y0, T a1, T a2, T a3, T a4) {
+        return y0 + ((a1 + a2 * DLIT(2.0)) + (a3 * DLIT(2.0) + a4)) * at.h6;
+    };
+    at.y4.r = comb(y.r, k1.r, k2.r, k3.r, at.k4.r);
+    at.y4.s = comb(y.s, k1.s, k2.s, k3.s, at.k4.s);
+    at.y4.c = comb(y.c, k1.c, k2.c, k3.c, at.k4.c);
+    at.y4.ph = comb(y.ph, k1.ph, k2.ph, k3.ph, at.k4.ph);
+    at.y4.pr = comb(y.pr, k1.pr, k2.pr, k3.pr, at.k4.pr);
+    at.y4.pth = comb(y.pth, k1.pth, k2.pth, k3.pth, at.k4.pth);
+    at.k5 = kerr_rhs_scs<T, FORM>(at.y4, v, c);
     return at;
 }
 
 template <class C> __device__ __forceinline__ C absv(C x) { return x < C(0.0f) ? -x : x; }
 
-// max_i |h/6 (k4_i - k5_i)| / (tol (1 + max(|y_i|, |y4_i|))) over r, theta,
-// phi, p_r, p_theta, evaluated in C; NaN/overflow -> 1e30.
+// max_i |h/6 (k4_i - k5_i)| / (tol (1 + max(|y_i|, |y4_i|))) over r, sin theta,
+// cos theta, phi, p_r, p_theta, evaluated in C; NaN/overflow -> 1e30.
 template <class C, class T>
-__device__ __forceinline__ C error_norm(const KS<T>& y, const KAttempt<T>& a, float tol_f) {
+__device__ __forceinline__ C error_norm(const KSC<T>& y, const KAttempt<T>& a, float tol_f) {
     const C tol = C(tol_f);
     const C h6 = C(a.h6);
     auto one = [&](T yv, T y4v, T k4v, T k5v) {
@@ -717,7 +747,9 @@ __device__ __forceinline__ C error_norm(const KS<T>& y, const KAttempt<T>& a, fl
     };
     C e = one(y.r, a.y4.r, a.k4.r, a.k5.r);
     C t;
-    t = one(y.th, a.y4.th, a.k4.th, a.k5.th);
+    t = one(y.s, a.y4.s, a.k4.s, a.k5.s);
+    e = t > e ? t : e;
+    t = one(y.c, a.y4.c, a.k4.c, a.k5.c);
     e = t > e ? t : e;
     t = one(y.ph, a.y4.ph, a.k4.ph, a.k5.ph);
     e = t > e ? t : e;
@@ -733,13 +765,14 @@ __device__ __forceinline__ C error_norm(const KS<T>& y, const KAttempt<T>& a, fl
 // scale at the end: max_i |k4_i - k5_i| / (1 + max(|y_i|, |y4_i|)) * |h/6| / tol.
 // Equal to error_norm up to rounding (a few ulp), for the FP32 fast path.
 template <class T>
-__device__ __forceinline__ T error_norm_fast(const KS<T>& y, const KAttempt<T>& a, float tol_f) {
+__device__ __forceinline__ T error_norm_fast(const KSC<T>& y, const KAttempt<T>& a, float tol_f) {
     auto one = [&](T yv, T y4v, T k4v, T k5v) {
         const T m = DM<T>::fmax_(absv(yv), absv(y4v));
         return absv(k4v - k5v) * DM<T>::rcp_fast(DLIT(1.0) + m);
     };
     T e = one(y.r, a.y4.r, a.k4.r, a.k5.r);
-    e = DM<T>::fmax_(e, one(y.th, a.y4.th, a.k4.th, a.k5.th));
+    e = DM<T>::fmax_(e, one(y.s, a.y4.s, a.k4.s, a.k5.s));
+    e = DM<T>::fmax_(e, one(y.c, a.y4.c, a.k4.c, a.k5.c));
     e = DM<T>::fmax_(e, one(y.ph, a.y4.ph, a.k4.ph, a.k5.ph));
     e = DM<T>::fmax_(e, one(y.pr, a.y4.pr, a.k4.pr, a.k5.pr));
     e = DM<T>::fmax_(e, one(y.pth, a.y4.pth, a.k4.pth, a.k5.pth));
@@ -783,15 +816,14 @@ template <class T> __device__ __forceinline__ T hermite_d(T y0, T y1, T d0, T d1
     return h00 * y0 + h10 * h * d0 + h01 * y1 + h11 * h * d1;
 }
 
-// theta = pi/2 inside an accepted step: three Newton steps on the Hermite
+// cos(theta) = 0 inside an accepted step: three Newton steps on the Hermite
 // interpolant from the linear estimate, clamped to [0, 1].
-template <class T> __device__ __forceinline__ T crossing_fraction(T th0, T th1, T d0, T d1, T h) {
-    const T mid = DLIT(1.5707963267948966);
-    T s = (mid - th0) / (th1 - th0);
+template <class T> __device__ __forceinline__ T crossing_fraction(T c0, T c1, T d0, T d1, T h) {
+    T s = c0 / (c0 - c1);
 #pragma unroll 1
     for (int it = 0; it < 3; ++it) {
-        const T f = hermite(th0, th1, d0, d1, h, s) - mid;
-        const T fp = hermite_d(th0, th1, d0, d1, h, s);
+        const T f = hermite(c0, c1, d0, d1, h, s);
+        const T fp = hermite_d(c0, c1, d0, d1, h, s);
         if (!(absv(fp) > DLIT(1e-30))) break;
         T sn = s - f / fp;
         sn = sn < DLIT(0.0) ? DLIT(0.0) : (sn > DLIT(1.0) ? DLIT(1.0) : sn);
@@ -826,7 +858,7 @@ template <class T> __device__ __forceinline__ T photon_orbit_radius(const View<T
 // cross-multiplied comparisons, then divided once (the value equals the max
 // of the ratios up to the choice among ratios equal to rounding).
 template <class T>
-__device__ __forceinline__ double error_norm_fp64_1div(const KS<T>& y, const KAttempt<T>& a, float tol_f) {
+__device__ __forceinline__ double error_norm_fp64_1div(const KSC<T>& y, const KAttempt<T>& a, float tol_f) {
     const double tol = tol_f, h6 = a.h6;
     double num = 0.0, den = 1.0;
     auto one = [&](T yv, T y4v, T k4v, T k5v) {
@@ -839,7 +871,8 @@ __device__ __forceinline__ double error_norm_fp64_1div(const KS<T>& y, const KAt
         }
     };
     one(y.r, a.y4.r, a.k4.r, a.k5.r);
-    one(y.th, a.y4.th, a.k4.th, a.k5.th);
+    one(y.s, a.y4.s, a.k4.s, a.k5.s);
+    one(y.c, a.y4.c, a.k4.c, a.k5.c);
     one(y.ph, a.y4.ph, a.k4.ph, a.k5.ph);
     one(y.pr, a.y4.pr, a.k4.pr, a.k5.pr);
     one(y.pth, a.y4.pth, a.k4.pth, a.k5.pth);

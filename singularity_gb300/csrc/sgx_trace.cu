@@ -99,8 +99,9 @@ template <class T, int FL> struct KerrFixed {
         }
         if (y.r > v.escape_r) {
             term = TERM_ESCAPE;
-            t0 = y.th;
+            t0 = DM<T>::sin_(y.th);
             t1 = y.ph;
+            t2 = DM<T>::cos_(y.th);
             return true;
         }
         T frac;
@@ -156,8 +157,9 @@ template <class T, int FL> struct SchwFixed {
         }
         if (y.r > v.escape_r) {
             term = TERM_ESCAPE;
-            t0 = y.th;
+            t0 = DM<T>::sin_(y.th);
             t1 = y.ph;
+            t2 = DM<T>::cos_(y.th);
             return true;
         }
         T frac;
@@ -195,7 +197,7 @@ template <class T, int FL> struct KerrAdaptive {
     static constexpr bool FAST = (FL & FL_FAST) != 0;
     static constexpr int FORM = FAST ? ((FL & FL_HWTRIG) ? RHS_SEP_HWTRIG : RHS_SEP) : RHS_REF;
     static constexpr bool MIXED = (FL & FL_MIXED) != 0;
-    KS<T> y, k1;
+    KSC<T> y, k1;  // theta carried as (sin theta, cos theta)
     KC<T> c;
     T h, r_c;
     T t0, t1, t2;
@@ -204,10 +206,12 @@ template <class T, int FL> struct KerrAdaptive {
     __device__ __forceinline__ bool init(const View<T>& v, const CamDir<T>& cd, const PassDesc& pass) {
         steps = rej = zone = 0;
         T E, L;
-        if (!kerr_init(v, cd, y, E, L)) {
+        KS<T> y0;
+        if (!kerr_init(v, cd, y0, E, L)) {
             term = TERM_NO_ROOT;
             return false;
         }
+        y = KSC<T>{y0.r, v.sin_th, v.cos_th, y0.ph, y0.pr, y0.pth};
         if constexpr (MIXED) {
             double Ed, Ld, prd, pthd;
             if (!kerr_init_fp64_constants(v, cd, Ed, Ld, prd, pthd)) {
@@ -224,7 +228,7 @@ template <class T, int FL> struct KerrAdaptive {
         }
         c = make_kc(v, E, L);
         h = T(pass.h_init_frac) * y.r;
-        k1 = kerr_rhs<T, FORM>(y, v, c);
+        k1 = kerr_rhs_scs<T, FORM>(y, v, c);
         if (v.max_steps == 0u) {
             term = TERM_BUDGET;
             return false;
@@ -239,8 +243,9 @@ template <class T, int FL> struct KerrAdaptive {
         }
         if (y.r > v.escape_r) {
             term = TERM_ESCAPE;
-            t0 = y.th;
+            t0 = y.s;
             t1 = y.ph;
+            t2 = y.c;
             return true;
         }
         const T hmax = T(pass.h_max_frac) * y.r;
@@ -270,9 +275,10 @@ template <class T, int FL> struct KerrAdaptive {
         if (!accept) {
             ++rej;
         } else {
-            if ((v.flags & SGX_FLAG_DISC_ON) && crosses_plane(y.th, at.y4.th)) {
+            // theta = pi/2 for theta in (0, pi): cos(theta) changes sign with sin(theta) > 0
+            if ((v.flags & SGX_FLAG_DISC_ON) && (y.c * at.y4.c < DLIT(0.0)) && at.y4.s > DLIT(0.0)) {
                 const T hs = at.h6 * DLIT(6.0);
-                const T sfr = crossing_fraction(y.th, at.y4.th, k1.th, at.k5.th, hs);
+                const T sfr = crossing_fraction(y.c, at.y4.c, k1.c, at.k5.c, hs);
                 const T r_cross = hermite(y.r, at.y4.r, k1.r, at.k5.r, hs, sfr);
                 if (r_cross >= v.r_in && r_cross <= v.r_out) {
                     const T T_local = disc_temperature(r_cross, v.r_in, v.peak_T);
@@ -285,6 +291,7 @@ template <class T, int FL> struct KerrAdaptive {
                 }
             }
             y = at.y4;
+            renormalise(y);
             k1 = at.k5;
         }
         if (steps >= v.max_steps) {
@@ -301,7 +308,7 @@ template <class T, int FL> struct KerrAdaptive {
 // an escape, disc emission for a hot crossing, black otherwise.
 template <class T> __device__ __forceinline__ V3<T> shade_record(const View<T>& v, const Rec<T>& r) {
     const std::uint32_t term = r.meta & 7u;
-    if (term == TERM_ESCAPE && (v.flags & SGX_FLAG_STARFIELD_ON)) return sky_color(r.t0, r.t1);
+    if (term == TERM_ESCAPE && (v.flags & SGX_FLAG_STARFIELD_ON)) return sky_color_sc(r.t0, r.t2, r.t1);
     if (term == TERM_DISC) {
         const T T_local = disc_temperature(r.t0, v.r_in, v.peak_T);
         if (v.metric == SGX_METRIC_KERR) return kerr_disc(v, r.t2, r.t0, r.t1, T_local);
@@ -649,13 +656,13 @@ cudaError_t dispatch(int metric, int precision, int integrator, int rhs_form, F&
         if (precision == SGX_PRECISION_FP64)
             return ref ? f.template operator()<double, KerrAdaptive, 0>()
                        : f.template operator()<double, KerrAdaptive, FL_FAST>();
+        // the error-controlled form evaluates no sine or cosine per stage, so
+        // forms 0 and 2 are the same kernel
         if (precision == SGX_PRECISION_MIXED)
-            return ref  ? f.template operator()<float, KerrAdaptive, FL_MIXED>()
-                   : hw ? f.template operator()<float, KerrAdaptive, FL_FAST | FL_MIXED | FL_HWTRIG>()
-                        : f.template operator()<float, KerrAdaptive, FL_FAST | FL_MIXED>();
-        return ref  ? f.template operator()<float, KerrAdaptive, 0>()
-               : hw ? f.template operator()<float, KerrAdaptive, FL_FAST | FL_HWTRIG>()
-                    : f.template operator()<float, KerrAdaptive, FL_FAST>();
+            return ref ? f.template operator()<float, KerrAdaptive, FL_MIXED>()
+                       : f.template operator()<float, KerrAdaptive, FL_FAST | FL_MIXED>();
+        return ref ? f.template operator()<float, KerrAdaptive, 0>()
+                   : f.template operator()<float, KerrAdaptive, FL_FAST>();
     }
     if (metric == SGX_METRIC_KERR) {
         if (precision == SGX_PRECISION_FP64)
