@@ -73,7 +73,8 @@ typedef struct sgx_render_opts {
     float fp64_zone;         /* mixed: FP64 control band half-width in M (default 0.05) */
     uint32_t sample_begin;   /* first Halton sample of this pass (default 0) */
     uint32_t sample_count;   /* samples in this pass; 0 = all remaining (default 0) */
-    uint32_t block_threads;  /* launch shape: threads per block; 0 = tuned default */
+    uint32_t block_threads;  /* launch shape: threads per block, a multiple of 32 up to 256;
+                                0 = tuned default */
     uint32_t blocks_per_sm;  /* launch shape: resident blocks per SM; 0 = occupancy limit */
     uint32_t refill_interval;/* steps between warp refills of finished rays; 0 = 32 */
     uint32_t rhs_form;       /* Kerr right-hand side: 0 = the same Hamiltonian in Carter's

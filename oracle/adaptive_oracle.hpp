@@ -24,8 +24,9 @@
 //   * the max-norm over (r, s, c, phi, p_r, p_theta) of that estimate scaled
 //     by tol * (1 + max(|y|, |y_new|)); accept when <= 1;
 //   * the step update h *= clamp(0.85 / sqrt(sqrt(err)), 0.2, 4) and the ceiling
-//     h <= h_max_frac * r — written with IEEE sqrt and division only, so a CPU
-//     and a GPU controller round identically;
+//     h <= h_max_frac * r, written with IEEE sqrt and division (the GPU's FP32
+//     path evaluates the same factor as 0.85 * 2^(-log2(err)/4) on its
+//     special-function unit, so its step sizes differ in the last bits);
 //   * equatorial crossings: a sign change of cos(theta) with sin(theta) > 0
 //     (the reference's theta = pi/2 crossing for theta in (0, pi)), located on
 //     the cubic Hermite interpolant of cos(theta) over the accepted step
@@ -131,7 +132,7 @@ template <class T> inline Attempt<T> rk4_attempt(const SCState<T>& y, const SCSt
     const SCState<T> k2 = sc_rhs(sc_add_scaled(y, k1, OLIT(0.5) * h), c);
     const SCState<T> k3 = sc_rhs(sc_add_scaled(y, k2, OLIT(0.5) * h), c);
     a.k4 = sc_rhs(sc_add_scaled(y, k3, h), c);
-    a.h6 = h / OLIT(6.0);
+    a.h6 = h * OLIT(0.16666666666666666);  // h/6 as a product (no division per attempt)
     a.y4.r = rk4_combine(y.r, k1.r, k2.r, k3.r, a.k4.r, a.h6);
     a.y4.s = rk4_combine(y.s, k1.s, k2.s, k3.s, a.k4.s, a.h6);
     a.y4.c = rk4_combine(y.c, k1.c, k2.c, k3.c, a.k4.c, a.h6);

@@ -99,6 +99,9 @@ sgx_status check_opts(sgx_context* c, const sgx_render_opts& o) {
     if (o.integrator > SGX_INTEGRATOR_ADAPTIVE) return fail(c, SGX_ERR_INVALID_ARGUMENT, "unknown integrator");
     if (o.format > SGX_FORMAT_RGBA16F_HDR) return fail(c, SGX_ERR_INVALID_ARGUMENT, "unknown format");
     if (o.rhs_form > 2) return fail(c, SGX_ERR_INVALID_ARGUMENT, "unknown rhs_form");
+    // the tracer's warp votes assume whole warps, and its launch bounds 256 threads
+    if (o.block_threads != 0 && (o.block_threads % 32u != 0 || o.block_threads > 256u))
+        return fail(c, SGX_ERR_INVALID_ARGUMENT, "block_threads must be 0 or a multiple of 32 up to 256");
     if ((o.tile_w == 0) != (o.tile_h == 0) || o.tile_w > 4096 || o.tile_h > 4096)
         return fail(c, SGX_ERR_INVALID_ARGUMENT, "tile_w and tile_h must both be 0 or both in [1, 4096]");
     if (o.integrator == SGX_INTEGRATOR_ADAPTIVE) {

@@ -718,7 +718,7 @@ __device__ __forceinline__ KAttempt<T> kerr_attempt(const KSC<T>& y, const KSC<T
     const KSC<T> k2 = kerr_rhs_scs<T, FORM>(ksc_axpy(y, k1, hh), v, c);
     const KSC<T> k3 = kerr_rhs_scs<T, FORM>(ksc_axpy(y, k2, hh), v, c);
     at.k4 = kerr_rhs_scs<T, FORM>(ksc_axpy(y, k3, h), v, c);
-    at.h6 = h / DLIT(6.0);
+    at.h6 = h * DLIT(0.16666666666666666);  // h/6 as a product (the oracle alike)
     auto comb = [&](T y0, T a1, T a2, T a3, T a4) {
         return y0 + ((a1 + a2 * DLIT(2.0)) + (a3 * DLIT(2.0) + a4)) * at.h6;
     };
@@ -732,7 +732,10 @@ __device__ __forceinline__ KAttempt<T> kerr_attempt(const KSC<T>& y, const KSC<T
     return at;
 }
 
-template <class C> __device__ __forceinline__ C absv(C x) { return x < C(0.0f) ? -x : x; }
+// |x| as an operand modifier (a compare-and-select would cost two instructions;
+// the two differ only in the sign of a zero result).
+__device__ __forceinline__ float absv(float x) { return fabsf(x); }
+__device__ __forceinline__ double absv(double x) { return fabs(x); }
 
 // max_i |h/6 (k4_i - k5_i)| / (tol (1 + max(|y_i|, |y4_i|))) over r, sin theta,
 // cos theta, phi, p_r, p_theta, evaluated in C; NaN/overflow -> 1e30.
@@ -790,13 +793,16 @@ template <class C> __device__ __forceinline__ C step_factor(C e) {
     return f;
 }
 
-// The same factor from one square root and one approximate reciprocal square root.
+// The same factor as 0.85 * 2^(-log2(e) / 4) from the SFU's base-2
+// logarithm and exponential (PTX lg2.approx / ex2.approx, relative error
+// ~2^-22 over the range e takes), clamped without branches.
 __device__ __forceinline__ float step_factor_fast(float e) {
-    if (e <= 1e-30f) return 4.0f;
-    float f = 0.85f * rsqrtf(sqrtf(e));
-    f = f < 0.2f ? 0.2f : f;
-    f = f > 4.0f ? 4.0f : f;
-    return f;
+    float l, p;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(l) : "f"(e));
+    const float x = -0.25f * l;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(p) : "f"(x));
+    const float f = fminf(fmaxf(0.85f * p, 0.2f), 4.0f);
+    return e <= 1e-30f ? 4.0f : f;
 }
 
 template <class T> __device__ __forceinline__ T hermite(T y0, T y1, T d0, T d1, T h, T s) {

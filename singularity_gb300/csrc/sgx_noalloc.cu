@@ -116,6 +116,10 @@ extern "C" sgx_status sgx_render_noalloc(const sgx_uniforms* u, const sgx_render
         set_err(err, err_len, "sgx_render_noalloc: fixed-step integrator and RGBA8/RGBA32F output only");
         return SGX_ERR_INVALID_ARGUMENT;
     }
+    if (o.block_threads != 0 && (o.block_threads % 32u != 0 || o.block_threads > 256u)) {
+        set_err(err, err_len, "sgx_render_noalloc: block_threads must be 0 or a multiple of 32 up to 256");
+        return SGX_ERR_INVALID_ARGUMENT;
+    }
     const std::uint32_t spp = u->supersample < 1u ? 1u : (u->supersample > 1024u ? 1024u : u->supersample);
     if (o.sample_begin != 0 || (o.sample_count != 0 && o.sample_count != spp)) {
         set_err(err, err_len, "sgx_render_noalloc: renders whole frames only (sample_begin 0, all samples)");

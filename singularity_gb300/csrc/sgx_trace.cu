@@ -65,6 +65,7 @@ constexpr int FL_MIXED = 2;
 
 // Kerr, fixed step (geodesic_kernel.cu:303-403).
 template <class T, int FL> struct KerrFixed {
+    static constexpr int kMinBlocks = sizeof(T) == 4 ? 4 : 1;
     static constexpr bool FAST = (FL & FL_FAST) != 0;
     static constexpr int FORM = FAST ? ((FL & FL_HWTRIG) ? RHS_SEP_HWTRIG : RHS_SEP) : RHS_REF;
     KS<T> y;
@@ -131,6 +132,7 @@ template <class T, int FL> struct KerrFixed {
 
 // Schwarzschild, fixed step (geodesic_kernel.cu:229-297).
 template <class T, int FL> struct SchwFixed {
+    static constexpr int kMinBlocks = sizeof(T) == 4 ? 4 : 1;
     SS<T> y;
     T prev_th, prev_r, prev_uph;
     T t0, t1, t2;
@@ -197,6 +199,7 @@ template <class T, int FL> struct KerrAdaptive {
     static constexpr bool FAST = (FL & FL_FAST) != 0;
     static constexpr int FORM = FAST ? ((FL & FL_HWTRIG) ? RHS_SEP_HWTRIG : RHS_SEP) : RHS_REF;
     static constexpr bool MIXED = (FL & FL_MIXED) != 0;
+    static constexpr int kMinBlocks = sizeof(T) == 4 ? (MIXED ? 4 : 4) : 1;
     KSC<T> y, k1;  // theta carried as (sin theta, cos theta)
     KC<T> c;
     T h, r_c;
@@ -248,8 +251,7 @@ template <class T, int FL> struct KerrAdaptive {
             t2 = y.c;
             return true;
         }
-        const T hmax = T(pass.h_max_frac) * y.r;
-        h = h > hmax ? hmax : h;
+        h = DM<T>::fmin_(h, T(pass.h_max_frac) * y.r);
         const KAttempt<T> at = kerr_attempt<T, FORM>(y, k1, h, v, c);
         ++steps;
         bool accept;
@@ -408,19 +410,20 @@ enum : int { MODE_IDLE = 0, MODE_ACTIVE = 1, MODE_DONE = 2 };
 // The persistent tracer over a set of views.  Ray ids enumerate, view by
 // view, tiles of tile_w x tile_h pixels (padded to whole tiles), the pixels
 // of a tile row-major, and a pixel's samples innermost; ids that land in the
-// padding carry no work.  FP32 variants are held to 64 registers (4 blocks of
-// 256 per SM): the precision form would otherwise take 80 and 3 blocks for
-// its few FP64 temporaries (1.5 % faster capped); FP64 variants keep their
-// registers (capped they spill up to 1.4 KB).
-template <class T> struct TraceMinBlocks {
-    static constexpr int value = sizeof(T) == 4 ? 4 : 1;
-};
+// padding carry no work.  Each policy names its resident blocks of 256 per
+// SM (kMinBlocks), which caps its registers: 4 = 64 registers, 3 = 80;
+// FP64 variants keep their registers (capped they spill up to 1.4 KB).
 template <class T, class Ray>
-__global__ void __launch_bounds__(256, TraceMinBlocks<T>::value) trace_persistent(PassDesc pass) {
+__global__ void __launch_bounds__(256, Ray::kMinBlocks) trace_persistent(PassDesc pass) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    // Block totals of the ray counters and each lane's record slot live in
+    // shared memory, not in registers held across the integration loop.
+    __shared__ unsigned long long s_count[5];  // steps, rejected, zone steps, budget hits, rays
+    __shared__ std::uint64_t s_rec[256];
     const ViewSet& vs = pass.vs;
     const SmemSet<T> m = carve<T>(smem_raw, vs.n, vs.max_S);
     load_set(m, vs, true);
+    if (threadIdx.x < 5u) s_count[threadIdx.x] = 0ull;
     __syncthreads();
     Rec<T>* __restrict__ results = static_cast<Rec<T>*>(pass.results);
 
@@ -429,19 +432,17 @@ __global__ void __launch_bounds__(256, TraceMinBlocks<T>::value) trace_persisten
     Ray ray;
     int mode = MODE_IDLE;
     std::uint32_t vid = 0;
-    std::uint64_t rec = 0;
     bool exhausted = false;
-    unsigned long long my_steps = 0, my_budget = 0, my_rays = 0, my_rej = 0, my_zone = 0;
 
     for (;;) {
         // 1. store the hit records of rays that ended.
         if (mode == MODE_DONE) {
-            results[rec] = ray.record();
-            my_steps += ray.steps;
-            my_rej += ray.rej;
-            my_zone += ray.zone;
-            my_budget += (ray.term == TERM_BUDGET) ? 1ull : 0ull;
-            my_rays += 1ull;
+            results[s_rec[threadIdx.x]] = ray.record();
+            atomicAdd(&s_count[0], (unsigned long long)ray.steps);
+            if (ray.rej != 0u) atomicAdd(&s_count[1], (unsigned long long)ray.rej);
+            if (ray.zone != 0u) atomicAdd(&s_count[2], (unsigned long long)ray.zone);
+            if (ray.term == TERM_BUDGET) atomicAdd(&s_count[3], 1ull);
+            atomicAdd(&s_count[4], 1ull);
             mode = MODE_IDLE;
         }
         // 2. refill idle lanes from the queue, one atomic per warp.
@@ -474,8 +475,8 @@ __global__ void __launch_bounds__(256, TraceMinBlocks<T>::value) trace_persisten
                         const std::uint32_t gx = (tile - ty * tiles_x) * tw + (within - wy * tw);
                         const std::uint32_t gy = ty * th + wy;
                         if (gx < v.width && gy < v.height) {
-                            rec = m.rec_off[vid] + std::uint64_t(sl) * (std::uint64_t(v.width) * v.height) +
-                                  std::uint64_t(gy) * v.width + gx;
+                            s_rec[threadIdx.x] = m.rec_off[vid] + std::uint64_t(sl) * (std::uint64_t(v.width) * v.height) +
+                                                 std::uint64_t(gy) * v.width + gx;
                             const T ox = v.spp == 1u ? DLIT(0.5) : m.off_x[sl];
                             const T oy = v.spp == 1u ? DLIT(0.5) : m.off_y[sl];
                             const CamDir<T> cd = camera_dir(v, gx, gy, ox, oy);
@@ -497,11 +498,14 @@ __global__ void __launch_bounds__(256, TraceMinBlocks<T>::value) trace_persisten
             if (__all_sync(kFull, mode != MODE_ACTIVE)) break;
         }
     }
-    warp_add(&pass.counters->steps, my_steps);
-    warp_add(&pass.counters->rejected, my_rej);
-    warp_add(&pass.counters->zone_steps, my_zone);
-    warp_add(&pass.counters->budget_hits, my_budget);
-    warp_add(&pass.counters->rays, my_rays);
+    __syncthreads();
+    if (threadIdx.x == 0u) {
+        if (s_count[0] != 0ull) atomicAdd(&pass.counters->steps, s_count[0]);
+        if (s_count[1] != 0ull) atomicAdd(&pass.counters->rejected, s_count[1]);
+        if (s_count[2] != 0ull) atomicAdd(&pass.counters->zone_steps, s_count[2]);
+        if (s_count[3] != 0ull) atomicAdd(&pass.counters->budget_hits, s_count[3]);
+        if (s_count[4] != 0ull) atomicAdd(&pass.counters->rays, s_count[4]);
+    }
 }
 
 template <class T, class Ray>

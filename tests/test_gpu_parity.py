@@ -174,6 +174,10 @@ def test_errors_are_status_codes(renderer, sgx):
     assert e.value.status == 1
     with pytest.raises(sgx.SgxError):
         renderer.render(u, sgx.default_opts(tile_w=8, tile_h=0))
+    for bt in (100, 288):  # partial warps / beyond the tracer's 256-thread bound
+        with pytest.raises(sgx.SgxError) as e:
+            renderer.render(u, sgx.default_opts(block_threads=bt))
+        assert e.value.status == 1
     # the context stays usable after rejected calls
     img = renderer.render_image(u)
     assert img.shape == (8, 8, 4)
