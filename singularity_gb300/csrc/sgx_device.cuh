@@ -104,6 +104,7 @@ template <class T> struct View {
     T uphi_den;  // cam_r * max(sin_th, 1e-6)
     // scene
     T M, a, a2, rs, r_in, r_out, peak_T, h, escape_r, time_sec, exposure, turbulence;
+    T twoM;   // 2 M
     T hcut;   // capture radius: 1.02 r_+ (Kerr) or u.horizon_cut (Schwarzschild)
     T f_cam;  // Schwarzschild 1 - rs/r_cam
     T f_obs;  // Kerr shading 1 - 2M/r_cam
@@ -142,6 +143,7 @@ template <class T> __device__ inline View<T> make_view(const sgx_uniforms& u) {
     v.M = T(u.mass_M);
     v.a = T(u.spin_a);
     v.a2 = v.a * v.a;
+    v.twoM = DLIT(2.0) * v.M;
     v.rs = T(u.rs);
     v.r_in = T(u.disc_r_inner);
     v.r_out = T(u.disc_r_outer);
@@ -395,7 +397,7 @@ template <class T> struct KS {
 template <class T> struct KC {
     T E, L;
     T aE, aL;          // a E, a L
-    T twoaE, fourE;    // 2 a E, 4 E
+    T twoaE, twoE;     // 2 a E, 2 E
 };
 
 template <class T> __device__ __forceinline__ KC<T> make_kc(const View<T>& v, T E, T L) {
@@ -405,7 +407,7 @@ template <class T> __device__ __forceinline__ KC<T> make_kc(const View<T>& v, T 
     c.aE = v.a * E;
     c.aL = v.a * L;
     c.twoaE = DLIT(2.0) * c.aE;
-    c.fourE = DLIT(4.0) * E;
+    c.twoE = DLIT(2.0) * E;
     return c;
 }
 
@@ -461,11 +463,12 @@ template <class T> __device__ __forceinline__ KS<T> kerr_rhs_ref(const KS<T>& s,
 // B/Delta + L^2/s2 with B = -A E^2 + 4 M a r E L - a^2 L^2 (expand and use
 // r^2 + a^2 - Delta = 2 M r).  With Q = P/Delta and U = W/s2:
 //   dr = Delta p_r / Sigma,   dth = p_th / Sigma,   dphi = (a Q + U) / Sigma
-//   dp_r  = -(N_r  - N Sigma_r  / Sigma) / (2 Sigma),  N_r  = Delta' (p_r^2 + Q^2) - 4 r E Q
-//   dp_th = -(N_th - N Sigma_th / Sigma) / (2 Sigma),  N_th = -sin2t U (2 a E + U),
-//   Sigma_r = 2 r,  Sigma_th = -a^2 sin2t,  Delta' = 2 (r - M).
-// About 45 operations against the reference grouping's ~75; the 1/sin^2
-// guard (1e-10) applies to U as it does to the reference's L^2/s2 terms.
+//   dp_r  = -(N_r  - N Sigma_r  / Sigma) / (2 Sigma) = (r N/Sigma + (M - r)(p_r^2 + Q^2) + 2 E r Q) / Sigma
+//   dp_th = -(N_th - N Sigma_th / Sigma) / (2 Sigma) = -sin(th) cos(th) (a^2 N/Sigma - U (2 a E + U)) / Sigma
+// using N_r = 2 (r - M)(p_r^2 + Q^2) - 4 r E Q, Sigma_r = 2 r,
+// N_th = -sin(2 th) U (2 a E + U), Sigma_th = -a^2 sin(2 th).  About 41
+// operations against the reference grouping's ~75; the 1/sin^2 guard (1e-10)
+// applies to U as it does to the reference's L^2/s2 terms.
 template <class T>
 __device__ __forceinline__ KS<T> kerr_rhs_sep_sc(const KS<T>& s, T st, T ct, const View<T>& v, const KC<T>& c) {
     const T r = s.r;
@@ -473,10 +476,10 @@ __device__ __forceinline__ KS<T> kerr_rhs_sep_sc(const KS<T>& s, T st, T ct, con
     const T s2 = st * st;
     const T safe_s2 = DM<T>::fmax_(s2, DLIT(1e-10));
     const T r2 = r * r;
+    const T r2a2 = r2 + a2;
     const T Sigma = r2 + a2 * (ct * ct);
-    const T Delta = r * (r - DLIT(2.0) * v.M) + a2;
-    const T Del_r = DLIT(2.0) * r - DLIT(2.0) * v.M;
-    const T P = (r2 + a2) * c.E - c.aL;
+    const T Delta = r2a2 - v.twoM * r;
+    const T P = r2a2 * c.E - c.aL;
     const T W = c.L - c.aE * s2;
     const T iS = DM<T>::rcp_fast(Sigma);
     const T iD = DM<T>::rcp_fast(Delta);
@@ -489,12 +492,9 @@ __device__ __forceinline__ KS<T> kerr_rhs_sep_sc(const KS<T>& s, T st, T ct, con
     d.ph = (v.a * Q + U) * iS;
     const T pr2 = s.pr * s.pr;
     const T N = ((Delta * pr2 + s.pth * s.pth) - P * Q) + W * U;
-    const T N_r = Del_r * (Q * Q + pr2) - (c.fourE * r) * Q;
     const T NiS = N * iS;
-    const T m = DLIT(-0.5) * iS;
-    d.pr = m * (N_r - (DLIT(2.0) * r) * NiS);
-    const T sin2t = DLIT(2.0) * st * ct;
-    d.pth = m * (sin2t * (a2 * NiS - U * (c.twoaE + U)));
+    d.pr = (r * NiS + ((v.M - r) * (Q * Q + pr2) + (c.twoE * r) * Q)) * iS;
+    d.pth = -(iS * (st * ct)) * (a2 * NiS - U * (c.twoaE + U));
     return d;
 }
 

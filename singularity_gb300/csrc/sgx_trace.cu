@@ -240,15 +240,15 @@ template <class T, int FL> struct KerrAdaptive {
     }
 
     __device__ __forceinline__ bool step(const View<T>& v, const PassDesc& pass) {
-        if (!finite_(y.r) || y.r < v.hcut) {
-            term = TERM_HORIZON;
-            return true;
-        }
-        if (y.r > v.escape_r) {
-            term = TERM_ESCAPE;
-            t0 = y.s;
-            t1 = y.ph;
-            t2 = y.c;
+        if (!(y.r >= v.hcut && y.r <= v.escape_r)) {  // one test for NaN, capture and escape
+            if (!finite_(y.r) || y.r < v.hcut) {
+                term = TERM_HORIZON;
+            } else {
+                term = TERM_ESCAPE;
+                t0 = y.s;
+                t1 = y.ph;
+                t2 = y.c;
+            }
             return true;
         }
         h = DM<T>::fmin_(h, T(pass.h_max_frac) * y.r);
