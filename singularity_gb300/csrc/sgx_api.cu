@@ -139,6 +139,15 @@ sgx_status render_impl(sgx_context* c, const sgx_uniforms* u, const sgx_render_o
 
     SGX_CUDA(c, cudaMemcpyAsync(c->d_u, u, sizeof(sgx_uniforms), cudaMemcpyHostToDevice, st));
     SGX_CUDA(c, sgxk::launch_setup_views(c->d_u, 1, c->d_view, int(o.precision), st));
+    // The tracer takes the view's constants as a kernel parameter: a host copy
+    // of the device-computed slot, refreshed when the uniforms change.
+    if (c->h_view_precision != int(o.precision) || std::memcmp(&c->h_view_u, u, sizeof(sgx_uniforms)) != 0) {
+        c->h_view_precision = -1;
+        SGX_CUDA(c, cudaMemcpyAsync(c->h_view, c->d_view, sgxk::view_bytes(), cudaMemcpyDeviceToHost, st));
+        SGX_CUDA(c, cudaStreamSynchronize(st));
+        c->h_view_u = *u;
+        c->h_view_precision = int(o.precision);
+    }
     const std::uint32_t tw = o.tile_w;
     const std::uint32_t th = o.tile_h;
 
@@ -164,7 +173,7 @@ sgx_status render_impl(sgx_context* c, const sgx_uniforms* u, const sgx_render_o
         SGX_CUDA(c, cudaEventRecord(c->ev_trace0, st));
         sgxk::LaunchShape shape{int(o.block_threads), int(o.blocks_per_sm)};
         SGX_CUDA(c, sgxk::launch_trace(int(u->metric_type), int(o.precision), int(o.integrator), int(o.rhs_form),
-                                       pass, shape, st));
+                                       pass, shape, st, c->h_view));
         SGX_CUDA(c, cudaEventRecord(c->ev_trace1, st));
         const bool first = (s0 == 0);
         const bool finalize = (s0 + n == spp);
@@ -247,6 +256,7 @@ sgx_status sgx_create(int device, sgx_context** out) {
     ok = ok && cudaMalloc(reinterpret_cast<void**>(&c->d_words), sizeof(sgxk::ViewPlan::words)) == cudaSuccess;
     ok = ok && cudaMalloc(reinterpret_cast<void**>(&c->d_counters), sizeof(sgxk::PassCounters)) == cudaSuccess;
     ok = ok && cudaMallocHost(reinterpret_cast<void**>(&c->h_counters), sizeof(sgxk::PassCounters)) == cudaSuccess;
+    ok = ok && cudaMallocHost(&c->h_view, sgxk::view_bytes()) == cudaSuccess;
     ok = ok && cudaEventCreate(&c->ev_begin) == cudaSuccess && cudaEventCreate(&c->ev_trace0) == cudaSuccess
          && cudaEventCreate(&c->ev_trace1) == cudaSuccess && cudaEventCreate(&c->ev_end) == cudaSuccess;
     if (!ok) {
@@ -268,6 +278,7 @@ void sgx_destroy(sgx_context* c) {
     if (c->d_words) cudaFree(c->d_words);
     if (c->d_counters) cudaFree(c->d_counters);
     if (c->h_counters) cudaFreeHost(c->h_counters);
+    if (c->h_view) cudaFreeHost(c->h_view);
     for (cudaEvent_t ev : {c->ev_begin, c->ev_trace0, c->ev_trace1, c->ev_end})
         if (ev) cudaEventDestroy(ev);
     if (c->stream) cudaStreamDestroy(c->stream);

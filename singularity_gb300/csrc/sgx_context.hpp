@@ -28,6 +28,9 @@ struct sgx_context {
     std::uint64_t* d_words = nullptr;  // view-set layout words
     sgxk::PassCounters* d_counters = nullptr;
     sgxk::PassCounters* h_counters = nullptr;  // pinned
+    void* h_view = nullptr;            // pinned host copy of view slot 0 (single-view tracer parameter)
+    sgx_uniforms h_view_u{};           // ... made from these uniforms
+    int h_view_precision = -1;         // ... at this precision (-1: none yet)
     cudaEvent_t ev_begin = nullptr, ev_trace0 = nullptr, ev_trace1 = nullptr, ev_end = nullptr;
     bool frame_valid = false;     // accumulator holds a complete frame
     std::uint32_t frame_spp = 0;

@@ -84,8 +84,11 @@ cudaError_t launch_setup_views(const sgx_uniforms* d_u, std::uint32_t n, void* d
                                cudaStream_t st);
 
 // Persistent tracer over a ViewSet.  precision: sgx_precision; integrator: sgx_integrator.
+// h_view: for a single-view pass, a host copy of that view's constants
+// (view_bytes() from the device slot setup_views wrote), passed to the kernel
+// as a parameter; nullptr = every view read from shared memory.
 cudaError_t launch_trace(int metric, int precision, int integrator, int rhs_form, const PassDesc& pass,
-                         LaunchShape shape, cudaStream_t st);
+                         LaunchShape shape, cudaStream_t st, const void* h_view = nullptr);
 
 // Per-sample probe (parity tests) of a single view: n samples, device arrays.
 cudaError_t launch_probe(const void* d_view, int metric, int precision, int integrator, int rhs_form,

@@ -17,7 +17,8 @@
 //     a pixel's samples in sample order — the reference's accumulation order —
 //     so colour work runs converged, once per sample, outside the step loop,
 //     and results do not depend on which warp traced which sample;
-//   * view constants and the pass's Halton offsets live in shared memory.
+//   * view constants and the pass's Halton offsets live in shared memory (a
+//     single-view pass takes its view as a kernel parameter instead).
 // All loops are bounded: a ray ends after max_steps integrator steps, and the
 // queue is a single counter that only grows.
 
@@ -25,6 +26,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
 #include <type_traits>
 
 #include "sgx_device.cuh"
@@ -413,8 +415,12 @@ enum : int { MODE_IDLE = 0, MODE_ACTIVE = 1, MODE_DONE = 2 };
 // padding carry no work.  Each policy names its resident blocks of 256 per
 // SM (kMinBlocks), which caps its registers: 4 = 64 registers, 3 = 80;
 // FP64 variants keep their registers (capped they spill up to 1.4 KB).
-template <class T, class Ray>
-__global__ void __launch_bounds__(256, Ray::kMinBlocks) trace_persistent(PassDesc pass) {
+// ONE: a single-view pass whose constants arrive as the kernel parameter
+// `one`, read from the constant bank as instruction operands instead of
+// shared-memory loads held in registers.
+template <class T, class Ray, bool ONE>
+__global__ void __launch_bounds__(256, Ray::kMinBlocks)
+    trace_persistent(const __grid_constant__ PassDesc pass, const __grid_constant__ View<T> one) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     // Block totals of the ray counters and each lane's record slot live in
     // shared memory, not in registers held across the integration loop.
@@ -433,6 +439,10 @@ __global__ void __launch_bounds__(256, Ray::kMinBlocks) trace_persistent(PassDes
     int mode = MODE_IDLE;
     std::uint32_t vid = 0;
     bool exhausted = false;
+    auto view_of = [&](std::uint32_t i) -> const View<T>& {
+        if constexpr (ONE) return one;
+        else return m.views[i];
+    };
 
     for (;;) {
         // 1. store the hit records of rays that ended.
@@ -457,8 +467,8 @@ __global__ void __launch_bounds__(256, Ray::kMinBlocks) trace_persistent(PassDes
                 if (mode == MODE_IDLE) {
                     const std::uint64_t id = base + __popc(idle & lt_mask);
                     if (id < vs.total_rays) {
-                        vid = vs.n == 1u ? 0u : find_view(m.ray_off, vs.n, id);
-                        const View<T>& v = m.views[vid];
+                        vid = (ONE || vs.n == 1u) ? 0u : find_view(m.ray_off, vs.n, id);
+                        const View<T>& v = view_of(vid);
                         const std::uint32_t Sv = m.S[vid];
                         const std::uint64_t local = id - m.ray_off[vid];
                         const std::uint64_t seq = local / Sv;
@@ -492,7 +502,7 @@ __global__ void __launch_bounds__(256, Ray::kMinBlocks) trace_persistent(PassDes
             continue;  // every id this round fell in tile padding
         }
         // 3. integrate.
-        const View<T>& v = m.views[vid];
+        const View<T>& v = view_of(vid);
         for (std::uint32_t j = 0; j < pass.refill; ++j) {
             if (mode == MODE_ACTIVE && ray.step(v, pass)) mode = MODE_DONE;
             if (__all_sync(kFull, mode != MODE_ACTIVE)) break;
@@ -613,9 +623,11 @@ __global__ void encode_kernel(const float4* __restrict__ acc, std::uint32_t npix
 // ---------------------------------------------------------------------------
 // Dispatch
 // ---------------------------------------------------------------------------
-template <class T, template <class, int> class Policy, int FL>
-cudaError_t run_persistent(const PassDesc& pass, LaunchShape shape, cudaStream_t st) {
-    auto kern = trace_persistent<T, Policy<T, FL>>;
+template <class T, class Ray, bool ONE>
+cudaError_t run_kernel(const PassDesc& pass, LaunchShape shape, const void* h_view, cudaStream_t st) {
+    auto kern = trace_persistent<T, Ray, ONE>;
+    View<T> one{};
+    if constexpr (ONE) std::memcpy(&one, h_view, sizeof(View<T>));
     const std::size_t smem = set_smem_bytes<T>(pass.vs.n, pass.vs.max_S);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
@@ -632,8 +644,14 @@ cudaError_t run_persistent(const PassDesc& pass, LaunchShape shape, cudaStream_t
     std::uint64_t blocks = std::uint64_t(sms) * per_sm;
     const std::uint64_t need = (pass.vs.total_rays + threads - 1) / threads;
     if (need < blocks) blocks = need > 0 ? need : 1;
-    kern<<<unsigned(blocks), threads, smem, st>>>(pass);
+    kern<<<unsigned(blocks), threads, smem, st>>>(pass, one);
     return cudaGetLastError();
+}
+
+template <class T, template <class, int> class Policy, int FL>
+cudaError_t run_persistent(const PassDesc& pass, LaunchShape shape, const void* h_view, cudaStream_t st) {
+    if (h_view != nullptr && pass.vs.n == 1u) return run_kernel<T, Policy<T, FL>, true>(pass, shape, h_view, st);
+    return run_kernel<T, Policy<T, FL>, false>(pass, shape, nullptr, st);
 }
 
 template <class T, template <class, int> class Policy, int FL>
@@ -766,10 +784,10 @@ cudaError_t launch_setup_views(const sgx_uniforms* d_u, std::uint32_t n, void* d
 }
 
 cudaError_t launch_trace(int metric, int precision, int integrator, int rhs_form, const PassDesc& pass,
-                         LaunchShape shape, cudaStream_t st) {
+                         LaunchShape shape, cudaStream_t st, const void* h_view) {
     return dispatch(metric, precision, integrator, rhs_form,
                     [&]<class T, template <class, int> class Policy, int FL>() {
-                        return run_persistent<T, Policy, FL>(pass, shape, st);
+                        return run_persistent<T, Policy, FL>(pass, shape, h_view, st);
                     });
 }
 
