@@ -38,40 +38,37 @@ SGX_HD double hsqrt(double x) { return sqrt(x); }
 // State layout: y[0..5] = r, theta, phi, p_r, p_theta, psi (swept angle);
 // derivative layout d[0..4] = dr, dtheta, dphi, dp_r, dp_theta.
 
-// The right-hand side in the shared-reciprocal algebra.
+// The right-hand side in Carter's separated form (the same Hamiltonian as
+// kerr_hamilton.h:97-155): with P = (r^2 + a^2) E - a L, W = L - a E s2,
+// Q = P / Delta, U = W / s2 and N = 2 Sigma H = Delta p_r^2 + p_th^2 - P Q + W U,
+//   dr = Delta p_r / Sigma, dth = p_th / Sigma, dphi = (a Q + U) / Sigma,
+//   dp_r  = (r N / Sigma + (M - r)(p_r^2 + Q^2) + 2 E r Q) / Sigma,
+//   dp_th = -sin(th) cos(th) (a^2 N / Sigma - U (2 a E + U)) / Sigma.
+// Operation for operation the forward kernel's rhs_g (sgx_diff_impl.cuh).
 template <class T>
 SGX_HD_CALL void rhs(const T* y, T E, T L, T a, T M, T* d) {
     const T st = hsin(y[1]), ct = hcos(y[1]);
-    const T r = y[0], pr = y[3], pth = y[4];
-    const T a2 = a * a, s2 = st * st, c2 = ct * ct, r2 = r * r;
+    const T r = y[0];
+    const T a2 = a * a;
+    const T s2 = st * st;
     const T ss = s2 < T(1e-10) ? T(1e-10) : s2;
+    const T r2 = r * r;
     const T r2a2 = r2 + a2;
-    const T Sig = r2 + a2 * c2;
-    const T Dr = T(2) * (r - M);
-    const T Del = r * (r - T(2) * M) + a2;
-    const T a2s2 = a2 * s2;
-    const T A = r2a2 * r2a2 - a2s2 * Del;
+    const T Sig = r2 + a2 * (ct * ct);
+    const T Del = r2a2 - (T(2) * M) * r;
+    const T aE = a * E;
+    const T P = r2a2 * E - a * L;
+    const T W = L - aE * s2;
     const T iS = T(1) / Sig, iD = T(1) / Del, is2 = T(1) / ss;
-    const T iSD = iS * iD, iS2 = iS * iS;
-    const T E2 = E * E, L2 = L * L;
-    const T cEL = T(4) * M * a * E * L;
-    const T aL2 = a2 * L2;
-    const T tMaE = T(2) * M * a * E;
-    d[2] = (tMaE * r * s2 + (Del - a2s2) * L) * iSD * is2;
-    d[0] = Del * pr * iS;
-    d[1] = pth * iS;
-    const T B = (cEL * r - A * E2) - aL2;
-    const T Ar = T(4) * r * r2a2 - a2s2 * Dr;
-    const T Br = cEL - Ar * E2;
-    const T s2t = T(2) * st * ct;
-    const T St = -a2 * s2t;
-    const T pr2 = pr * pr;
-    const T Dp2 = Del * pr2 + pth * pth;
-    const T tr = T(2) * r;
-    const T Hr = iSD * (Br - B * (tr * Del + Sig * Dr) * iSD) + Dr * pr2 * iS - tr * iS2 * (L2 * is2 + Dp2);
-    const T Ht = iSD * (a2 * Del * s2t * E2) - B * St * iS2 * iD - iS2 * (L2 * is2 * (St + Sig * s2t * is2) + Dp2 * St);
-    d[3] = T(-0.5) * Hr;
-    d[4] = T(-0.5) * Ht;
+    const T Q = P * iD, U = W * is2;
+    d[0] = Del * y[3] * iS;
+    d[1] = y[4] * iS;
+    d[2] = (a * Q + U) * iS;
+    const T pr2 = y[3] * y[3];
+    const T N = ((Del * pr2 + y[4] * y[4]) - P * Q) + W * U;
+    const T NiS = N * iS;
+    d[3] = (r * NiS + ((M - r) * (Q * Q + pr2) + (T(2) * E * r) * Q)) * iS;
+    d[4] = -(iS * (st * ct)) * (a2 * NiS - U * (T(2) * aE + U));
 }
 
 // w . d(rhs)/d(r, theta, p_r, p_theta, E, L, a), w the adjoint of d[0..4].
@@ -80,157 +77,107 @@ SGX_HD_CALL void rhs(const T* y, T E, T L, T a, T M, T* d) {
 template <class T>
 SGX_HD_CALL void rhs_vjp(const T* y, T E, T L, T a, T M, const T* w, T* gy, T* gc) {
     // forward intermediates
-    const T th = y[1];
-    const T st = hsin(th), ct = hcos(th);
+    const T st = hsin(y[1]), ct = hcos(y[1]);
     const T r = y[0], pr = y[3], pth = y[4];
-    const T a2 = a * a, s2 = st * st, c2 = ct * ct, r2 = r * r;
+    const T a2 = a * a;
+    const T s2 = st * st;
     const bool s2_free = !(s2 < T(1e-10));
     const T ss = s2_free ? s2 : T(1e-10);
+    const T r2 = r * r;
     const T r2a2 = r2 + a2;
+    const T c2 = ct * ct;
     const T Sig = r2 + a2 * c2;
-    const T Dr = T(2) * (r - M);
-    const T Del = r * (r - T(2) * M) + a2;
-    const T a2s2 = a2 * s2;
-    const T A = r2a2 * r2a2 - a2s2 * Del;
+    const T Del = r2a2 - (T(2) * M) * r;
+    const T aE = a * E;
+    const T P = r2a2 * E - a * L;
+    const T W = L - aE * s2;
     const T iS = T(1) / Sig, iD = T(1) / Del, is2 = T(1) / ss;
-    const T iSD = iS * iD, iS2 = iS * iS;
-    const T E2 = E * E, L2 = L * L;
-    const T cEL = T(4) * M * a * E * L;
-    const T tMaE = T(2) * M * a * E;
-    const T P = tMaE * r * s2 + (Del - a2s2) * L;
-    const T B = (cEL * r - A * E2) - a2 * L2;
-    const T Ar = T(4) * r * r2a2 - a2s2 * Dr;
-    const T Br = cEL - Ar * E2;
-    const T s2t = T(2) * st * ct;
-    const T St = -a2 * s2t;
+    const T Q = P * iD, U = W * is2;
     const T pr2 = pr * pr;
-    const T Dp2 = Del * pr2 + pth * pth;
-    const T tr = T(2) * r;
-    const T G = tr * Del + Sig * Dr;
-    const T X = Br - B * G * iSD;
-    const T Y = L2 * is2 + Dp2;
-    const T U = a2 * Del * s2t * E2;
-    const T W = St + Sig * s2t * is2;
-    const T V = L2 * is2 * W + Dp2 * St;
+    const T N = ((Del * pr2 + pth * pth) - P * Q) + W * U;
+    const T NiS = N * iS;
+    const T X = Q * Q + pr2;
+    const T A3 = r * NiS + ((M - r) * X + (T(2) * E * r) * Q);
+    const T C2 = a * Q + U;
+    const T V1 = T(2) * aE + U;
+    const T B4 = a2 * NiS - U * V1;
+    const T sc = st * ct;
 
-    // reverse
-    const T w_r = w[0], w_th = w[1], w_ph = w[2];
-    const T Hr_b = T(-0.5) * w[3], Ht_b = T(-0.5) * w[4];
-    // Ht = iSD U - B St iS2 iD - iS2 V
-    T iSD_b = Ht_b * U;
-    const T U_b = Ht_b * iSD;
-    T B_b = -Ht_b * St * iS2 * iD;
-    T St_b = -Ht_b * B * iS2 * iD;
-    T iS2_b = -Ht_b * B * St * iD - Ht_b * V;
-    T iD_b = -Ht_b * B * St * iS2;
-    const T V_b = -Ht_b * iS2;
-    // V = L2 is2 W + Dp2 St
-    T L2_b = V_b * is2 * W;
-    T is2_b = V_b * L2 * W;
-    const T W_b = V_b * L2 * is2;
-    T Dp2_b = V_b * St;
-    St_b += V_b * Dp2;
-    // W = St + Sig s2t is2
-    St_b += W_b;
-    T Sig_b = W_b * s2t * is2;
-    T s2t_b = W_b * Sig * is2;
-    is2_b += W_b * Sig * s2t;
-    // U = a2 Del s2t E2
-    T a2_b = U_b * Del * s2t * E2;
-    T Del_b = U_b * a2 * s2t * E2;
-    s2t_b += U_b * a2 * Del * E2;
-    T E2_b = U_b * a2 * Del * s2t;
-    // Hr = iSD X + Dr pr2 iS - tr iS2 Y
-    iSD_b += Hr_b * X;
-    const T X_b = Hr_b * iSD;
-    T Dr_b = Hr_b * pr2 * iS;
-    T pr2_b = Hr_b * Dr * iS;
-    T iS_b = Hr_b * Dr * pr2;
-    T tr_b = -Hr_b * iS2 * Y;
-    iS2_b += -Hr_b * tr * Y;
-    const T Y_b = -Hr_b * tr * iS2;
-    // Y = L2 is2 + Dp2
-    L2_b += Y_b * is2;
-    is2_b += Y_b * L2;
-    Dp2_b += Y_b;
-    // X = Br - B G iSD
-    const T Br_b = X_b;
-    B_b += -X_b * G * iSD;
-    const T G_b = -X_b * B * iSD;
-    iSD_b += -X_b * B * G;
-    // G = tr Del + Sig Dr
-    tr_b += G_b * Del;
-    Del_b += G_b * tr;
-    Sig_b += G_b * Dr;
-    Dr_b += G_b * Sig;
-    // Dp2 = Del pr2 + pth^2
-    Del_b += Dp2_b * pr2;
-    pr2_b += Dp2_b * Del;
-    T pth_b = T(2) * pth * Dp2_b;
-    T pr_b = T(2) * pr * pr2_b;
-    // St = -a2 s2t ; s2t = 2 st ct
-    a2_b += -St_b * s2t;
-    s2t_b += -St_b * a2;
-    T st_b = T(2) * ct * s2t_b;
-    T ct_b = T(2) * st * s2t_b;
-    // Br = cEL - Ar E2 ; Ar = 4 r r2a2 - a2s2 Dr
-    T cEL_b = Br_b;
-    const T Ar_b = -Br_b * E2;
-    E2_b += -Br_b * Ar;
-    T r_b = T(4) * r2a2 * Ar_b;
-    T r2a2_b = T(4) * r * Ar_b;
-    T a2s2_b = -Ar_b * Dr;
-    Dr_b += -Ar_b * a2s2;
-    // B = cEL r - A E2 - a2 L2
-    cEL_b += B_b * r;
-    r_b += B_b * cEL;
-    const T A_b = -B_b * E2;
-    E2_b += -B_b * A;
-    a2_b += -B_b * L2;
-    L2_b += -B_b * a2;
-    // dth = pth iS ; dr = Del pr iS
-    pth_b += w_th * iS;
-    iS_b += w_th * pth + w_r * Del * pr;
-    Del_b += w_r * pr * iS;
-    pr_b += w_r * Del * iS;
-    // dph = P iSD is2 ; P = tMaE r s2 + (Del - a2s2) L
-    const T P_b = w_ph * iSD * is2;
-    iSD_b += w_ph * P * is2;
-    is2_b += w_ph * P * iSD;
-    const T tMaE_b = P_b * r * s2;
-    r_b += P_b * tMaE * s2;
-    T s2_b = P_b * tMaE * r;
-    Del_b += P_b * L;
-    a2s2_b += -P_b * L;
-    T L_b = P_b * (Del - a2s2);
-    // constants: tMaE = 2 M a E ; cEL = 4 M a E L ; E2, L2
-    T a_b = tMaE_b * T(2) * M * E + cEL_b * T(4) * M * E * L;
-    T E_b = tMaE_b * T(2) * M * a + cEL_b * T(4) * M * a * L + T(2) * E * E2_b;
-    L_b += cEL_b * T(4) * M * a * E + T(2) * L * L2_b;
-    // iSD = iS iD ; iS2 = iS^2 ; reciprocals
-    iS_b += iSD_b * iD + T(2) * iS * iS2_b;
-    iD_b += iSD_b * iS;
-    Sig_b += -iS_b * iS * iS;
+    // reverse: d0 = Del pr iS, d1 = pth iS, d2 = C2 iS, d3 = A3 iS, d4 = -(iS sc) B4
+    const T w0 = w[0], w1 = w[1], w2 = w[2], w3 = w[3], w4 = w[4];
+    T iS_b = w0 * Del * pr + w1 * pth + w2 * C2 + w3 * A3 - w4 * sc * B4;
+    T Del_b = w0 * pr * iS;
+    T pr_b = w0 * Del * iS;
+    T pth_b = w1 * iS;
+    const T C2_b = w2 * iS;
+    const T A3_b = w3 * iS;
+    const T sc_b = -w4 * iS * B4;
+    const T B4_b = -w4 * iS * sc;
+    // C2 = a Q + U
+    T a_b = C2_b * Q;
+    T Q_b = C2_b * a;
+    T U_b = C2_b;
+    // A3 = r NiS + (M - r) X + 2 E r Q
+    T r_b = A3_b * (NiS - X + T(2) * E * Q);
+    T NiS_b = A3_b * r;
+    const T X_b = A3_b * (M - r);
+    T E_b = A3_b * T(2) * r * Q;
+    Q_b += A3_b * T(2) * E * r;
+    // B4 = a2 NiS - U V1 ; V1 = 2 aE + U
+    T a2_b = B4_b * NiS;
+    NiS_b += B4_b * a2;
+    U_b += -B4_b * V1;
+    const T V1_b = -B4_b * U;
+    T aE_b = T(2) * V1_b;
+    U_b += V1_b;
+    // X = Q^2 + pr2
+    Q_b += T(2) * Q * X_b;
+    T pr2_b = X_b;
+    // NiS = N iS
+    const T N_b = NiS_b * iS;
+    iS_b += NiS_b * N;
+    // N = Del pr2 + pth^2 - P Q + W U
+    Del_b += N_b * pr2;
+    pr2_b += N_b * Del;
+    pth_b += T(2) * pth * N_b;
+    T P_b = -N_b * Q;
+    Q_b += -N_b * P;
+    T W_b = N_b * U;
+    U_b += N_b * W;
+    // Q = P iD ; U = W is2
+    P_b += Q_b * iD;
+    const T iD_b = Q_b * P;
+    W_b += U_b * is2;
+    const T is2_b = U_b * W;
+    // reciprocals
+    const T Sig_b = -iS_b * iS * iS;
     Del_b += -iD_b * iD * iD;
-    if (s2_free) s2_b += -is2_b * is2 * is2;
-    // A = r2a2^2 - a2s2 Del ; a2s2 = a2 s2
-    r2a2_b += T(2) * r2a2 * A_b;
-    a2s2_b += -A_b * Del;
-    Del_b += -A_b * a2s2;
-    a2_b += a2s2_b * s2;
-    s2_b += a2s2_b * a2;
-    // Del = r (r - 2M) + a2 ; Dr = 2 (r - M) ; tr = 2 r
-    r_b += Del_b * Dr + T(2) * Dr_b + T(2) * tr_b;
-    a2_b += Del_b;
-    // Sig = r2 + a2 c2 ; r2a2 = r2 + a2 ; r2 = r^2
-    T r2_b = Sig_b + r2a2_b;
+    T s2_b = s2_free ? -is2_b * is2 * is2 : T(0);
+    // W = L - aE s2
+    T L_b = W_b;
+    aE_b += -W_b * s2;
+    s2_b += -W_b * aE;
+    // P = r2a2 E - a L
+    T r2a2_b = P_b * E;
+    E_b += P_b * r2a2;
+    a_b += -P_b * L;
+    L_b += -P_b * a;
+    // aE = a E
+    a_b += aE_b * E;
+    E_b += aE_b * a;
+    // Del = r2a2 - 2 M r
+    r2a2_b += Del_b;
+    r_b += -(T(2) * M) * Del_b;
+    // Sig = r2 + a2 c2 ; r2a2 = r2 + a2
+    const T r2_b = Sig_b + r2a2_b;
     a2_b += Sig_b * c2 + r2a2_b;
     const T c2_b = Sig_b * a2;
+    pr_b += T(2) * pr * pr2_b;
     r_b += T(2) * r * r2_b;
-    // c2 = ct^2 ; s2 = st^2 ; st, ct of theta
-    ct_b += T(2) * ct * c2_b;
-    st_b += T(2) * st * s2_b;
     a_b += T(2) * a * a2_b;
+    // sc = st ct ; c2 = ct^2 ; s2 = st^2 ; st, ct of theta
+    const T st_b = sc_b * ct + T(2) * st * s2_b;
+    const T ct_b = sc_b * st + T(2) * ct * c2_b;
 
     gy[0] = r_b;
     gy[1] = st_b * ct - ct_b * st;

@@ -66,8 +66,9 @@ template <class S> __device__ __forceinline__ S smooth01(const S& x) {
     return x * x * (S(T(3)) - S(T(2)) * x);
 }
 
-// Kerr Hamiltonian right-hand side (kerr_hamilton.h:97-155): the reference's
-// grouping with three shared reciprocals, generic in the scalar.
+// Kerr Hamiltonian right-hand side (kerr_hamilton.h:97-155) in Carter's
+// separated form, generic in the scalar; operation for operation sgxa::rhs
+// (sgx_adjoint.cuh), which states the equations.
 template <class S, class T>
 __device__ __forceinline__ void rhs_g(const S* y, const S& E, const S& L, const S& a, T M, S* d) {
     S st, ct;
@@ -76,40 +77,25 @@ __device__ __forceinline__ void rhs_g(const S* y, const S& E, const S& L, const 
     const S a2 = a * a;
     const S s2 = st * st;
     const S safe_s2 = selv(value_of(s2) < T(1e-10), S(T(1e-10)), s2);
-    const S c2 = ct * ct;
     const S r2 = r * r;
     const S r2a2 = r2 + a2;
-    const S Sigma = r2 + a2 * c2;
-    const S Del_r = S(T(2)) * (r - S(M));
-    const S Delta = r * (r - S(T(2) * M)) + a2;
-    const S a2s2 = a2 * s2;
-    const S A = r2a2 * r2a2 - a2s2 * Delta;
+    const S Sigma = r2 + a2 * (ct * ct);
+    const S Delta = r2a2 - S(T(2) * M) * r;
+    const S aE = a * E;
+    const S P = r2a2 * E - a * L;
+    const S W = L - aE * s2;
     const S iS = S(T(1)) / Sigma;
     const S iD = S(T(1)) / Delta;
     const S is2 = S(T(1)) / safe_s2;
-    const S iSD = iS * iD;
-    const S iS2 = iS * iS;
-    const S E2 = E * E, L2 = L * L;
-    const S cEL = S(T(4) * M) * a * E * L;
-    const S aL2 = a2 * L2;
-    const S twoMaE = S(T(2) * M) * a * E;
-    d[2] = (twoMaE * r * s2 + (Delta - a2s2) * L) * iSD * is2;
+    const S Q = P * iD, U = W * is2;
     d[0] = Delta * y[3] * iS;
     d[1] = y[4] * iS;
-    const S B = (cEL * r - A * E2) - aL2;
-    const S A_r = S(T(4)) * r * r2a2 - a2s2 * Del_r;
-    const S B_r = cEL - A_r * E2;
-    const S sin2t = S(T(2)) * st * ct;
-    const S Sig_t = -a2 * sin2t;
+    d[2] = (a * Q + U) * iS;
     const S pr2 = y[3] * y[3];
-    const S Dp2 = Delta * pr2 + y[4] * y[4];
-    const S two_r = S(T(2)) * r;
-    const S dH_dr = iSD * (B_r - B * (two_r * Delta + Sigma * Del_r) * iSD) + Del_r * pr2 * iS -
-                    two_r * iS2 * (L2 * is2 + Dp2);
-    const S dH_dth = iSD * (a2 * Delta * sin2t * E2) - B * Sig_t * iS2 * iD -
-                     iS2 * (L2 * is2 * (Sig_t + Sigma * sin2t * is2) + Dp2 * Sig_t);
-    d[3] = S(T(-0.5)) * dH_dr;
-    d[4] = S(T(-0.5)) * dH_dth;
+    const S N = ((Delta * pr2 + y[4] * y[4]) - P * Q) + W * U;
+    const S NiS = N * iS;
+    d[3] = (r * NiS + ((S(M) - r) * (Q * Q + pr2) + (S(T(2)) * E * r) * Q)) * iS;
+    d[4] = -(iS * (st * ct)) * (a2 * NiS - U * (S(T(2)) * aE + U));
 }
 
 // One fixed RK4 step with the reference's pole damping, plus the swept angle.
