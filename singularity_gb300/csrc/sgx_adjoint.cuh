@@ -34,6 +34,23 @@ SGX_HD float hsqrt(float x) { return sqrtf(x); }
 SGX_HD double hsin(double x) { return sin(x); }
 SGX_HD double hcos(double x) { return cos(x); }
 SGX_HD double hsqrt(double x) { return sqrt(x); }
+// sine and cosine from one range reduction on the device
+SGX_HD void hsincos(float x, float* s, float* c) {
+#if defined(__CUDA_ARCH__)
+    sincosf(x, s, c);
+#else
+    *s = sinf(x);
+    *c = cosf(x);
+#endif
+}
+SGX_HD void hsincos(double x, double* s, double* c) {
+#if defined(__CUDA_ARCH__)
+    sincos(x, s, c);
+#else
+    *s = sin(x);
+    *c = cos(x);
+#endif
+}
 
 // State layout: y[0..5] = r, theta, phi, p_r, p_theta, psi (swept angle);
 // derivative layout d[0..4] = dr, dtheta, dphi, dp_r, dp_theta.
@@ -46,8 +63,7 @@ SGX_HD double hsqrt(double x) { return sqrt(x); }
 //   dp_th = -sin(th) cos(th) (a^2 N / Sigma - U (2 a E + U)) / Sigma.
 // Operation for operation the forward kernel's rhs_g (sgx_diff_impl.cuh).
 template <class T>
-SGX_HD_CALL void rhs(const T* y, T E, T L, T a, T M, T* d) {
-    const T st = hsin(y[1]), ct = hcos(y[1]);
+SGX_HD_CALL void rhs_sc(const T* y, T st, T ct, T E, T L, T a, T M, T* d) {
     const T r = y[0];
     const T a2 = a * a;
     const T s2 = st * st;
@@ -71,13 +87,18 @@ SGX_HD_CALL void rhs(const T* y, T E, T L, T a, T M, T* d) {
     d[4] = -(iS * (st * ct)) * (a2 * NiS - U * (T(2) * aE + U));
 }
 
-// w . d(rhs)/d(r, theta, p_r, p_theta, E, L, a), w the adjoint of d[0..4].
-// gy[0..4] receives the state part (gy[2] = 0: the right-hand side does not
-// depend on phi); gc[0..2] += the constants' part.
+template <class T> SGX_HD void rhs(const T* y, T E, T L, T a, T M, T* d) {
+    T st, ct;
+    hsincos(y[1], &st, &ct);
+    rhs_sc(y, st, ct, E, L, a, M, d);
+}
+
+// w . d(rhs)/d(r, theta, p_r, p_theta, E, L, a), w the adjoint of d[0..4],
+// with st, ct = sin, cos of y[1].  gy[0..4] receives the state part (gy[2] = 0:
+// the right-hand side does not depend on phi); gc[0..2] += the constants' part.
 template <class T>
-SGX_HD_CALL void rhs_vjp(const T* y, T E, T L, T a, T M, const T* w, T* gy, T* gc) {
+SGX_HD_CALL void rhs_vjp_sc(const T* y, T st, T ct, T E, T L, T a, T M, const T* w, T* gy, T* gc) {
     // forward intermediates
-    const T st = hsin(y[1]), ct = hcos(y[1]);
     const T r = y[0], pr = y[3], pth = y[4];
     const T a2 = a * a;
     const T s2 = st * st;
@@ -189,13 +210,18 @@ SGX_HD_CALL void rhs_vjp(const T* y, T E, T L, T a, T M, const T* w, T* gy, T* g
     gc[2] += a_b;
 }
 
+template <class T> SGX_HD void rhs_vjp(const T* y, T E, T L, T a, T M, const T* w, T* gy, T* gc) {
+    T st, ct;
+    hsincos(y[1], &st, &ct);
+    rhs_vjp_sc(y, st, ct, E, L, a, M, w, gy, gc);
+}
+
 // Pole-damped step length h * clamp(5 |sin(theta)|, 0.05, 1) and its theta
 // derivative (kerr_hamilton.h:165-178).
-template <class T> SGX_HD T damped_h(T h, T th, T* dh_dth) {
-    const T s = hsin(th);
+template <class T> SGX_HD T damped_h_sc(T h, T s, T c, T* dh_dth) {
     const T as = s < T(0) ? -s : s;
     T ps = as * T(5);
-    T dps = (s < T(0) ? T(-5) : T(5)) * hcos(th);
+    T dps = (s < T(0) ? T(-5) : T(5)) * c;
     if (ps > T(1)) {
         ps = T(1);
         dps = T(0);
@@ -205,6 +231,11 @@ template <class T> SGX_HD T damped_h(T h, T th, T* dh_dth) {
     }
     *dh_dth = h * dps;
     return h * ps;
+}
+template <class T> SGX_HD T damped_h(T h, T th, T* dh_dth) {
+    T s, c;
+    hsincos(th, &s, &c);
+    return damped_h_sc(h, s, c, dh_dth);
 }
 
 // One RK4 step y -> o (with the swept angle when `fade`).
@@ -234,17 +265,23 @@ template <class T> SGX_HD void step(const T* y, T E, T L, T a, T M, T h, bool fa
 // replaced by the adjoint of its input; gc[0..2] += the step's terms of
 // dLoss/d(E, L, a).
 template <class T> SGX_HD void step_vjp(const T* y, T E, T L, T a, T M, T h, bool fade, T* lam, T* gc) {
+    // sin, cos of each stage's theta, shared by its right-hand side and reverse pass
+    T s1, c1, s2, c2, s3, c3, s4, c4;
+    hsincos(y[1], &s1, &c1);
     T dhd;
-    const T he = damped_h(h, y[1], &dhd);
+    const T he = damped_h_sc(h, s1, c1, &dhd);
     const T hh = T(0.5) * he;
     T k1[5], k2[5], k3[5], k4[5], y2[6], y3[6], y4[6];
-    rhs(y, E, L, a, M, k1);
+    rhs_sc(y, s1, c1, E, L, a, M, k1);
     for (int i = 0; i < 5; ++i) y2[i] = y[i] + k1[i] * hh;
-    rhs(y2, E, L, a, M, k2);
+    hsincos(y2[1], &s2, &c2);
+    rhs_sc(y2, s2, c2, E, L, a, M, k2);
     for (int i = 0; i < 5; ++i) y3[i] = y[i] + k2[i] * hh;
-    rhs(y3, E, L, a, M, k3);
+    hsincos(y3[1], &s3, &c3);
+    rhs_sc(y3, s3, c3, E, L, a, M, k3);
     for (int i = 0; i < 5; ++i) y4[i] = y[i] + k3[i] * he;
-    rhs(y4, E, L, a, M, k4);
+    hsincos(y4[1], &s4, &c4);
+    rhs_sc(y4, s4, c4, E, L, a, M, k4);
     const T h6 = he / T(6);
     T lo[5];
     for (int i = 0; i < 5; ++i) lo[i] = lam[i];
@@ -261,7 +298,8 @@ template <class T> SGX_HD void step_vjp(const T* y, T E, T L, T a, T M, T h, boo
             o2 = y[2] + s2 * h6;
         }
         const T dth = o1 - y[1], dph = o2 - y[2];
-        const T s = hsin(o1), c = hcos(o1);
+        T s, c;
+        hsincos(o1, &s, &c);
         const T q = hsqrt(dth * dth + s * s * dph * dph);
         if (q > T(0)) {
             const T iq = lam[5] / q;
@@ -287,7 +325,7 @@ template <class T> SGX_HD void step_vjp(const T* y, T E, T L, T a, T M, T h, boo
     ly[2] += l_y2_psi;
     T g[5];
     // k4 = f(y4), y4 = y + he k3
-    rhs_vjp(y4, E, L, a, M, lk4, g, gc);
+    rhs_vjp_sc(y4, s4, c4, E, L, a, M, lk4, g, gc);
     for (int i = 0; i < 5; ++i) {
         ly[i] += g[i];
         lk3[i] += he * g[i];
@@ -295,21 +333,21 @@ template <class T> SGX_HD void step_vjp(const T* y, T E, T L, T a, T M, T h, boo
     }
     T l_hh = T(0);
     // k3 = f(y3), y3 = y + hh k2
-    rhs_vjp(y3, E, L, a, M, lk3, g, gc);
+    rhs_vjp_sc(y3, s3, c3, E, L, a, M, lk3, g, gc);
     for (int i = 0; i < 5; ++i) {
         ly[i] += g[i];
         lk2[i] += hh * g[i];
         l_hh += g[i] * k2[i];
     }
     // k2 = f(y2), y2 = y + hh k1
-    rhs_vjp(y2, E, L, a, M, lk2, g, gc);
+    rhs_vjp_sc(y2, s2, c2, E, L, a, M, lk2, g, gc);
     for (int i = 0; i < 5; ++i) {
         ly[i] += g[i];
         lk1[i] += hh * g[i];
         l_hh += g[i] * k1[i];
     }
     // k1 = f(y)
-    rhs_vjp(y, E, L, a, M, lk1, g, gc);
+    rhs_vjp_sc(y, s1, c1, E, L, a, M, lk1, g, gc);
     for (int i = 0; i < 5; ++i) ly[i] += g[i];
     // he = h ps(theta), hh = he / 2
     ly[1] += (l_he + T(0.5) * l_hh) * dhd;

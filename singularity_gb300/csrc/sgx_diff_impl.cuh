@@ -70,9 +70,8 @@ template <class S> __device__ __forceinline__ S smooth01(const S& x) {
 // separated form, generic in the scalar; operation for operation sgxa::rhs
 // (sgx_adjoint.cuh), which states the equations.
 template <class S, class T>
-__device__ __forceinline__ void rhs_g(const S* y, const S& E, const S& L, const S& a, T M, S* d) {
-    S st, ct;
-    DM<S>::sincos_(y[1], &st, &ct);
+__device__ __forceinline__ void rhs_g_sc(const S* y, const S& st, const S& ct, const S& E, const S& L, const S& a,
+                                         T M, S* d) {
     const S r = y[0];
     const S a2 = a * a;
     const S s2 = st * st;
@@ -98,16 +97,24 @@ __device__ __forceinline__ void rhs_g(const S* y, const S& E, const S& L, const 
     d[4] = -(iS * (st * ct)) * (a2 * NiS - U * (S(T(2)) * aE + U));
 }
 
+template <class S, class T>
+__device__ __forceinline__ void rhs_g(const S* y, const S& E, const S& L, const S& a, T M, S* d) {
+    S st, ct;
+    DM<S>::sincos_(y[1], &st, &ct);
+    rhs_g_sc(y, st, ct, E, L, a, M, d);
+}
+
 // One fixed RK4 step with the reference's pole damping, plus the swept angle.
 template <class S, class T>
 __device__ __forceinline__ void step_g(const S* y, const S& E, const S& L, const S& a, T M, T h, bool fade, S* o) {
-    const S st0 = DM<S>::sin_(y[1]);
+    S st0, ct0;  // sin, cos of the step's theta: the pole damping and k1
+    DM<S>::sincos_(y[1], &st0, &ct0);
     S ps = selv(value_of(st0) < T(0), -st0, st0) * S(T(5));
     ps = selv(value_of(ps) > T(1), S(T(1)), selv(value_of(ps) < T(0.05), S(T(0.05)), ps));
     const S he = S(h) * ps;
     const S hh = S(T(0.5)) * he;
     S k1[5], k2[5], k3[5], k4[5], t[5];
-    rhs_g(y, E, L, a, M, k1);
+    rhs_g_sc(y, st0, ct0, E, L, a, M, k1);
 #pragma unroll
     for (int i = 0; i < 5; ++i) t[i] = y[i] + k1[i] * hh;
     rhs_g(t, E, L, a, M, k2);
