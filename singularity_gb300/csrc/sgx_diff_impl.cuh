@@ -14,6 +14,7 @@
 #include <cstdint>
 #include <cstring>
 #include <string>
+#include <type_traits>
 
 #include "sgx.h"
 #include "sgx_context.hpp"
@@ -59,6 +60,17 @@ template <class T> struct DiffBufs {
 
 template <class S> __device__ __forceinline__ S selv(bool c, const S& a, const S& b) { return c ? a : b; }
 
+// 1/x of the right-hand side: the SFU reciprocal in FP32 (sgxa::hrcp alike),
+// a division in FP64 and for dual numbers.
+template <class S> __device__ __forceinline__ S rcp_g(const S& x) {
+    if constexpr (std::is_same_v<S, float>) return DM<float>::rcp_fast(x);
+    else if constexpr (std::is_same_v<S, double>) return 1.0 / x;
+    else {
+        using T = decltype(value_of(x));
+        return S(T(1)) / x;
+    }
+}
+
 template <class S> __device__ __forceinline__ S smooth01(const S& x) {
     using T = decltype(value_of(x));
     if (value_of(x) <= T(0)) return S(T(0));
@@ -83,9 +95,9 @@ __device__ __forceinline__ void rhs_g_sc(const S* y, const S& st, const S& ct, c
     const S aE = a * E;
     const S P = r2a2 * E - a * L;
     const S W = L - aE * s2;
-    const S iS = S(T(1)) / Sigma;
-    const S iD = S(T(1)) / Delta;
-    const S is2 = S(T(1)) / safe_s2;
+    const S iS = rcp_g(Sigma);
+    const S iD = rcp_g(Delta);
+    const S is2 = rcp_g(safe_s2);
     const S Q = P * iD, U = W * is2;
     d[0] = Delta * y[3] * iS;
     d[1] = y[4] * iS;
