@@ -35,7 +35,14 @@
 //     instead of at 1.02 r_+ (see diff_trace), and ends once it moves outward
 //     beyond r_out (escaped rays are black here).
 // Integration is the reference's fixed-step Kerr RK4 with its pole damping
-// (kerr_hamilton.h:165-178), checks and escape as geodesic_kernel.cu:351-401.
+// (kerr_hamilton.h:165-178), checks and escape as geodesic_kernel.cu:351-401,
+// with sin(theta) and cos(theta) carried as two more state components
+// (ds = cos(theta) dtheta, dc = -sin(theta) dtheta, put back on the unit
+// circle after each step by n = 3/2 - (s^2 + c^2)/2): the right-hand side and
+// the pole damping read them instead of evaluating sin and cos, while theta
+// itself is still integrated for the crossing test, the swept angle and the
+// slab's path length.
+
 
 #pragma once
 
@@ -130,6 +137,47 @@ inline V3<T> diff_disc_colour(const Params<T>& u, const KConst<T>& c, T cam_r, T
     return vmul(col, flux * bands * g2 * g2);
 }
 
+// State of the form: the Kerr state and (sin theta, cos theta).
+template <class T> struct DiffState {
+    KState<T> k;  // t unused, r, theta, phi, p_r, p_theta
+    T s, c;       // sin(theta), cos(theta)
+};
+
+// One fixed RK4 step of DiffState with the reference's pole damping
+// h clamp(5 |sin theta|, 0.05, 1) (kerr_hamilton.h:165-178).
+template <class T> inline DiffState<T> diff_rk4(const DiffState<T>& y, T h, const KConst<T>& cc) {
+    T as = y.s < OLIT(0.0) ? -y.s : y.s;
+    T ps = as * OLIT(5.0);
+    ps = (ps > OLIT(1.0)) ? OLIT(1.0) : ((ps < OLIT(0.05)) ? OLIT(0.05) : ps);
+    const T he = h * ps;
+    const T hh = OLIT(0.5) * he;
+    auto f = [&](const KState<T>& k, T st, T ct, T& ds, T& dc) {
+        const KState<T> d = kerr_rhs_sc<T, false>(k, st, ct, cc);
+        ds = ct * d.theta;
+        dc = -(st * d.theta);
+        return d;
+    };
+    T ds1, dc1, ds2, dc2, ds3, dc3, ds4, dc4;
+    const KState<T> k1 = f(y.k, y.s, y.c, ds1, dc1);
+    const KState<T> k2 = f(k_add_scaled(y.k, k1, hh), y.s + ds1 * hh, y.c + dc1 * hh, ds2, dc2);
+    const KState<T> k3 = f(k_add_scaled(y.k, k2, hh), y.s + ds2 * hh, y.c + dc2 * hh, ds3, dc3);
+    const KState<T> k4 = f(k_add_scaled(y.k, k3, he), y.s + ds3 * he, y.c + dc3 * he, ds4, dc4);
+    const T h6 = he / OLIT(6.0);
+    DiffState<T> o;
+    o.k.t = y.k.t;
+    o.k.r = rk4_combine(y.k.r, k1.r, k2.r, k3.r, k4.r, h6);
+    o.k.theta = rk4_combine(y.k.theta, k1.theta, k2.theta, k3.theta, k4.theta, h6);
+    o.k.phi = rk4_combine(y.k.phi, k1.phi, k2.phi, k3.phi, k4.phi, h6);
+    o.k.p_r = rk4_combine(y.k.p_r, k1.p_r, k2.p_r, k3.p_r, k4.p_r, h6);
+    o.k.p_theta = rk4_combine(y.k.p_theta, k1.p_theta, k2.p_theta, k3.p_theta, k4.p_theta, h6);
+    const T s1 = rk4_combine(y.s, ds1, ds2, ds3, ds4, h6);
+    const T c1 = rk4_combine(y.c, dc1, dc2, dc3, dc4, h6);
+    const T n = OLIT(1.5) - OLIT(0.5) * (s1 * s1 + c1 * c1);
+    o.s = s1 * n;
+    o.c = c1 * n;
+    return o;
+}
+
 template <class T> struct DiffOut {
     V3<T> hdr;
     std::uint32_t steps, crossings;
@@ -186,11 +234,14 @@ inline DiffOut<T> diff_trace_p(const sgx_uniforms& ub, T spin, T incl, T r_in_M,
     up_.spin_a = a;
     up_.r_in = r_in;
     up_.peak_T = peak_T;
-    KState<T> y;
+    DiffState<T> ys;
+    KState<T>& y = ys.k;
     KConst<T> c;
     DiffOut<T> out{v3(OLIT(0.0), OLIT(0.0), OLIT(0.0)), 0u, 0u};
     // kerr_init reads cos(cam_theta) itself; the closed-form frame above agrees with it.
     if (!kerr_init(cam, up_, y, c)) return out;
+    ys.s = si;
+    ys.c = ci;
     // Capture radius: the prograde equatorial photon orbit radius (the smallest
     // photon orbit; an ingoing ray from outside that gets inside it falls in)
     // less 0.05 M.  The fixed-step RK4 turns unstable as Delta -> 0, and the
@@ -210,13 +261,13 @@ inline DiffOut<T> diff_trace_p(const sgx_uniforms& ub, T spin, T incl, T r_in_M,
         if (y.r > u.escape_r) break;
         if (slab && (u.flags & SGX_FLAG_DISC_ON) && step > 0) {
             // emission and absorption of the step prev -> y, evaluated at y
-            const T z = y.r * M<T>::cos(y.theta);
+            const T z = y.r * ys.c;
             const T rho = slab_profile(z, H);
             T w = smooth01((y.r - r_in) / eps) * smooth01((u.r_out - y.r) / eps);
             if (fade) w = w * (OLIT(1.0) - smooth01((psi - T(o.fade_start)) / T(o.fade_width)));
             if (rho > OLIT(0.0) && w > OLIT(0.0)) {
                 const T dr = y.r - prev.r, dth = y.theta - prev.theta, dph = y.phi - prev.phi;
-                const T st = M<T>::sin(y.theta);
+                const T st = ys.s;
                 const T ds = M<T>::sqrt(dr * dr + y.r * y.r * (dth * dth + st * st * dph * dph));
                 const T alpha = w * (OLIT(1.0) - M<T>::exp(-kappa * rho * ds));
                 ++out.crossings;
@@ -253,9 +304,9 @@ inline DiffOut<T> diff_trace_p(const sgx_uniforms& ub, T spin, T incl, T r_in_M,
         // region) and nothing emits out there
         if (y.p_r > OLIT(0.0) && y.r > u.r_out) break;
         prev = y;
-        y = kerr_rk4(y, u.h_step, c);
+        ys = diff_rk4(ys, u.h_step, c);
         if (fade) {
-            const T dth = y.theta - prev.theta, dph = y.phi - prev.phi, st = M<T>::sin(y.theta);
+            const T dth = y.theta - prev.theta, dph = y.phi - prev.phi, st = ys.s;
             psi_prev = psi;
             psi = psi + M<T>::sqrt(dth * dth + st * st * dph * dph);
         }

@@ -5,34 +5,26 @@
 // (kerr_hamilton.h:97-178), derived by hand: given the adjoint of a step's
 // output, they return the adjoint of its input state and of the constants
 // (E, L_z, a).  The adjoint sweep of sgx_diff.cu multiplies by these instead
-// of building the step's 6 x 9 Jacobian with dual numbers: four right-hand
-// side evaluations and four reverse passes per step instead of nine-lane
+// of building the step's 8 x 11 Jacobian with dual numbers: four right-hand
+// side evaluations and four reverse passes per step instead of eleven-lane
 // dual arithmetic.
 //
-// Host-and-device code (plain arithmetic, sinf/cosf/sqrtf overloads), so the
-// derivatives can be checked against finite differences on the CPU.
+// Host-and-device code (plain arithmetic, sqrt overloads, the SFU reciprocal
+// on the device in FP32), so the derivatives can be checked against finite
+// differences on the CPU.
 #pragma once
 
 #include <cmath>
 
 #if defined(__CUDACC__)
 #define SGX_HD __host__ __device__ __forceinline__
-// The right-hand side and its reverse pass are called four times per step;
-// one out-of-line copy each keeps the adjoint kernel inside the
-// instruction cache.
-#define SGX_HD_CALL __host__ __device__ __noinline__
 #else
 #define SGX_HD inline
-#define SGX_HD_CALL inline
 #endif
 
 namespace sgxa {
 
-SGX_HD float hsin(float x) { return sinf(x); }
-SGX_HD float hcos(float x) { return cosf(x); }
 SGX_HD float hsqrt(float x) { return sqrtf(x); }
-SGX_HD double hsin(double x) { return sin(x); }
-SGX_HD double hcos(double x) { return cos(x); }
 SGX_HD double hsqrt(double x) { return sqrt(x); }
 // 1/x: PTX rcp.approx.ftz.f32 on the device in FP32 (one SFU instruction, at
 // most 1 ulp from 1/x; the forward kernel's rhs_g does the same), exact
@@ -47,26 +39,11 @@ SGX_HD float hrcp(float x) {
 #endif
 }
 SGX_HD double hrcp(double x) { return 1.0 / x; }
-// sine and cosine from one range reduction on the device
-SGX_HD void hsincos(float x, float* s, float* c) {
-#if defined(__CUDA_ARCH__)
-    sincosf(x, s, c);
-#else
-    *s = sinf(x);
-    *c = cosf(x);
-#endif
-}
-SGX_HD void hsincos(double x, double* s, double* c) {
-#if defined(__CUDA_ARCH__)
-    sincos(x, s, c);
-#else
-    *s = sin(x);
-    *c = cos(x);
-#endif
-}
-
-// State layout: y[0..5] = r, theta, phi, p_r, p_theta, psi (swept angle);
-// derivative layout d[0..4] = dr, dtheta, dphi, dp_r, dp_theta.
+// State layout: y[0..7] = r, theta, phi, p_r, p_theta, psi (swept angle),
+// s = sin(theta), c = cos(theta); derivative layout d[0..6] = dr, dtheta,
+// dphi, dp_r, dp_theta, ds, dc.  theta is integrated for the swept angle and
+// the emission's path length; the right-hand side reads (s, c).
+SGX_HD constexpr int sidx(int i) { return i < 5 ? i : i + 1; }  // state index of derivative i
 
 // The right-hand side in Carter's separated form (the same Hamiltonian as
 // kerr_hamilton.h:97-155): with P = (r^2 + a^2) E - a L, W = L - a E s2,
@@ -74,9 +51,12 @@ SGX_HD void hsincos(double x, double* s, double* c) {
 //   dr = Delta p_r / Sigma, dth = p_th / Sigma, dphi = (a Q + U) / Sigma,
 //   dp_r  = (r N / Sigma + (M - r)(p_r^2 + Q^2) + 2 E r Q) / Sigma,
 //   dp_th = -sin(th) cos(th) (a^2 N / Sigma - U (2 a E + U)) / Sigma.
-// Operation for operation the forward kernel's rhs_g (sgx_diff_impl.cuh).
+// plus ds = cos(th) dth, dc = -sin(th) dth, with sin(th), cos(th) read from
+// the state.  Operation for operation the forward kernel's rhs_g7
+// (sgx_diff_impl.cuh).
 template <class T>
-SGX_HD_CALL void rhs_sc(const T* y, T st, T ct, T E, T L, T a, T M, T* d) {
+SGX_HD void rhs7(const T* y, T E, T L, T a, T M, T* d) {
+    const T st = y[6], ct = y[7];
     const T r = y[0];
     const T a2 = a * a;
     const T s2 = st * st;
@@ -98,20 +78,17 @@ SGX_HD_CALL void rhs_sc(const T* y, T st, T ct, T E, T L, T a, T M, T* d) {
     const T NiS = N * iS;
     d[3] = (r * NiS + ((M - r) * (Q * Q + pr2) + (T(2) * E * r) * Q)) * iS;
     d[4] = -(iS * (st * ct)) * (a2 * NiS - U * (T(2) * aE + U));
+    d[5] = ct * d[1];
+    d[6] = -(st * d[1]);
 }
 
-template <class T> SGX_HD void rhs(const T* y, T E, T L, T a, T M, T* d) {
-    T st, ct;
-    hsincos(y[1], &st, &ct);
-    rhs_sc(y, st, ct, E, L, a, M, d);
-}
-
-// w . d(rhs)/d(r, theta, p_r, p_theta, E, L, a), w the adjoint of d[0..4],
-// with st, ct = sin, cos of y[1].  gy[0..4] receives the state part (gy[2] = 0:
-// the right-hand side does not depend on phi); gc[0..2] += the constants' part.
+// w . d(rhs7)/d(r, p_r, p_theta, sin th, cos th, E, L, a), w the adjoint of
+// d[0..6].  gy[0..7] receives the state part (zero for theta, phi and psi,
+// which the right-hand side does not read); gc[0..2] += the constants' part.
 template <class T>
-SGX_HD_CALL void rhs_vjp_sc(const T* y, T st, T ct, T E, T L, T a, T M, const T* w, T* gy, T* gc) {
+SGX_HD void rhs_vjp7(const T* y, T E, T L, T a, T M, const T* w, T* gy, T* gc) {
     // forward intermediates
+    const T st = y[6], ct = y[7];
     const T r = y[0], pr = y[3], pth = y[4];
     const T a2 = a * a;
     const T s2 = st * st;
@@ -137,8 +114,10 @@ SGX_HD_CALL void rhs_vjp_sc(const T* y, T st, T ct, T E, T L, T a, T M, const T*
     const T B4 = a2 * NiS - U * V1;
     const T sc = st * ct;
 
-    // reverse: d0 = Del pr iS, d1 = pth iS, d2 = C2 iS, d3 = A3 iS, d4 = -(iS sc) B4
-    const T w0 = w[0], w1 = w[1], w2 = w[2], w3 = w[3], w4 = w[4];
+    // reverse: d5 = ct d1, d6 = -st d1 fold into d1's adjoint;
+    // d0 = Del pr iS, d1 = pth iS, d2 = C2 iS, d3 = A3 iS, d4 = -(iS sc) B4
+    const T d1v = pth * iS;
+    const T w0 = w[0], w1 = w[1] + w[5] * ct - w[6] * st, w2 = w[2], w3 = w[3], w4 = w[4];
     T iS_b = w0 * Del * pr + w1 * pth + w2 * C2 + w3 * A3 - w4 * sc * B4;
     T Del_b = w0 * pr * iS;
     T pr_b = w0 * Del * iS;
@@ -209,32 +188,29 @@ SGX_HD_CALL void rhs_vjp_sc(const T* y, T st, T ct, T E, T L, T a, T M, const T*
     pr_b += T(2) * pr * pr2_b;
     r_b += T(2) * r * r2_b;
     a_b += T(2) * a * a2_b;
-    // sc = st ct ; c2 = ct^2 ; s2 = st^2 ; st, ct of theta
-    const T st_b = sc_b * ct + T(2) * st * s2_b;
-    const T ct_b = sc_b * st + T(2) * ct * c2_b;
+    // sc = st ct ; c2 = ct^2 ; s2 = st^2 ; and d5, d6
+    const T st_b = sc_b * ct + T(2) * st * s2_b - w[6] * d1v;
+    const T ct_b = sc_b * st + T(2) * ct * c2_b + w[5] * d1v;
 
     gy[0] = r_b;
-    gy[1] = st_b * ct - ct_b * st;
+    gy[1] = T(0);
     gy[2] = T(0);
     gy[3] = pr_b;
     gy[4] = pth_b;
+    gy[5] = T(0);
+    gy[6] = st_b;
+    gy[7] = ct_b;
     gc[0] += E_b;
     gc[1] += L_b;
     gc[2] += a_b;
 }
 
-template <class T> SGX_HD void rhs_vjp(const T* y, T E, T L, T a, T M, const T* w, T* gy, T* gc) {
-    T st, ct;
-    hsincos(y[1], &st, &ct);
-    rhs_vjp_sc(y, st, ct, E, L, a, M, w, gy, gc);
-}
-
-// Pole-damped step length h * clamp(5 |sin(theta)|, 0.05, 1) and its theta
-// derivative (kerr_hamilton.h:165-178).
-template <class T> SGX_HD T damped_h_sc(T h, T s, T c, T* dh_dth) {
+// Pole-damped step length h * clamp(5 |s|, 0.05, 1) and its derivative in s
+// (kerr_hamilton.h:165-178, |sin theta| read from the state).
+template <class T> SGX_HD T damped_h_s(T h, T s, T* dh_ds) {
     const T as = s < T(0) ? -s : s;
     T ps = as * T(5);
-    T dps = (s < T(0) ? T(-5) : T(5)) * c;
+    T dps = s < T(0) ? T(-5) : T(5);
     if (ps > T(1)) {
         ps = T(1);
         dps = T(0);
@@ -242,129 +218,135 @@ template <class T> SGX_HD T damped_h_sc(T h, T s, T c, T* dh_dth) {
         ps = T(0.05);
         dps = T(0);
     }
-    *dh_dth = h * dps;
+    *dh_ds = h * dps;
     return h * ps;
 }
-template <class T> SGX_HD T damped_h(T h, T th, T* dh_dth) {
-    T s, c;
-    hsincos(th, &s, &c);
-    return damped_h_sc(h, s, c, dh_dth);
-}
 
-// One RK4 step y -> o (with the swept angle when `fade`).
+// One RK4 step y -> o: (s, c) back on the unit circle by
+// n = 3/2 - (s^2 + c^2)/2, and the swept angle when `fade`.
 template <class T> SGX_HD void step(const T* y, T E, T L, T a, T M, T h, bool fade, T* o) {
     T dhd;
-    const T he = damped_h(h, y[1], &dhd);
+    const T he = damped_h_s(h, y[6], &dhd);
     const T hh = T(0.5) * he;
-    T k1[5], k2[5], k3[5], k4[5], t[5];
-    rhs(y, E, L, a, M, k1);
-    for (int i = 0; i < 5; ++i) t[i] = y[i] + k1[i] * hh;
-    rhs(t, E, L, a, M, k2);
-    for (int i = 0; i < 5; ++i) t[i] = y[i] + k2[i] * hh;
-    rhs(t, E, L, a, M, k3);
-    for (int i = 0; i < 5; ++i) t[i] = y[i] + k3[i] * he;
-    rhs(t, E, L, a, M, k4);
+    T k1[7], k2[7], k3[7], k4[7], t[8];
+    t[5] = y[5];
+    rhs7(y, E, L, a, M, k1);
+    for (int i = 0; i < 7; ++i) t[sidx(i)] = y[sidx(i)] + k1[i] * hh;
+    rhs7(t, E, L, a, M, k2);
+    for (int i = 0; i < 7; ++i) t[sidx(i)] = y[sidx(i)] + k2[i] * hh;
+    rhs7(t, E, L, a, M, k3);
+    for (int i = 0; i < 7; ++i) t[sidx(i)] = y[sidx(i)] + k3[i] * he;
+    rhs7(t, E, L, a, M, k4);
     const T h6 = he / T(6);
-    for (int i = 0; i < 5; ++i) o[i] = y[i] + ((k1[i] + k2[i] * T(2)) + (k3[i] * T(2) + k4[i])) * h6;
+    for (int i = 0; i < 7; ++i) o[sidx(i)] = y[sidx(i)] + ((k1[i] + k2[i] * T(2)) + (k3[i] * T(2) + k4[i])) * h6;
+    const T n = T(1.5) - T(0.5) * (o[6] * o[6] + o[7] * o[7]);
+    o[6] = o[6] * n;
+    o[7] = o[7] * n;
     if (fade) {
-        const T dth = o[1] - y[1], dph = o[2] - y[2], s = hsin(o[1]);
+        const T dth = o[1] - y[1], dph = o[2] - y[2], s = o[6];
         o[5] = y[5] + hsqrt(dth * dth + s * s * dph * dph);
     } else {
         o[5] = y[5];
     }
 }
 
-// Adjoint of one step: lam (adjoint of the step's output, 6 components) is
+// Adjoint of one step: lam (adjoint of the step's output, 8 components) is
 // replaced by the adjoint of its input; gc[0..2] += the step's terms of
 // dLoss/d(E, L, a).
 template <class T> SGX_HD void step_vjp(const T* y, T E, T L, T a, T M, T h, bool fade, T* lam, T* gc) {
-    // sin, cos of each stage's theta, shared by its right-hand side and reverse pass
-    T s1, c1, s2, c2, s3, c3, s4, c4;
-    hsincos(y[1], &s1, &c1);
     T dhd;
-    const T he = damped_h_sc(h, s1, c1, &dhd);
+    const T he = damped_h_s(h, y[6], &dhd);
     const T hh = T(0.5) * he;
-    T k1[5], k2[5], k3[5], k4[5], y2[6], y3[6], y4[6];
-    rhs_sc(y, s1, c1, E, L, a, M, k1);
-    for (int i = 0; i < 5; ++i) y2[i] = y[i] + k1[i] * hh;
-    hsincos(y2[1], &s2, &c2);
-    rhs_sc(y2, s2, c2, E, L, a, M, k2);
-    for (int i = 0; i < 5; ++i) y3[i] = y[i] + k2[i] * hh;
-    hsincos(y3[1], &s3, &c3);
-    rhs_sc(y3, s3, c3, E, L, a, M, k3);
-    for (int i = 0; i < 5; ++i) y4[i] = y[i] + k3[i] * he;
-    hsincos(y4[1], &s4, &c4);
-    rhs_sc(y4, s4, c4, E, L, a, M, k4);
+    T k1[7], k2[7], k3[7], k4[7], y2[8], y3[8], y4[8];
+    y2[5] = y3[5] = y4[5] = y[5];
+    rhs7(y, E, L, a, M, k1);
+    for (int i = 0; i < 7; ++i) y2[sidx(i)] = y[sidx(i)] + k1[i] * hh;
+    rhs7(y2, E, L, a, M, k2);
+    for (int i = 0; i < 7; ++i) y3[sidx(i)] = y[sidx(i)] + k2[i] * hh;
+    rhs7(y3, E, L, a, M, k3);
+    for (int i = 0; i < 7; ++i) y4[sidx(i)] = y[sidx(i)] + k3[i] * he;
+    rhs7(y4, E, L, a, M, k4);
     const T h6 = he / T(6);
-    T lo[5];
-    for (int i = 0; i < 5; ++i) lo[i] = lam[i];
-    T ly[6];
+    T ks[7];
+    for (int i = 0; i < 7; ++i) ks[i] = (k1[i] + k2[i] * T(2)) + (k3[i] * T(2) + k4[i]);
+    // RK4 output before and after the renormalisation of (s, c)
+    const T s_hat = y[6] + ks[5] * h6, c_hat = y[7] + ks[6] * h6;
+    const T n = T(1.5) - T(0.5) * (s_hat * s_hat + c_hat * c_hat);
+    const T os = s_hat * n;
+    T lo[8];
+    for (int i = 0; i < 8; ++i) lo[i] = lam[i];
+    T ly[8];
+    for (int i = 0; i < 8; ++i) ly[i] = T(0);
     ly[5] = lam[5];
-    // swept angle: o5 = y5 + sqrt(dth^2 + sin^2(o1) dph^2)
+    // swept angle: o5 = y5 + sqrt(dth^2 + os^2 dph^2)
     T l_y1_psi = T(0), l_y2_psi = T(0);
     if (fade && lam[5] != T(0)) {
-        T o1 = y[1], o2 = y[2];
-        {
-            const T s1 = (k1[1] + k2[1] * T(2)) + (k3[1] * T(2) + k4[1]);
-            const T s2 = (k1[2] + k2[2] * T(2)) + (k3[2] * T(2) + k4[2]);
-            o1 = y[1] + s1 * h6;
-            o2 = y[2] + s2 * h6;
-        }
-        const T dth = o1 - y[1], dph = o2 - y[2];
-        T s, c;
-        hsincos(o1, &s, &c);
-        const T q = hsqrt(dth * dth + s * s * dph * dph);
+        const T dth = ks[1] * h6, dph = ks[2] * h6;
+        const T q = hsqrt(dth * dth + os * os * dph * dph);
         if (q > T(0)) {
             const T iq = lam[5] / q;
-            lo[1] += iq * (dth + s * c * dph * dph);
-            lo[2] += iq * s * s * dph;
+            lo[1] += iq * dth;
+            lo[2] += iq * os * os * dph;
+            lo[6] += iq * os * dph * dph;
             l_y1_psi = -iq * dth;
-            l_y2_psi = -iq * s * s * dph;
+            l_y2_psi = -iq * os * os * dph;
         }
     }
-    // o = y + (k1 + 2 k2 + 2 k3 + k4) h6
-    T lk1[5], lk2[5], lk3[5], lk4[5];
+    // (os, oc) = n (s_hat, c_hat)
+    {
+        const T tt = lo[6] * s_hat + lo[7] * c_hat;
+        const T ls = lo[6] * n - s_hat * tt;
+        const T lc = lo[7] * n - c_hat * tt;
+        lo[6] = ls;
+        lo[7] = lc;
+    }
+    // o = y + ks h6
+    T lk1[7], lk2[7], lk3[7], lk4[7];
     T l_he = T(0);
-    for (int i = 0; i < 5; ++i) {
-        ly[i] = lo[i];
-        lk1[i] = lo[i] * h6;
-        lk2[i] = lo[i] * (T(2) * h6);
-        lk3[i] = lo[i] * (T(2) * h6);
-        lk4[i] = lo[i] * h6;
-        l_he += lo[i] * ((k1[i] + k2[i] * T(2)) + (k3[i] * T(2) + k4[i]));
+    for (int i = 0; i < 7; ++i) {
+        const T l = lo[sidx(i)];
+        ly[sidx(i)] += l;
+        lk1[i] = l * h6;
+        lk2[i] = l * (T(2) * h6);
+        lk3[i] = l * (T(2) * h6);
+        lk4[i] = l * h6;
+        l_he += l * ks[i];
     }
     l_he *= T(1) / T(6);
     ly[1] += l_y1_psi;
     ly[2] += l_y2_psi;
-    T g[5];
+    T g[8];
     // k4 = f(y4), y4 = y + he k3
-    rhs_vjp_sc(y4, s4, c4, E, L, a, M, lk4, g, gc);
-    for (int i = 0; i < 5; ++i) {
-        ly[i] += g[i];
-        lk3[i] += he * g[i];
-        l_he += g[i] * k3[i];
+    rhs_vjp7(y4, E, L, a, M, lk4, g, gc);
+    for (int i = 0; i < 7; ++i) {
+        const T gi = g[sidx(i)];
+        ly[sidx(i)] += gi;
+        lk3[i] += he * gi;
+        l_he += gi * k3[i];
     }
     T l_hh = T(0);
     // k3 = f(y3), y3 = y + hh k2
-    rhs_vjp_sc(y3, s3, c3, E, L, a, M, lk3, g, gc);
-    for (int i = 0; i < 5; ++i) {
-        ly[i] += g[i];
-        lk2[i] += hh * g[i];
-        l_hh += g[i] * k2[i];
+    rhs_vjp7(y3, E, L, a, M, lk3, g, gc);
+    for (int i = 0; i < 7; ++i) {
+        const T gi = g[sidx(i)];
+        ly[sidx(i)] += gi;
+        lk2[i] += hh * gi;
+        l_hh += gi * k2[i];
     }
     // k2 = f(y2), y2 = y + hh k1
-    rhs_vjp_sc(y2, s2, c2, E, L, a, M, lk2, g, gc);
-    for (int i = 0; i < 5; ++i) {
-        ly[i] += g[i];
-        lk1[i] += hh * g[i];
-        l_hh += g[i] * k1[i];
+    rhs_vjp7(y2, E, L, a, M, lk2, g, gc);
+    for (int i = 0; i < 7; ++i) {
+        const T gi = g[sidx(i)];
+        ly[sidx(i)] += gi;
+        lk1[i] += hh * gi;
+        l_hh += gi * k1[i];
     }
     // k1 = f(y)
-    rhs_vjp_sc(y, s1, c1, E, L, a, M, lk1, g, gc);
-    for (int i = 0; i < 5; ++i) ly[i] += g[i];
-    // he = h ps(theta), hh = he / 2
-    ly[1] += (l_he + T(0.5) * l_hh) * dhd;
-    for (int i = 0; i < 6; ++i) lam[i] = ly[i];
+    rhs_vjp7(y, E, L, a, M, lk1, g, gc);
+    for (int i = 0; i < 7; ++i) ly[sidx(i)] += g[sidx(i)];
+    // he = h ps(s), hh = he / 2
+    ly[6] += (l_he + T(0.5) * l_hh) * dhd;
+    for (int i = 0; i < 8; ++i) lam[i] = ly[i];
 }
 
 }  // namespace sgxa

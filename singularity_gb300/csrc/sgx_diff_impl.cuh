@@ -27,7 +27,7 @@ using namespace sgxd;
 
 constexpr int kCk = 64;       // steps between checkpoints
 constexpr int kMaxCross = 8;  // crossings recorded per ray (crossing model)
-constexpr int NS = 6;         // state: r, theta, phi, p_r, p_theta, psi (swept angle)
+constexpr int NS = 8;         // state: r, theta, phi, p_r, p_theta, psi (swept angle), sin(theta), cos(theta)
 constexpr int NC = NS + 1;    // checkpoint: state and transmittance
 
 template <class T> struct DiffConst {
@@ -79,11 +79,14 @@ template <class S> __device__ __forceinline__ S smooth01(const S& x) {
 }
 
 // Kerr Hamiltonian right-hand side (kerr_hamilton.h:97-155) in Carter's
-// separated form, generic in the scalar; operation for operation sgxa::rhs
-// (sgx_adjoint.cuh), which states the equations.
+// separated form, generic in the scalar, with sin(theta), cos(theta) read from
+// the state (y[6], y[7]); d[0..6] = dr, dtheta, dphi, dp_r, dp_theta, ds, dc.
+// Operation for operation sgxa::rhs7 (sgx_adjoint.cuh), which states the
+// equations.
 template <class S, class T>
-__device__ __forceinline__ void rhs_g_sc(const S* y, const S& st, const S& ct, const S& E, const S& L, const S& a,
-                                         T M, S* d) {
+__device__ __forceinline__ void rhs_g7(const S* y, const S& E, const S& L, const S& a, T M, S* d) {
+    const S& st = y[6];
+    const S& ct = y[7];
     const S r = y[0];
     const S a2 = a * a;
     const S s2 = st * st;
@@ -107,40 +110,41 @@ __device__ __forceinline__ void rhs_g_sc(const S* y, const S& st, const S& ct, c
     const S NiS = N * iS;
     d[3] = (r * NiS + ((S(M) - r) * (Q * Q + pr2) + (S(T(2)) * E * r) * Q)) * iS;
     d[4] = -(iS * (st * ct)) * (a2 * NiS - U * (S(T(2)) * aE + U));
+    d[5] = ct * d[1];
+    d[6] = -(st * d[1]);
 }
 
-template <class S, class T>
-__device__ __forceinline__ void rhs_g(const S* y, const S& E, const S& L, const S& a, T M, S* d) {
-    S st, ct;
-    DM<S>::sincos_(y[1], &st, &ct);
-    rhs_g_sc(y, st, ct, E, L, a, M, d);
-}
-
-// One fixed RK4 step with the reference's pole damping, plus the swept angle.
+// One fixed RK4 step with the reference's pole damping, plus the swept angle;
+// (sin theta, cos theta) integrated with the state and put back on the unit
+// circle by n = 3/2 - (s^2 + c^2)/2.  Operation for operation sgxa::step.
 template <class S, class T>
 __device__ __forceinline__ void step_g(const S* y, const S& E, const S& L, const S& a, T M, T h, bool fade, S* o) {
-    S st0, ct0;  // sin, cos of the step's theta: the pole damping and k1
-    DM<S>::sincos_(y[1], &st0, &ct0);
+    const S st0 = y[6];
     S ps = selv(value_of(st0) < T(0), -st0, st0) * S(T(5));
     ps = selv(value_of(ps) > T(1), S(T(1)), selv(value_of(ps) < T(0.05), S(T(0.05)), ps));
     const S he = S(h) * ps;
     const S hh = S(T(0.5)) * he;
-    S k1[5], k2[5], k3[5], k4[5], t[5];
-    rhs_g_sc(y, st0, ct0, E, L, a, M, k1);
+    S k1[7], k2[7], k3[7], k4[7], t[NS];
+    t[5] = y[5];
+    rhs_g7(y, E, L, a, M, k1);
 #pragma unroll
-    for (int i = 0; i < 5; ++i) t[i] = y[i] + k1[i] * hh;
-    rhs_g(t, E, L, a, M, k2);
+    for (int i = 0; i < 7; ++i) t[sgxa::sidx(i)] = y[sgxa::sidx(i)] + k1[i] * hh;
+    rhs_g7(t, E, L, a, M, k2);
 #pragma unroll
-    for (int i = 0; i < 5; ++i) t[i] = y[i] + k2[i] * hh;
-    rhs_g(t, E, L, a, M, k3);
+    for (int i = 0; i < 7; ++i) t[sgxa::sidx(i)] = y[sgxa::sidx(i)] + k2[i] * hh;
+    rhs_g7(t, E, L, a, M, k3);
 #pragma unroll
-    for (int i = 0; i < 5; ++i) t[i] = y[i] + k3[i] * he;
-    rhs_g(t, E, L, a, M, k4);
+    for (int i = 0; i < 7; ++i) t[sgxa::sidx(i)] = y[sgxa::sidx(i)] + k3[i] * he;
+    rhs_g7(t, E, L, a, M, k4);
     const S h6 = he / S(T(6));
 #pragma unroll
-    for (int i = 0; i < 5; ++i) o[i] = y[i] + ((k1[i] + k2[i] * S(T(2))) + (k3[i] * S(T(2)) + k4[i])) * h6;
+    for (int i = 0; i < 7; ++i)
+        o[sgxa::sidx(i)] = y[sgxa::sidx(i)] + ((k1[i] + k2[i] * S(T(2))) + (k3[i] * S(T(2)) + k4[i])) * h6;
+    const S n = S(T(1.5)) - S(T(0.5)) * (o[6] * o[6] + o[7] * o[7]);
+    o[6] = o[6] * n;
+    o[7] = o[7] * n;
     if (fade) {
-        const S dth = o[1] - y[1], dph = o[2] - y[2], st = DM<S>::sin_(o[1]);
+        const S dth = o[1] - y[1], dph = o[2] - y[2], st = o[6];
         o[5] = y[5] + DM<S>::sqrt_(dth * dth + st * st * dph * dph);
     } else {
         o[5] = y[5];
@@ -278,6 +282,8 @@ __device__ __forceinline__ bool init_g(const S& a, const S& incl, const DiffCons
     y[3] = g_rr * ur;
     y[4] = Sigma * uth;
     y[5] = S(T(0));
+    y[6] = si;
+    y[7] = ci;
     return true;
 }
 
@@ -285,9 +291,10 @@ __device__ __forceinline__ bool init_g(const S& a, const S& incl, const DiffCons
 // colour; false (alpha = 0) outside the layer, the annulus or past the fade.
 template <class S, class T>
 __device__ __forceinline__ bool slab_g(const S& r0, const S& th0, const S& ph0, const S& r1, const S& th1,
-                                       const S& ph1, const S& psi1, const S& L, const S& a, const S& r_in,
-                                       const S& t_scale, const DiffConst<T>& k, S* col, S& alpha) {
-    const S q = r1 * DM<S>::cos_(th1) / S(k.H);
+                                       const S& ph1, const S& psi1, const S& s1, const S& c1, const S& L,
+                                       const S& a, const S& r_in, const S& t_scale, const DiffConst<T>& k, S* col,
+                                       S& alpha) {
+    const S q = r1 * c1 / S(k.H);
     if (!(value_of(q) * value_of(q) < T(1))) return false;
     S w = smooth01((r1 - r_in) / S(k.eps)) * smooth01((S(k.r_out) - r1) / S(k.eps));
     if (k.fade) w = w * (S(T(1)) - smooth01((psi1 - S(k.fade_start)) / S(k.fade_width)));
@@ -295,8 +302,7 @@ __device__ __forceinline__ bool slab_g(const S& r0, const S& th0, const S& ph0, 
     const S b = S(T(1)) - q * q;
     const S rho = b * b;
     const S dr = r1 - r0, dth = th1 - th0, dph = ph1 - ph0;
-    const S st = DM<S>::sin_(th1);
-    const S ds = DM<S>::sqrt_(dr * dr + r1 * r1 * (dth * dth + st * st * dph * dph));
+    const S ds = DM<S>::sqrt_(dr * dr + r1 * r1 * (dth * dth + s1 * s1 * dph * dph));
     alpha = w * (S(T(1)) - DM<S>::exp_(-(S(k.kappa) * rho * ds)));
     const S T_local = disc_temperature(r1, r_in, S(k.peak_T) * t_scale);
     if (value_of(T_local) > T(0)) {
@@ -362,8 +368,8 @@ __global__ void __launch_bounds__(128) diff_forward_kernel(DiffConst<T> k, DiffP
                 if constexpr (SLAB) {
                     T col[3], alpha;
                     if (disc && n > 0 &&
-                        slab_g<T, T>(prev[0], prev[1], prev[2], y[0], y[1], y[2], y[5], L, a, r_in, p.t_scale, k,
-                                     col, alpha)) {
+                        slab_g<T, T>(prev[0], prev[1], prev[2], y[0], y[1], y[2], y[5], y[6], y[7], L, a, r_in,
+                                     p.t_scale, k, col, alpha)) {
 #pragma unroll
                         for (int c = 0; c < 3; ++c) hdr[c] = hdr[c] + tau * alpha * col[c];
                         tau = tau * (T(1) - alpha);
@@ -462,11 +468,11 @@ __device__ __forceinline__ void step_adjoint(const T* yp, T E, T L, T a, const D
         for (int i = 0; i < NS; ++i) lam[i] += pend[i];
         return;
     }
-    using D9 = Dual<T, 9>;
-    D9 yd[NS], od[NS];
+    using DJ = Dual<T, NS + 3>;
+    DJ yd[NS], od[NS];
 #pragma unroll
-    for (int i = 0; i < NS; ++i) yd[i] = D9::var(yp[i], i);
-    step_g<D9, T>(yd, D9::var(E, 6), D9::var(L, 7), D9::var(a, 8), k.M, k.h, fade, od);
+    for (int i = 0; i < NS; ++i) yd[i] = DJ::var(yp[i], i);
+    step_g<DJ, T>(yd, DJ::var(E, NS), DJ::var(L, NS + 1), DJ::var(a, NS + 2), k.M, k.h, fade, od);
     T nl[NS];
 #pragma unroll
     for (int i = 0; i < NS; ++i) {
@@ -477,9 +483,9 @@ __device__ __forceinline__ void step_adjoint(const T* yp, T E, T L, T a, const D
     }
 #pragma unroll
     for (int j = 0; j < NS; ++j) {
-        muE += lam[j] * od[j].d[6];
-        muL += lam[j] * od[j].d[7];
-        mua += lam[j] * od[j].d[8];
+        muE += lam[j] * od[j].d[NS];
+        muL += lam[j] * od[j].d[NS + 1];
+        mua += lam[j] * od[j].d[NS + 2];
     }
 #pragma unroll
     for (int i = 0; i < NS; ++i) lam[i] = nl[i] + pend[i];
@@ -516,7 +522,7 @@ __global__ void __launch_bounds__(128, 4) diff_backward_kernel(DiffConst<T> k, D
     T E, L, y0[NS];
     init_g<T, T>(a, p.incl, k, gx, gy, b.ox[s], b.oy[s], y0, E, L);
 
-    T lam[NS] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+    T lam[NS] = {};
     T muE = T(0), muL = T(0), mua = T(0), g_a = T(0), g_rin = T(0), g_ts = T(0);
     const bool fade = k.fade != 0u;
     T Y[kCk + 1][NS];
@@ -565,34 +571,36 @@ __global__ void __launch_bounds__(128, 4) diff_backward_kernel(DiffConst<T> k, D
             if constexpr (SLAB) {
                 tb[kk - kbeg] = tau;  // transmittance before step kk's emission
                 T col[3], alpha;
-                if (slab_g<T, T>(yp[0], yp[1], yp[2], yc[0], yc[1], yc[2], yc[5], L, a, r_in, p.t_scale, k, col,
-                                 alpha))
+                if (slab_g<T, T>(yp[0], yp[1], yp[2], yc[0], yc[1], yc[2], yc[5], yc[6], yc[7], L, a, r_in,
+                                 p.t_scale, k, col, alpha))
                     tau = tau * (T(1) - alpha);
             }
         }
         for (std::uint32_t kk = kend; kk > kbeg; --kk) {
             const T* yp = Y[kk - 1 - kbeg];
             const T* yc = Y[kk - kbeg];
-            T pend[NS] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+            T pend[NS] = {};
             using D = Dual<T, 11>;
+            using DS = Dual<T, 13>;
             if constexpr (SLAB) {
                 T colv[3], alv;
                 if ((k.flags & SGX_FLAG_DISC_ON) &&
-                    slab_g<T, T>(yp[0], yp[1], yp[2], yc[0], yc[1], yc[2], yc[5], L, a, r_in, p.t_scale, k, colv,
-                                 alv)) {
-                    // d(colour, alpha)/d(r0, th0, ph0, r1, th1, ph1, psi1, L, a, r_in, t_scale)
-                    D col[3], ald;
-                    slab_g<D, T>(D::var(yp[0], 0), D::var(yp[1], 1), D::var(yp[2], 2), D::var(yc[0], 3),
-                                 D::var(yc[1], 4), D::var(yc[2], 5), D::var(yc[5], 6), D::var(L, 7), D::var(a, 8),
-                                 D::var(r_in, 9), D::var(p.t_scale, 10), k, col, ald);
+                    slab_g<T, T>(yp[0], yp[1], yp[2], yc[0], yc[1], yc[2], yc[5], yc[6], yc[7], L, a, r_in,
+                                 p.t_scale, k, colv, alv)) {
+                    // d(colour, alpha)/d(r0, th0, ph0, r1, th1, ph1, psi1, L, a, r_in, t_scale, s1, c1)
+                    DS col[3], ald;
+                    slab_g<DS, T>(DS::var(yp[0], 0), DS::var(yp[1], 1), DS::var(yp[2], 2), DS::var(yc[0], 3),
+                                  DS::var(yc[1], 4), DS::var(yc[2], 5), DS::var(yc[5], 6), DS::var(yc[6], 11),
+                                  DS::var(yc[7], 12), DS::var(L, 7), DS::var(a, 8), DS::var(r_in, 9),
+                                  DS::var(p.t_scale, 10), k, col, ald);
                     const T tj = tb[kk - kbeg];
                     const T gcs = tj * alv;
                     const T gal = tj * (g[0] * (colv[0] - R[0]) + g[1] * (colv[1] - R[1]) + g[2] * (colv[2] - R[2]));
 #pragma unroll
                     for (int c = 0; c < 3; ++c) R[c] = alv * colv[c] + (T(1) - alv) * R[c];
-                    T qv[11];
+                    T qv[13];
 #pragma unroll
-                    for (int x = 0; x < 11; ++x)
+                    for (int x = 0; x < 13; ++x)
                         qv[x] = gcs * (g[0] * col[0].d[x] + g[1] * col[1].d[x] + g[2] * col[2].d[x]) + gal * ald.d[x];
                     pend[0] += qv[0];
                     pend[1] += qv[1];
@@ -605,6 +613,8 @@ __global__ void __launch_bounds__(128, 4) diff_backward_kernel(DiffConst<T> k, D
                     g_a += qv[8] * k.M;
                     g_rin += qv[9] * k.M;
                     g_ts += qv[10];
+                    lam[6] += qv[11];
+                    lam[7] += qv[12];
                 }
             } else {
                 for (std::uint32_t j = 0; j < nc; ++j) {
