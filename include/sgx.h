@@ -81,7 +81,8 @@ typedef struct sgx_render_opts {
                                     separated form, three reciprocals (default),
                                 1 = the reference's division-for-division form,
                                 2 = form 0 with the SFU's sine/cosine where |sin(theta)| >= 1/4
-                                    (FP32; faster, FP32-vs-FP64 image error ~1.2x) */
+                                    (fixed-step FP32 only; the adaptive integrator carries
+                                    sin/cos of theta in its state, so there 2 equals 0) */
     uint32_t tile_w;         /* ray order: tiles of tile_w x tile_h pixels, samples innermost;  */
     uint32_t tile_h;         /*   0 = whole rows (tile_w = width, tile_h = 1)                  */
 } sgx_render_opts;
