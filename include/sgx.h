@@ -80,9 +80,9 @@ typedef struct sgx_render_opts {
     uint32_t rhs_form;       /* Kerr right-hand side: 0 = the same Hamiltonian in Carter's
                                     separated form, three reciprocals (default),
                                 1 = the reference's division-for-division form,
-                                2 = form 0 with the SFU's sine/cosine where |sin(theta)| >= 1/4
-                                    (fixed-step FP32 only; the adaptive integrator carries
-                                    sin/cos of theta in its state, so there 2 equals 0) */
+                                2 = form 0 with sin/cos of theta carried in the fixed-step
+                                    state instead of evaluated per stage (FP32; the adaptive
+                                    integrator always carries them, so there 2 equals 0) */
     uint32_t tile_w;         /* ray order: tiles of tile_w x tile_h pixels, samples innermost;  */
     uint32_t tile_h;         /*   0 = whole rows (tile_w = width, tile_h = 1)                  */
 } sgx_render_opts;

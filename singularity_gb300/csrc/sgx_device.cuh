@@ -498,20 +498,11 @@ __device__ __forceinline__ KS<T> kerr_rhs_sep_sc(const KS<T>& s, T st, T ct, con
     return d;
 }
 
-// Kerr RHS forms: 0 = the reference's divisions, 1 = the separated form,
-// 2 = the separated form with the SFU's sine/cosine (FP32 only; CUDA's
-// __sincosf) wherever |sin(theta)| >= 1/4 — its absolute error (~4e-7) would
-// be a large relative error of the 1/sin^2 terms nearer the poles, where the
-// IEEE-accurate sincosf is kept.
-constexpr int RHS_REF = 0, RHS_SEP = 1, RHS_SEP_HWTRIG = 2;
+// Kerr RHS forms: 0 = the reference's divisions, 1 = the separated form.
+constexpr int RHS_REF = 0, RHS_SEP = 1;
 
 template <class T, int FORM> __device__ __forceinline__ void rhs_sincos(T x, T* s, T* c) {
-    if constexpr (FORM == RHS_SEP_HWTRIG && std::is_same_v<T, float>) {
-        __sincosf(x, s, c);
-        if (fabsf(*s) < 0.25f) sincosf(x, s, c);
-    } else {
-        DM<T>::sincos_(x, s, c);
-    }
+    DM<T>::sincos_(x, s, c);
 }
 
 template <class T, int FORM = RHS_SEP>
@@ -566,6 +557,39 @@ __device__ __forceinline__ KS<T> kerr_rk4(const KS<T>& y, T h, const View<T>& v,
     o.ph = y.ph + ((k1.ph + k2.ph * DLIT(2.0)) + (k3.ph * DLIT(2.0) + k4.ph)) * h6;
     o.pr = y.pr + ((k1.pr + k2.pr * DLIT(2.0)) + (k3.pr * DLIT(2.0) + k4.pr)) * h6;
     o.pth = y.pth + ((k1.pth + k2.pth * DLIT(2.0)) + (k3.pth * DLIT(2.0) + k4.pth)) * h6;
+    return o;
+}
+
+// The same step with sin(theta), cos(theta) carried alongside the state
+// (st, ct: in and out): the stages read them instead of evaluating sin and
+// cos (ds = cos dtheta, dc = -sin dtheta), and the pair is put back on the unit
+// circle after the step by n = 3/2 - (s^2 + c^2)/2; theta itself is still
+// integrated for the reference's crossing test.  Separated right-hand side.
+template <class T>
+__device__ __forceinline__ KS<T> kerr_rk4_sc(const KS<T>& y, T& st, T& ct, T h, const View<T>& v, const KC<T>& c) {
+    T ps = DM<T>::fmin_(DM<T>::fmax_((st < DLIT(0.0) ? -st : st) * DLIT(5.0), DLIT(0.05)), DLIT(1.0));
+    h = h * ps;
+    const T hh = DLIT(0.5) * h;
+    const KS<T> k1 = kerr_rhs_sep_sc(y, st, ct, v, c);
+    const T s1 = st + (ct * k1.th) * hh, c1 = ct - (st * k1.th) * hh;
+    const KS<T> k2 = kerr_rhs_sep_sc(ks_axpy(y, k1, hh), s1, c1, v, c);
+    const T s2 = st + (c1 * k2.th) * hh, c2 = ct - (s1 * k2.th) * hh;
+    const KS<T> k3 = kerr_rhs_sep_sc(ks_axpy(y, k2, hh), s2, c2, v, c);
+    const T s3 = st + (c2 * k3.th) * h, c3 = ct - (s2 * k3.th) * h;
+    const KS<T> k4 = kerr_rhs_sep_sc(ks_axpy(y, k3, h), s3, c3, v, c);
+    const T h6 = h / DLIT(6.0);
+    auto comb = [&](T y0, T a1, T a2, T a3, T a4) { return y0 + ((a1 + a2 * DLIT(2.0)) + (a3 * DLIT(2.0) + a4)) * h6; };
+    KS<T> o;
+    o.r = comb(y.r, k1.r, k2.r, k3.r, k4.r);
+    o.th = comb(y.th, k1.th, k2.th, k3.th, k4.th);
+    o.ph = comb(y.ph, k1.ph, k2.ph, k3.ph, k4.ph);
+    o.pr = comb(y.pr, k1.pr, k2.pr, k3.pr, k4.pr);
+    o.pth = comb(y.pth, k1.pth, k2.pth, k3.pth, k4.pth);
+    const T sn = comb(st, ct * k1.th, c1 * k2.th, c2 * k3.th, c3 * k4.th);
+    const T cn = comb(ct, -(st * k1.th), -(s1 * k2.th), -(s2 * k3.th), -(s3 * k4.th));
+    const T n = DLIT(1.5) - DLIT(0.5) * (sn * sn + cn * cn);
+    st = sn * n;
+    ct = cn * n;
     return o;
 }
 

@@ -62,17 +62,19 @@ __device__ __forceinline__ std::uint32_t pack_meta(std::uint32_t term, std::uint
 
 // Policy flags: bit 0 = separated-form Kerr RHS, bit 1 = mixed precision.
 constexpr int FL_FAST = 1;    // separated-form Kerr RHS
-constexpr int FL_HWTRIG = 4;  // ... with the SFU sine/cosine (FP32)
+constexpr int FL_SC = 4;      // fixed step: sin/cos of theta carried in the state
 constexpr int FL_MIXED = 2;
 
 // Kerr, fixed step (geodesic_kernel.cu:303-403).
 template <class T, int FL> struct KerrFixed {
     static constexpr int kMinBlocks = sizeof(T) == 4 ? 4 : 1;
     static constexpr bool FAST = (FL & FL_FAST) != 0;
-    static constexpr int FORM = FAST ? ((FL & FL_HWTRIG) ? RHS_SEP_HWTRIG : RHS_SEP) : RHS_REF;
+    static constexpr bool SC = (FL & FL_SC) != 0;
+    static constexpr int FORM = FAST ? RHS_SEP : RHS_REF;
     KS<T> y;
     KC<T> c;
     T prev_th, prev_r;
+    T s_th, c_th;  // SC: sin, cos of theta
     T t0, t1, t2;  // termination data: (r_cross, phi, T_local) or (theta, phi)
     std::uint32_t steps, term;
     static constexpr std::uint32_t rej = 0, zone = 0;
@@ -87,6 +89,10 @@ template <class T, int FL> struct KerrFixed {
         c = make_kc(v, E, L);
         prev_th = y.th;
         prev_r = y.r;
+        if constexpr (SC) {
+            s_th = v.sin_th;
+            c_th = v.cos_th;
+        }
         if (v.max_steps == 0u) {
             term = TERM_BUDGET;
             return false;
@@ -102,9 +108,14 @@ template <class T, int FL> struct KerrFixed {
         }
         if (y.r > v.escape_r) {
             term = TERM_ESCAPE;
-            t0 = DM<T>::sin_(y.th);
+            if constexpr (SC) {
+                t0 = s_th;
+                t2 = c_th;
+            } else {
+                t0 = DM<T>::sin_(y.th);
+                t2 = DM<T>::cos_(y.th);
+            }
             t1 = y.ph;
-            t2 = DM<T>::cos_(y.th);
             return true;
         }
         T frac;
@@ -121,7 +132,8 @@ template <class T, int FL> struct KerrFixed {
         }
         prev_th = y.th;
         prev_r = y.r;
-        y = kerr_rk4<T, FORM>(y, fixed_step_h(v, y.r), v, c);
+        if constexpr (SC) y = kerr_rk4_sc(y, s_th, c_th, fixed_step_h(v, y.r), v, c);
+        else y = kerr_rk4<T, FORM>(y, fixed_step_h(v, y.r), v, c);
         if (++steps >= v.max_steps) {
             term = TERM_BUDGET;
             return true;
@@ -199,7 +211,7 @@ template <class T, int FL> struct SchwFixed {
 // step() is one attempt; max_steps bounds the attempts.
 template <class T, int FL> struct KerrAdaptive {
     static constexpr bool FAST = (FL & FL_FAST) != 0;
-    static constexpr int FORM = FAST ? ((FL & FL_HWTRIG) ? RHS_SEP_HWTRIG : RHS_SEP) : RHS_REF;
+    static constexpr int FORM = FAST ? RHS_SEP : RHS_REF;
     static constexpr bool MIXED = (FL & FL_MIXED) != 0;
     static constexpr int kMinBlocks = sizeof(T) == 4 ? (MIXED ? 4 : 4) : 1;
     KSC<T> y, k1;  // theta carried as (sin theta, cos theta)
@@ -669,7 +681,8 @@ cudaError_t run_probe(const void* d_view, std::uint64_t n, const std::uint32_t* 
 // One call site per (metric, precision, integrator, RHS form): F is invoked
 // with the chosen <T, Policy, FL> as a generic lambda's template arguments.
 // rhs_form: 0 the separated form, 1 the reference's divisions, 2 the
-// separated form with the SFU sine/cosine (FP32; FP64 runs form 0).
+// separated form with sin/cos of theta carried in the fixed-step state (FP32;
+// FP64 runs form 0; the error-controlled form always carries them).
 template <class F>
 cudaError_t dispatch(int metric, int precision, int integrator, int rhs_form, F&& f) {
     const bool adaptive = integrator == SGX_INTEGRATOR_ADAPTIVE;
@@ -691,7 +704,7 @@ cudaError_t dispatch(int metric, int precision, int integrator, int rhs_form, F&
             return ref ? f.template operator()<double, KerrFixed, 0>()
                        : f.template operator()<double, KerrFixed, FL_FAST>();
         return ref  ? f.template operator()<float, KerrFixed, 0>()
-               : hw ? f.template operator()<float, KerrFixed, FL_FAST | FL_HWTRIG>()
+               : hw ? f.template operator()<float, KerrFixed, FL_FAST | FL_SC>()
                     : f.template operator()<float, KerrFixed, FL_FAST>();
     }
     // Schwarzschild: the reference's fixed-step integrator for every form.
