@@ -81,19 +81,54 @@ void print_help() {
 }
 
 // --- PNG (stored deflate blocks, no compression library) -------------------
-std::uint32_t crc32_of(const unsigned char* p, std::size_t n, std::uint32_t c = 0xFFFFFFFFu) {
-    static std::uint32_t table[256];
-    static bool init = false;
-    if (!init) {
+// CRC-32 (reflected, polynomial 0xEDB88320) by slicing-by-8: eight 256-entry
+// tables, eight input bytes per iteration.
+struct Crc32 {
+    std::uint32_t t[8][256];
+    Crc32() {
         for (std::uint32_t i = 0; i < 256; ++i) {
             std::uint32_t v = i;
             for (int k = 0; k < 8; ++k) v = (v & 1u) ? 0xEDB88320u ^ (v >> 1) : v >> 1;
-            table[i] = v;
+            t[0][i] = v;
         }
-        init = true;
+        for (std::uint32_t i = 0; i < 256; ++i)
+            for (int k = 1; k < 8; ++k) t[k][i] = (t[k - 1][i] >> 8) ^ t[0][t[k - 1][i] & 0xFFu];
     }
-    for (std::size_t i = 0; i < n; ++i) c = table[(c ^ p[i]) & 0xFFu] ^ (c >> 8);
-    return c;
+    // c: running value (start 0xFFFFFFFF; the stored CRC is c ^ 0xFFFFFFFF)
+    std::uint32_t update(std::uint32_t c, const unsigned char* p, std::size_t n) const {
+        while (n >= 8) {
+            const std::uint32_t lo = c ^ (std::uint32_t(p[0]) | std::uint32_t(p[1]) << 8 | std::uint32_t(p[2]) << 16 |
+                                          std::uint32_t(p[3]) << 24);
+            const std::uint32_t hi =
+                std::uint32_t(p[4]) | std::uint32_t(p[5]) << 8 | std::uint32_t(p[6]) << 16 | std::uint32_t(p[7]) << 24;
+            c = t[7][lo & 0xFFu] ^ t[6][(lo >> 8) & 0xFFu] ^ t[5][(lo >> 16) & 0xFFu] ^ t[4][lo >> 24] ^
+                t[3][hi & 0xFFu] ^ t[2][(hi >> 8) & 0xFFu] ^ t[1][(hi >> 16) & 0xFFu] ^ t[0][hi >> 24];
+            p += 8;
+            n -= 8;
+        }
+        while (n-- > 0) c = t[0][(c ^ *p++) & 0xFFu] ^ (c >> 8);
+        return c;
+    }
+};
+
+const Crc32& crc_tables() {
+    static const Crc32 t;
+    return t;
+}
+
+// Adler-32 with the modulo deferred over runs of 5552 bytes (the longest run
+// whose sums cannot overflow 32 bits).
+void adler_update(std::uint32_t& a, std::uint32_t& b, const unsigned char* p, std::size_t n) {
+    while (n > 0) {
+        std::size_t k = n < 5552 ? n : 5552;
+        n -= k;
+        while (k-- > 0) {
+            a += *p++;
+            b += a;
+        }
+        a %= 65521u;
+        b %= 65521u;
+    }
 }
 
 void put32(std::vector<unsigned char>& o, std::uint32_t v) {
@@ -108,47 +143,85 @@ void chunk(std::vector<unsigned char>& o, const char* type, const std::vector<un
     const std::size_t start = o.size();
     o.insert(o.end(), type, type + 4);
     o.insert(o.end(), body.begin(), body.end());
-    put32(o, crc32_of(o.data() + start, o.size() - start) ^ 0xFFFFFFFFu);
+    put32(o, crc_tables().update(0xFFFFFFFFu, o.data() + start, o.size() - start) ^ 0xFFFFFFFFu);
 }
 
+// RGBA8 image as a PNG: filter 0 on every row, the zlib stream as stored
+// (uncompressed) deflate blocks of at most 65535 bytes; the IDAT chunk is
+// assembled in one buffer (one copy of the pixels) and checksummed once.
 bool write_png_rgba8(const char* path, const std::uint8_t* px, std::uint32_t w, std::uint32_t h) {
-    std::vector<unsigned char> raw;
-    raw.reserve(std::size_t(h) * (std::size_t(w) * 4 + 1));
-    for (std::uint32_t y = 0; y < h; ++y) {
-        raw.push_back(0);
-        raw.insert(raw.end(), px + std::size_t(y) * w * 4, px + std::size_t(y + 1) * w * 4);
-    }
-    std::vector<unsigned char> z = {0x78, 0x01};
+    const std::size_t rowb = std::size_t(w) * 4;
+    const std::size_t raw_n = (rowb + 1) * h;  // filter byte + pixels, per row
+    const std::size_t nblk = raw_n == 0 ? 1 : (raw_n + 65534) / 65535;
+    const std::size_t idat_n = 2 + 5 * nblk + raw_n + 4;
+    if (idat_n > 0x7FFFFFFFu) return false;  // a PNG chunk holds at most 2^31 - 1 bytes
+    std::vector<unsigned char> idat(8 + idat_n + 4);
+    unsigned char* q = idat.data();
+    auto be32 = [](unsigned char* d, std::uint32_t v) {
+        d[0] = static_cast<unsigned char>(v >> 24);
+        d[1] = static_cast<unsigned char>(v >> 16);
+        d[2] = static_cast<unsigned char>(v >> 8);
+        d[3] = static_cast<unsigned char>(v);
+    };
+    be32(q, std::uint32_t(idat_n));
+    q[4] = 'I';
+    q[5] = 'D';
+    q[6] = 'A';
+    q[7] = 'T';
+    unsigned char* d = q + 8;
+    *d++ = 0x78;
+    *d++ = 0x01;
+    // the raw stream (row r: filter byte 0, then rowb pixel bytes) cut into blocks
     std::uint32_t a = 1, b = 0;
-    for (unsigned char c : raw) {
-        a = (a + c) % 65521u;
-        b = (b + a) % 65521u;
-    }
-    for (std::size_t off = 0; off < raw.size() || off == 0;) {
-        const std::size_t n = std::min<std::size_t>(65535, raw.size() - off);
-        const bool last = off + n >= raw.size();
-        z.push_back(last ? 1 : 0);
-        z.push_back(static_cast<unsigned char>(n & 0xFF));
-        z.push_back(static_cast<unsigned char>(n >> 8));
-        z.push_back(static_cast<unsigned char>(~n & 0xFF));
-        z.push_back(static_cast<unsigned char>((~n >> 8) & 0xFF));
-        z.insert(z.end(), raw.begin() + off, raw.begin() + off + n);
-        off += n;
-        if (last) break;
-    }
-    put32(z, (b << 16) | a);
-    std::vector<unsigned char> out = {0x89, 'P', 'N', 'G', '\r', '\n', 0x1A, '\n'};
+    std::size_t left = raw_n, row = 0, in_row = 0;  // in_row 0: the filter byte is next
+    const unsigned char zero = 0;
+    do {
+        const std::size_t n = left < 65535 ? left : 65535;
+        left -= n;
+        *d++ = left == 0 ? 1 : 0;
+        *d++ = static_cast<unsigned char>(n & 0xFF);
+        *d++ = static_cast<unsigned char>(n >> 8);
+        *d++ = static_cast<unsigned char>(~n & 0xFF);
+        *d++ = static_cast<unsigned char>((~n >> 8) & 0xFF);
+        for (std::size_t k = n; k > 0;) {
+            if (in_row == 0) {
+                *d++ = 0;
+                adler_update(a, b, &zero, 1);
+                in_row = 1;
+                --k;
+                continue;
+            }
+            const std::size_t take = std::min(k, rowb - (in_row - 1));
+            const unsigned char* src = px + row * rowb + (in_row - 1);
+            std::memcpy(d, src, take);
+            adler_update(a, b, src, take);
+            d += take;
+            k -= take;
+            in_row += take;
+            if (in_row == rowb + 1) {
+                in_row = 0;
+                ++row;
+            }
+        }
+    } while (left > 0);
+    be32(d, (b << 16) | a);
+    d += 4;
+    be32(d, crc_tables().update(0xFFFFFFFFu, q + 4, 4 + idat_n) ^ 0xFFFFFFFFu);
+    std::vector<unsigned char> head = {0x89, 'P', 'N', 'G', '\r', '\n', 0x1A, '\n'};
     std::vector<unsigned char> ihdr;
     put32(ihdr, w);
     put32(ihdr, h);
     ihdr.insert(ihdr.end(), {8, 6, 0, 0, 0});
-    chunk(out, "IHDR", ihdr);
-    chunk(out, "IDAT", z);
-    chunk(out, "IEND", {});
+    chunk(head, "IHDR", ihdr);
+    std::vector<unsigned char> tail;
+    chunk(tail, "IEND", {});
     std::FILE* f = std::fopen(path, "wb");
     if (f == nullptr) return false;
-    const bool ok = std::fwrite(out.data(), 1, out.size(), f) == out.size();
-    return (std::fclose(f) == 0) && ok;
+    bool ok = std::fwrite(head.data(), 1, head.size(), f) == head.size();
+    ok = ok && std::fwrite(idat.data(), 1, idat.size(), f) == idat.size();
+    ok = ok && std::fwrite(tail.data(), 1, tail.size(), f) == tail.size();
+    ok = (std::fclose(f) == 0) && ok;
+    return ok;
 }
 
 bool write_pfm(const char* path, const std::vector<float>& rgba, std::uint32_t w, std::uint32_t h) {
