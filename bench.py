@@ -250,8 +250,8 @@ def precision_study(S, N, O, lib, r, u, d_out, stream, torch, main_opts) -> dict
     out["note"] = ("speeds: one 16-spp 4K pass each; errors: full 256-spp frame, RGBA32F LDR mean, units of "
                    "full scale; Carter drift |Q_end-Q0|/(|Q0|+L^2+a^2E^2) and null-condition drift |2H_end|/E^2 "
                    "from the CPU oracle of the same integrator; E and L_z are constants of the Hamiltonian form "
-                   "(held exactly, zero drift by construction); rhs_form 2 (SFU sine/cosine) coincides with "
-                   "form 0 here: the error-controlled form evaluates no sine or cosine per stage")
+                   "(held exactly, zero drift by construction); rhs_form 2 (sin/cos of theta in the state) "
+                   "coincides with form 0 here: the error-controlled form always carries them")
     return out
 
 

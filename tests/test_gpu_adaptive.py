@@ -89,8 +89,8 @@ def test_fp32_vs_fp64_precision_target(renderer, oracle, sgx):
 
 def test_trig_forms_coincide_for_adaptive(renderer, sgx):
     """The error-controlled form carries (sin theta, cos theta) in its state and
-    evaluates no sine or cosine per stage, so rhs_form 2 (the SFU sine/cosine
-    of the fixed-step form) renders the same frame as form 0."""
+    evaluates no sine or cosine per stage, so rhs_form 2 (which makes the
+    fixed-step form carry them too) renders the same frame as form 0."""
     u = _scene(sgx, 64, 36, spp=4)
     a = renderer.render_image(u, sgx.default_opts(integrator=1, precision=0, rhs_form=0))
     b = renderer.render_image(u, sgx.default_opts(integrator=1, precision=0, rhs_form=2))
