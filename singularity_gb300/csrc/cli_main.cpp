@@ -62,6 +62,9 @@ void print_help() {
         "  --integrator fixed|adaptive   fixed-step RK4 (default) or error-controlled RK4\n"
         "  --precision fp32|mixed|fp64   arithmetic form (mixed: adaptive only)\n"
         "  --tolerance T                 adaptive error tolerance (default 1e-6)\n"
+        "  --rhs-form 0|1|2              Kerr right-hand side: 0 separated form (default),\n"
+        "                                1 the reference's divisions, 2 form 0 with sin/cos of\n"
+        "                                theta carried in the fixed-step state (FP32)\n"
         "  --peak-temp K                 disc peak temperature (default 4500)\n"
         "  --exposure X                  exposure before tone mapping (default 1.8)\n"
         "  --turbulence X                disc band amplitude (default 0.5)\n"
@@ -334,6 +337,14 @@ int main(int argc, char** argv) {
             have_opts = true;
         } else if (a == "--tolerance" && has_val) {
             opts.tolerance = std::strtof(argv[++i], nullptr);
+            have_opts = true;
+        } else if (a == "--rhs-form" && has_val) {
+            const std::string_view v = argv[++i];
+            if (v != "0" && v != "1" && v != "2") {
+                std::fprintf(stderr, "singularity_cuda_cli: --rhs-form must be 0, 1 or 2\n");
+                return 2;
+            }
+            opts.rhs_form = std::uint32_t(v[0] - '0');
             have_opts = true;
         } else if (a == "--peak-temp" && has_val) {
             peak_temp = std::strtof(argv[++i], nullptr);

@@ -48,6 +48,7 @@ def test_help(cli):
     (["--encode-mp4", "x.mp4"], "--encode-mp4 requires --frames > 1"),
     (["--integrator", "euler"], "--integrator must be fixed or adaptive"),
     (["--bloom-sigma", "100"], "--bloom-sigma must be in [0, 64]"),
+    (["--rhs-form", "3"], "--rhs-form must be 0, 1 or 2"),
 ])
 def test_usage_errors_exit_2(cli, args, msg):
     r = run(cli, *args)
@@ -165,3 +166,16 @@ def test_cli_bloom_and_seed(cli, tmp_path, sgx, renderer):
                 "--turbulence-seed", "7")
     assert plain.returncode == 0
     assert not np.array_equal(read_png(tmp_path / "p.png"), img)
+
+
+@pytest.mark.gpu
+def test_cli_rhs_form(cli, tmp_path, sgx, renderer):
+    """--rhs-form 2 renders the library's rhs_form 2 frame of the same scene
+    (sin/cos of theta carried in the fixed-step state), close to form 0."""
+    r = run(cli, "--output", tmp_path / "f2.png", "--res", "96x54", "--samples-per-pixel", "2", "--rhs-form", "2")
+    assert r.returncode == 0, r.stderr
+    img = read_png(tmp_path / "f2.png")
+    u = sgx.pack_uniforms(sgx.Scene(render_supersample=2), sgx.build_orbital_camera(30.0, 0.15, 0.0, 60.0), 96, 54)
+    np.testing.assert_array_equal(img, renderer.render_image(u, sgx.default_opts(rhs_form=2)))
+    f0 = renderer.render_image(u, sgx.default_opts())
+    assert (np.abs(img.astype(int) - f0.astype(int)).max(axis=-1) <= 1).mean() >= 0.99
