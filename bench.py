@@ -575,12 +575,14 @@ def main() -> None:
     achieved = ops_step * steps_per_launch / (per_launch_ms * 1e-3) / 1e12
     peak = C.c_double(0)
     lib.sgx_measure_fp32_peak(local, 20000, C.byref(peak))
+    # DRAM bytes of the trace kernel per launch: ncu dram__bytes_read.sum +
+    # dram__bytes_write.sum of one 4K 16-spp launch of the adaptive precision form
+    # (16.6 MB + 2072.5 MB for 132,710,400 rays; the 16-byte hit record per ray,
+    # part of it still in L2 when the kernel ends), in
+    # profiles/trace_persistent_kerr_adaptive_1280x720.md; other workloads: null
     traffic = None
-    tp = ROOT / "profiles" / "trace_kernel_traffic.json"
-    if tp.exists():
-        t = json.loads(tp.read_text())
-        key = f"{args.integrator}_bytes_per_ray"
-        traffic = t[key] * npix * SPP_PER_STEP if key in t else None
+    if args.integrator == "adaptive" and args.workload == "4k" and args.precision == "mixed":
+        traffic = 2089191680 / 132710400 * npix * SPP_PER_STEP
     roof = {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
             "frac": achieved / peak.value if peak.value else None, "traffic": traffic,
             "peak_source": "of measured: register-resident FMA ceiling (sgx_measure_fp32_peak) on this GPU; "
