@@ -39,7 +39,7 @@ def _oracle_opts(oracle, prec):
 
 
 @pytest.mark.parametrize("prec", ["f32", "mixed", "f64"])
-@pytest.mark.parametrize("spin,incl", [(0.94, 75.0), (0.5, 60.0), (0.0, 85.0), (0.998, 20.0)])
+@pytest.mark.parametrize("spin,incl", [(0.94, 75.0), (0.5, 60.0), (0.0, 85.0), (0.998, 20.0), (0.94, 1.0)])
 def test_probe_matches_adaptive_oracle(renderer, oracle, sgx, prec, spin, incl):
     u = _scene(sgx, 64, 36, spp=4, spin=spin, incl_deg=incl)
     rng = np.random.default_rng(3)
