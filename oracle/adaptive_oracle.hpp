@@ -27,6 +27,14 @@
 //     h <= h_max_frac * r, written with IEEE sqrt and division (the GPU's FP32
 //     path evaluates the same factor as 0.85 * 2^(-log2(err)/4) on its
 //     special-function unit, so its step sizes differ in the last bits);
+//   * early capture: a ray with Q >= 0 that is inside both its spherical
+//     photon orbit radius r_c(xi) less 0.05 M and the disc's inner edge while
+//     moving inward ends as captured.  A photon from outside that reaches
+//     r < r_c(xi) has eta > eta_c(xi) (for eta < eta_c the two radial turning
+//     points bracket r_c and the outer one stops it; Teo 2003), so no turning
+//     point is left outside the horizon, and inside r_in it can no longer
+//     reach the disc: the reference's 1.02 r_+ cut would end it with the same
+//     (black) result, after the smallest steps of its path;
 //   * equatorial crossings: a sign change of cos(theta) with sin(theta) > 0
 //     (the reference's theta = pi/2 crossing for theta in (0, pi)), located on
 //     the cubic Hermite interpolant of cos(theta) over the accepted step
@@ -62,7 +70,8 @@ struct AdaptiveOpts {
     float zone;           // mixed form: FP64 control band half-width in M (0.05)
     std::uint32_t max_steps;  // attempt budget (accepted + rejected); 0 -> the uniforms' max_steps
     std::uint32_t mixed;      // 1: the mixed precision form (T = float only)
-    std::uint32_t pad0, pad1;
+    std::uint32_t no_early_capture;  // 1: only the reference's horizon cut ends a captured ray (tests)
+    std::uint32_t pad1;
 };
 
 // Per-ray diagnostics for the precision comparison.
@@ -265,8 +274,14 @@ inline TraceOut<T> trace_kerr_adaptive(const CamRay<T>& cam, const Params<T>& u,
     const std::uint32_t max_steps = o.max_steps != 0u ? o.max_steps : u.max_steps;
     const T hcut = kerr_horizon_cut(u.mass_M, u.spin_a);
     const T r_plus = u.mass_M + M<T>::sqrt(M<T>::fmax(u.mass_M * u.mass_M - u.spin_a * u.spin_a, OLIT(0.0)));
-    const T r_c = mixed ? photon_orbit_radius(u.spin_a, u.mass_M, c.L / c.E) : OLIT(0.0);
+    const T r_c = photon_orbit_radius(u.spin_a, u.mass_M, c.L / c.E);
     const T zone = T(o.zone);
+    // early capture radius: min(r_c - 0.05 M, r_in) for Q >= 0, else none
+    T r_cap = OLIT(0.0);
+    if (o.no_early_capture == 0u && c.Q >= OLIT(0.0) && M<T>::isfinite(r_c)) {
+        r_cap = r_c - OLIT(0.05) * u.mass_M;
+        r_cap = r_cap < u.r_in ? r_cap : u.r_in;
+    }
 
     T h = T(o.h_init_frac) * y.r;
     SCState<T> k1 = sc_rhs(y, c);
@@ -277,7 +292,7 @@ inline TraceOut<T> trace_kerr_adaptive(const CamRay<T>& cam, const Params<T>& u,
             out = {black, steps, TERM_BUDGET};
             break;
         }
-        if (!M<T>::isfinite(y.r) || y.r < hcut) {
+        if (!M<T>::isfinite(y.r) || y.r < hcut || (y.r < r_cap && y.p_r < OLIT(0.0))) {
             out = {black, steps, TERM_HORIZON};
             break;
         }

@@ -28,12 +28,14 @@ REFERENCE_ROOT = Path(os.environ.get("SGX_REFERENCE_ROOT", "/root/reference"))
 
 class AdaptiveOpts(C.Structure):
     _fields_ = [("tol", C.c_float), ("h_init_frac", C.c_float), ("h_max_frac", C.c_float), ("zone", C.c_float),
-                ("max_steps", C.c_uint32), ("mixed", C.c_uint32), ("pad0", C.c_uint32), ("pad1", C.c_uint32)]
+                ("max_steps", C.c_uint32), ("mixed", C.c_uint32), ("no_early_capture", C.c_uint32),
+                ("pad1", C.c_uint32)]
 
 
-def adaptive_opts(tol=1e-6, h_init_frac=0.02, h_max_frac=0.1, zone=0.05, max_steps=0, mixed=False) -> "AdaptiveOpts":
+def adaptive_opts(tol=1e-6, h_init_frac=0.02, h_max_frac=0.1, zone=0.05, max_steps=0, mixed=False,
+                  early_capture=True) -> "AdaptiveOpts":
     """The adaptive integrator's options (defaults = the library's defaults)."""
-    return AdaptiveOpts(tol, h_init_frac, h_max_frac, zone, max_steps, int(bool(mixed)), 0, 0)
+    return AdaptiveOpts(tol, h_init_frac, h_max_frac, zone, max_steps, int(bool(mixed)), int(not early_capture), 0)
 
 
 class RayDiag(C.Structure):

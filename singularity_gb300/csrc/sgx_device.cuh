@@ -728,6 +728,11 @@ template <class T> __device__ __forceinline__ void renormalise(KSC<T>& y) {
     y.c = y.c * n;
 }
 
+// Carter constant at the camera (geodesic_kernel.cu:340-344).
+template <class T> __device__ __forceinline__ T carter_Q(const View<T>& v, T E, T L, T pth) {
+    return pth * pth + v.cos_th * v.cos_th * (L * L / DM<T>::fmax_(v.s2_c, DLIT(1e-6)) - v.a2 * E * E);
+}
+
 template <class T> struct KAttempt {
     KSC<T> y4, k4, k5;
     T h6;

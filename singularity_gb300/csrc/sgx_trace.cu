@@ -217,6 +217,7 @@ template <class T, int FL> struct KerrAdaptive {
     KSC<T> y, k1;  // theta carried as (sin theta, cos theta)
     KC<T> c;
     T h, r_c;
+    T r_cap;  // early capture: inside min(r_c - 0.05 M, r_in) moving inward (0: never)
     T t0, t1, t2;
     std::uint32_t steps, term, rej, zone;
 
@@ -239,10 +240,13 @@ template <class T, int FL> struct KerrAdaptive {
             L = float(Ld);
             y.pr = float(prd);
             y.pth = float(pthd);
-            r_c = photon_orbit_radius(v, L / E);
-        } else {
-            r_c = DLIT(0.0);
         }
+        // a photon from outside inside its spherical photon orbit radius r_c(xi) has no
+        // radial turning point left (Teo 2003); inside r_in it cannot reach the disc
+        r_c = photon_orbit_radius(v, L / E);
+        r_cap = DLIT(0.0);
+        if (finite_(r_c) && carter_Q(v, E, L, y.pth) >= DLIT(0.0))
+            r_cap = DM<T>::fmin_(r_c - DLIT(0.05) * v.M, v.r_in);
         c = make_kc(v, E, L);
         h = T(pass.h_init_frac) * y.r;
         k1 = kerr_rhs_scs<T, FORM>(y, v, c);
@@ -254,8 +258,9 @@ template <class T, int FL> struct KerrAdaptive {
     }
 
     __device__ __forceinline__ bool step(const View<T>& v, const PassDesc& pass) {
-        if (!(y.r >= v.hcut && y.r <= v.escape_r)) {  // one test for NaN, capture and escape
-            if (!finite_(y.r) || y.r < v.hcut) {
+        // one test for NaN, capture (the reference's cut or the early one) and escape
+        if (!(y.r >= v.hcut && y.r <= v.escape_r) || (y.r < r_cap && y.pr < DLIT(0.0))) {
+            if (!finite_(y.r) || y.r < v.hcut || y.r < r_cap) {
                 term = TERM_HORIZON;
             } else {
                 term = TERM_ESCAPE;

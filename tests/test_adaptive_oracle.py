@@ -107,3 +107,25 @@ def test_schwarzschild_metric_keeps_fixed_step(oracle, sgx):
     a, _ = oracle.render(u, adaptive=oracle.adaptive_opts())
     b, _ = oracle.render(u)
     np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("spin,incl,dist", [(0.94, 75.0, 40.0), (0.0, 60.0, 20.0), (0.998, 30.0, 15.0), (0.6, 85.0, 60.0)])
+def test_early_capture_changes_no_result(oracle, sgx, spin, incl, dist):
+    """A ray inside both its photon-orbit radius (less 0.05 M) and the disc's
+    inner edge, moving inward with Q >= 0, ends as captured: the same
+    termination and colour as tracing on to the reference's 1.02 r_+ cut,
+    in fewer attempts."""
+    u = _scene(sgx, 96, 54, spin=spin, dist=dist, incl_deg=incl, fov=45.0, max_steps=4000)
+    n = u.width * u.height
+    gy, gx = np.divmod(np.arange(n, dtype=np.uint32), u.width)
+    s = np.zeros(n, np.uint32)
+    for prec, mixed in (("f32", False), ("f32", True), ("f64", False)):
+        on = oracle.trace(u, gx, gy, s, precision=prec, adaptive=oracle.adaptive_opts(mixed=mixed))
+        off = oracle.trace(u, gx, gy, s, precision=prec, adaptive=oracle.adaptive_opts(mixed=mixed,
+                                                                                      early_capture=False))
+        np.testing.assert_array_equal(on[2], off[2])
+        np.testing.assert_array_equal(on[0], off[0])
+        assert np.all(on[1] <= off[1])
+        captured = on[2] == 0
+        if captured.any():
+            assert on[1][captured].mean() < off[1][captured].mean()
