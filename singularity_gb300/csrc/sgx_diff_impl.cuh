@@ -287,13 +287,15 @@ __device__ __forceinline__ bool init_g(const S& a, const S& incl, const DiffCons
     return true;
 }
 
-// Slab emission of the step y0 -> y1, evaluated at y1: absorption alpha and
-// colour; false (alpha = 0) outside the layer, the annulus or past the fade.
+// Slab emission of the step y0 -> y1, evaluated at y1, in two parts: the
+// absorption alpha (false, alpha = 0, outside the layer, the annulus or past
+// the fade) and the colour.  The colour depends on (r1, ph1, L, a, r_in,
+// t_scale) only, so the adjoint differentiates the parts over their own
+// inputs (10 and 6 dual lanes instead of 13).
 template <class S, class T>
-__device__ __forceinline__ bool slab_g(const S& r0, const S& th0, const S& ph0, const S& r1, const S& th1,
-                                       const S& ph1, const S& psi1, const S& s1, const S& c1, const S& L,
-                                       const S& a, const S& r_in, const S& t_scale, const DiffConst<T>& k, S* col,
-                                       S& alpha) {
+__device__ __forceinline__ bool slab_alpha_g(const S& r0, const S& th0, const S& ph0, const S& r1, const S& th1,
+                                             const S& ph1, const S& psi1, const S& s1, const S& c1, const S& r_in,
+                                             const DiffConst<T>& k, S& alpha) {
     const S q = r1 * c1 / S(k.H);
     if (!(value_of(q) * value_of(q) < T(1))) return false;
     S w = smooth01((r1 - r_in) / S(k.eps)) * smooth01((S(k.r_out) - r1) / S(k.eps));
@@ -304,12 +306,27 @@ __device__ __forceinline__ bool slab_g(const S& r0, const S& th0, const S& ph0, 
     const S dr = r1 - r0, dth = th1 - th0, dph = ph1 - ph0;
     const S ds = DM<S>::sqrt_(dr * dr + r1 * r1 * (dth * dth + s1 * s1 * dph * dph));
     alpha = w * (S(T(1)) - DM<S>::exp_(-(S(k.kappa) * rho * ds)));
+    return true;
+}
+
+template <class S, class T>
+__device__ __forceinline__ void slab_colour_g(const S& r1, const S& ph1, const S& L, const S& a, const S& r_in,
+                                              const S& t_scale, const DiffConst<T>& k, S* col) {
     const S T_local = disc_temperature(r1, r_in, S(k.peak_T) * t_scale);
     if (value_of(T_local) > T(0)) {
         disc_colour_g(r1, ph1, L, a, r_in, T_local, k, col);
     } else {
         col[0] = col[1] = col[2] = S(T(0));
     }
+}
+
+template <class S, class T>
+__device__ __forceinline__ bool slab_g(const S& r0, const S& th0, const S& ph0, const S& r1, const S& th1,
+                                       const S& ph1, const S& psi1, const S& s1, const S& c1, const S& L,
+                                       const S& a, const S& r_in, const S& t_scale, const DiffConst<T>& k, S* col,
+                                       S& alpha) {
+    if (!slab_alpha_g(r0, th0, ph0, r1, th1, ph1, psi1, s1, c1, r_in, k, alpha)) return false;
+    slab_colour_g(r1, ph1, L, a, r_in, t_scale, k, col);
     return true;
 }
 
@@ -581,40 +598,46 @@ __global__ void __launch_bounds__(128, 4) diff_backward_kernel(DiffConst<T> k, D
             const T* yc = Y[kk - kbeg];
             T pend[NS] = {};
             using D = Dual<T, 11>;
-            using DS = Dual<T, 13>;
+            using DA = Dual<T, 10>;
+            using DC = Dual<T, 6>;
             if constexpr (SLAB) {
                 T colv[3], alv;
                 if ((k.flags & SGX_FLAG_DISC_ON) &&
                     slab_g<T, T>(yp[0], yp[1], yp[2], yc[0], yc[1], yc[2], yc[5], yc[6], yc[7], L, a, r_in,
                                  p.t_scale, k, colv, alv)) {
-                    // d(colour, alpha)/d(r0, th0, ph0, r1, th1, ph1, psi1, L, a, r_in, t_scale, s1, c1)
-                    DS col[3], ald;
-                    slab_g<DS, T>(DS::var(yp[0], 0), DS::var(yp[1], 1), DS::var(yp[2], 2), DS::var(yc[0], 3),
-                                  DS::var(yc[1], 4), DS::var(yc[2], 5), DS::var(yc[5], 6), DS::var(yc[6], 11),
-                                  DS::var(yc[7], 12), DS::var(L, 7), DS::var(a, 8), DS::var(r_in, 9),
-                                  DS::var(p.t_scale, 10), k, col, ald);
+                    // d alpha / d(r0, th0, ph0, r1, th1, ph1, psi1, s1, c1, r_in)
+                    DA ald;
+                    slab_alpha_g<DA, T>(DA::var(yp[0], 0), DA::var(yp[1], 1), DA::var(yp[2], 2), DA::var(yc[0], 3),
+                                        DA::var(yc[1], 4), DA::var(yc[2], 5), DA::var(yc[5], 6), DA::var(yc[6], 7),
+                                        DA::var(yc[7], 8), DA::var(r_in, 9), k, ald);
+                    // d colour / d(r1, ph1, L, a, r_in, t_scale)
+                    DC col[3];
+                    slab_colour_g<DC, T>(DC::var(yc[0], 0), DC::var(yc[2], 1), DC::var(L, 2), DC::var(a, 3),
+                                         DC::var(r_in, 4), DC::var(p.t_scale, 5), k, col);
                     const T tj = tb[kk - kbeg];
                     const T gcs = tj * alv;
                     const T gal = tj * (g[0] * (colv[0] - R[0]) + g[1] * (colv[1] - R[1]) + g[2] * (colv[2] - R[2]));
 #pragma unroll
                     for (int c = 0; c < 3; ++c) R[c] = alv * colv[c] + (T(1) - alv) * R[c];
-                    T qv[13];
+                    T qa[10], qc[6];
 #pragma unroll
-                    for (int x = 0; x < 13; ++x)
-                        qv[x] = gcs * (g[0] * col[0].d[x] + g[1] * col[1].d[x] + g[2] * col[2].d[x]) + gal * ald.d[x];
-                    pend[0] += qv[0];
-                    pend[1] += qv[1];
-                    pend[2] += qv[2];
-                    lam[0] += qv[3];
-                    lam[1] += qv[4];
-                    lam[2] += qv[5];
-                    lam[5] += qv[6];
-                    muL += qv[7];
-                    g_a += qv[8] * k.M;
-                    g_rin += qv[9] * k.M;
-                    g_ts += qv[10];
-                    lam[6] += qv[11];
-                    lam[7] += qv[12];
+                    for (int x = 0; x < 10; ++x) qa[x] = gal * ald.d[x];
+#pragma unroll
+                    for (int x = 0; x < 6; ++x)
+                        qc[x] = gcs * (g[0] * col[0].d[x] + g[1] * col[1].d[x] + g[2] * col[2].d[x]);
+                    pend[0] += qa[0];
+                    pend[1] += qa[1];
+                    pend[2] += qa[2];
+                    lam[0] += qa[3] + qc[0];
+                    lam[1] += qa[4];
+                    lam[2] += qa[5] + qc[1];
+                    lam[5] += qa[6];
+                    lam[6] += qa[7];
+                    lam[7] += qa[8];
+                    muL += qc[2];
+                    g_a += qc[3] * k.M;
+                    g_rin += (qa[9] + qc[4]) * k.M;
+                    g_ts += qc[5];
                 }
             } else {
                 for (std::uint32_t j = 0; j < nc; ++j) {
