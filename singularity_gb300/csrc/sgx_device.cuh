@@ -707,8 +707,40 @@ template <class T> struct KSC {
     T r, s, c, ph, pr, pth;
 };
 
+// Packed FP32 pairs (PTX .f32x2, sm_100 and later): one instruction performs
+// the operation on both lanes with the scalar instruction's rounding, so a
+// component-wise update of the state costs half the issue slots.
+struct F2 {
+    unsigned long long v;
+};
+__device__ __forceinline__ F2 f2(float a, float b) {
+    F2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void unf2(F2 x, float& a, float& b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(x.v)); }
+__device__ __forceinline__ F2 fma2(F2 a, F2 b, F2 c) {
+    F2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(a.v), "l"(b.v), "l"(c.v));
+    return r;
+}
+__device__ __forceinline__ F2 add2(F2 a, F2 b) {
+    F2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+
 template <class T> __device__ __forceinline__ KSC<T> ksc_axpy(const KSC<T>& y, const KSC<T>& k, T f) {
-    return KSC<T>{y.r + k.r * f, y.s + k.s * f, y.c + k.c * f, y.ph + k.ph * f, y.pr + k.pr * f, y.pth + k.pth * f};
+    if constexpr (std::is_same_v<T, float>) {
+        const F2 ff = f2(f, f);
+        KSC<T> o;
+        unf2(fma2(f2(k.s, k.c), ff, f2(y.s, y.c)), o.s, o.c);
+        unf2(fma2(f2(k.r, k.ph), ff, f2(y.r, y.ph)), o.r, o.ph);
+        unf2(fma2(f2(k.pr, k.pth), ff, f2(y.pr, y.pth)), o.pr, o.pth);
+        return o;
+    } else {
+        return KSC<T>{y.r + k.r * f, y.s + k.s * f, y.c + k.c * f, y.ph + k.ph * f, y.pr + k.pr * f, y.pth + k.pth * f};
+    }
 }
 
 template <class T, int FORM>
@@ -748,15 +780,30 @@ __device__ __forceinline__ KAttempt<T> kerr_attempt(const KSC<T>& y, const KSC<T
     const KSC<T> k3 = kerr_rhs_scs<T, FORM>(ksc_axpy(y, k2, hh), v, c);
     at.k4 = kerr_rhs_scs<T, FORM>(ksc_axpy(y, k3, h), v, c);
     at.h6 = h * DLIT(0.16666666666666666);  // h/6 as a product (the oracle alike)
-    auto comb = [&](T y0, T a1, T a2, T a3, T a4) {
-        return y0 + ((a1 + a2 * DLIT(2.0)) + (a3 * DLIT(2.0) + a4)) * at.h6;
-    };
-    at.y4.r = comb(y.r, k1.r, k2.r, k3.r, at.k4.r);
-    at.y4.s = comb(y.s, k1.s, k2.s, k3.s, at.k4.s);
-    at.y4.c = comb(y.c, k1.c, k2.c, k3.c, at.k4.c);
-    at.y4.ph = comb(y.ph, k1.ph, k2.ph, k3.ph, at.k4.ph);
-    at.y4.pr = comb(y.pr, k1.pr, k2.pr, k3.pr, at.k4.pr);
-    at.y4.pth = comb(y.pth, k1.pth, k2.pth, k3.pth, at.k4.pth);
+    if constexpr (std::is_same_v<T, float>) {
+        // y0 + (fma(a2, 2, a1) + fma(a3, 2, a4)) h6 on component pairs
+        const F2 two = f2(2.0f, 2.0f), h6 = f2(at.h6, at.h6);
+        auto comb2 = [&](F2 y0, F2 a1, F2 a2, F2 a3, F2 a4) {
+            return fma2(add2(fma2(a2, two, a1), fma2(a3, two, a4)), h6, y0);
+        };
+        unf2(comb2(f2(y.s, y.c), f2(k1.s, k1.c), f2(k2.s, k2.c), f2(k3.s, k3.c), f2(at.k4.s, at.k4.c)), at.y4.s,
+             at.y4.c);
+        unf2(comb2(f2(y.r, y.ph), f2(k1.r, k1.ph), f2(k2.r, k2.ph), f2(k3.r, k3.ph), f2(at.k4.r, at.k4.ph)), at.y4.r,
+             at.y4.ph);
+        unf2(comb2(f2(y.pr, y.pth), f2(k1.pr, k1.pth), f2(k2.pr, k2.pth), f2(k3.pr, k3.pth),
+                   f2(at.k4.pr, at.k4.pth)),
+             at.y4.pr, at.y4.pth);
+    } else {
+        auto comb = [&](T y0, T a1, T a2, T a3, T a4) {
+            return y0 + ((a1 + a2 * DLIT(2.0)) + (a3 * DLIT(2.0) + a4)) * at.h6;
+        };
+        at.y4.r = comb(y.r, k1.r, k2.r, k3.r, at.k4.r);
+        at.y4.s = comb(y.s, k1.s, k2.s, k3.s, at.k4.s);
+        at.y4.c = comb(y.c, k1.c, k2.c, k3.c, at.k4.c);
+        at.y4.ph = comb(y.ph, k1.ph, k2.ph, k3.ph, at.k4.ph);
+        at.y4.pr = comb(y.pr, k1.pr, k2.pr, k3.pr, at.k4.pr);
+        at.y4.pth = comb(y.pth, k1.pth, k2.pth, k3.pth, at.k4.pth);
+    }
     at.k5 = kerr_rhs_scs<T, FORM>(at.y4, v, c);
     return at;
 }
