@@ -455,6 +455,34 @@ template <class T> __device__ __forceinline__ KS<T> kerr_rhs_ref(const KS<T>& s,
     return kerr_rhs_ref_sc(s, st, ct, v, c);
 }
 
+// Packed FP32 pairs (PTX .f32x2, sm_100 and later): one instruction performs
+// the operation on both lanes with the scalar instruction's rounding, so a
+// component-wise update of the state costs half the issue slots.
+struct F2 {
+    unsigned long long v;
+};
+__device__ __forceinline__ F2 f2(float a, float b) {
+    F2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void unf2(F2 x, float& a, float& b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(x.v)); }
+__device__ __forceinline__ F2 fma2(F2 a, F2 b, F2 c) {
+    F2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(a.v), "l"(b.v), "l"(c.v));
+    return r;
+}
+__device__ __forceinline__ F2 mul2(F2 a, F2 b) {
+    F2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+__device__ __forceinline__ F2 add2(F2 a, F2 b) {
+    F2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+
 // The same Hamiltonian in Carter's separated form (Carter 1968), with three
 // reciprocals.  With s2 = sin^2(theta), P = (r^2 + a^2) E - a L and
 // W = L - a E s2,
@@ -471,6 +499,34 @@ template <class T> __device__ __forceinline__ KS<T> kerr_rhs_ref(const KS<T>& s,
 // applies to U as it does to the reference's L^2/s2 terms.
 template <class T>
 __device__ __forceinline__ KS<T> kerr_rhs_sep_sc(const KS<T>& s, T st, T ct, const View<T>& v, const KC<T>& c) {
+    if constexpr (std::is_same_v<T, float>) {
+        // the same operations with independent pairs packed (.f32x2)
+        const float r = s.r, a2 = v.a2;
+        float s2, c2, pr2, pth2;
+        unf2(mul2(f2(st, ct), f2(st, ct)), s2, c2);
+        unf2(mul2(f2(s.pr, s.pth), f2(s.pr, s.pth)), pr2, pth2);
+        const float safe_s2 = fmaxf(s2, 1e-10f);
+        const float r2 = r * r;
+        const float r2a2 = r2 + a2;
+        const float Sigma = r2 + a2 * c2;
+        const float Delta = r2a2 - v.twoM * r;
+        const float P = r2a2 * c.E - c.aL;
+        const float W = c.L - c.aE * s2;
+        const float iS = DM<float>::rcp_fast(Sigma);
+        const float iD = DM<float>::rcp_fast(Delta);
+        const float is2 = DM<float>::rcp_fast(safe_s2);
+        float Q, U;
+        unf2(mul2(f2(P, W), f2(iD, is2)), Q, U);
+        KS<T> d;
+        d.th = s.pth * iS;
+        unf2(mul2(f2(Delta * s.pr, v.a * Q + U), f2(iS, iS)), d.r, d.ph);
+        const float N = ((Delta * pr2 + pth2) - P * Q) + W * U;
+        const float NiS = N * iS;
+        const float A3 = r * NiS + ((v.M - r) * (Q * Q + pr2) + (c.twoE * r) * Q);
+        const float B4 = a2 * NiS - U * (c.twoaE + U);
+        unf2(mul2(f2(A3, B4), f2(iS, -(iS * (st * ct)))), d.pr, d.pth);
+        return d;
+    }
     const T r = s.r;
     const T a2 = v.a2;
     const T s2 = st * st;
@@ -707,29 +763,6 @@ template <class T> struct KSC {
     T r, s, c, ph, pr, pth;
 };
 
-// Packed FP32 pairs (PTX .f32x2, sm_100 and later): one instruction performs
-// the operation on both lanes with the scalar instruction's rounding, so a
-// component-wise update of the state costs half the issue slots.
-struct F2 {
-    unsigned long long v;
-};
-__device__ __forceinline__ F2 f2(float a, float b) {
-    F2 r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(a), "f"(b));
-    return r;
-}
-__device__ __forceinline__ void unf2(F2 x, float& a, float& b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(x.v)); }
-__device__ __forceinline__ F2 fma2(F2 a, F2 b, F2 c) {
-    F2 r;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(a.v), "l"(b.v), "l"(c.v));
-    return r;
-}
-__device__ __forceinline__ F2 add2(F2 a, F2 b) {
-    F2 r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
-    return r;
-}
-
 template <class T> __device__ __forceinline__ KSC<T> ksc_axpy(const KSC<T>& y, const KSC<T>& k, T f) {
     if constexpr (std::is_same_v<T, float>) {
         const F2 ff = f2(f, f);
@@ -749,7 +782,13 @@ __device__ __forceinline__ KSC<T> kerr_rhs_scs(const KSC<T>& y, const View<T>& v
     KS<T> d;
     if constexpr (FORM != RHS_REF) d = kerr_rhs_sep_sc(k, y.s, y.c, v, c);
     else d = kerr_rhs_ref_sc(k, y.s, y.c, v, c);
-    return KSC<T>{d.r, y.c * d.th, -(y.s * d.th), d.ph, d.pr, d.pth};
+    if constexpr (std::is_same_v<T, float>) {
+        float ds, dc;
+        unf2(mul2(f2(y.c, y.s), f2(d.th, -d.th)), ds, dc);
+        return KSC<T>{d.r, ds, dc, d.ph, d.pr, d.pth};
+    } else {
+        return KSC<T>{d.r, y.c * d.th, -(y.s * d.th), d.ph, d.pr, d.pth};
+    }
 }
 
 // (s, c) back to the unit circle after an accepted step: one Newton step of
