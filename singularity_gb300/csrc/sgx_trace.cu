@@ -68,6 +68,7 @@ constexpr int FL_MIXED = 2;
 // Kerr, fixed step (geodesic_kernel.cu:303-403).
 template <class T, int FL> struct KerrFixed {
     static constexpr int kMinBlocks = sizeof(T) == 4 ? 4 : 1;
+    static constexpr int kMinBlocksMulti = kMinBlocks;
     static constexpr bool FAST = (FL & FL_FAST) != 0;
     static constexpr bool SC = (FL & FL_SC) != 0;
     static constexpr int FORM = FAST ? RHS_SEP : RHS_REF;
@@ -147,6 +148,7 @@ template <class T, int FL> struct KerrFixed {
 // Schwarzschild, fixed step (geodesic_kernel.cu:229-297).
 template <class T, int FL> struct SchwFixed {
     static constexpr int kMinBlocks = sizeof(T) == 4 ? 4 : 1;
+    static constexpr int kMinBlocksMulti = kMinBlocks;
     SS<T> y;
     T prev_th, prev_r, prev_uph;
     T t0, t1, t2;
@@ -213,7 +215,11 @@ template <class T, int FL> struct KerrAdaptive {
     static constexpr bool FAST = (FL & FL_FAST) != 0;
     static constexpr int FORM = FAST ? RHS_SEP : RHS_REF;
     static constexpr bool MIXED = (FL & FL_MIXED) != 0;
-    static constexpr int kMinBlocks = sizeof(T) == 4 ? (MIXED ? 4 : 4) : 1;
+    static constexpr int kMinBlocks = sizeof(T) == 4 ? 4 : 1;
+    // Multi-view passes hold their view's constants in shared memory and
+    // registers rather than the constant bank: 80 registers (3 blocks) beat
+    // 64 with spills there (1954 against 1877 Mrays/s on six 4K views).
+    static constexpr int kMinBlocksMulti = sizeof(T) == 4 ? 3 : 1;
     KSC<T> y, k1;  // theta carried as (sin theta, cos theta)
     KC<T> c;
     T h, r_c;
@@ -430,13 +436,14 @@ enum : int { MODE_IDLE = 0, MODE_ACTIVE = 1, MODE_DONE = 2 };
 // view, tiles of tile_w x tile_h pixels (padded to whole tiles), the pixels
 // of a tile row-major, and a pixel's samples innermost; ids that land in the
 // padding carry no work.  Each policy names its resident blocks of 256 per
-// SM (kMinBlocks), which caps its registers: 4 = 64 registers, 3 = 80;
-// FP64 variants keep their registers (capped they spill up to 1.4 KB).
+// SM (kMinBlocks for a single view, kMinBlocksMulti for a batch), which caps
+// its registers: 4 = 64 registers, 3 = 80; FP64 variants keep their
+// registers (capped they spill up to 1.4 KB).
 // ONE: a single-view pass whose constants arrive as the kernel parameter
 // `one`, read from the constant bank as instruction operands instead of
 // shared-memory loads held in registers.
 template <class T, class Ray, bool ONE>
-__global__ void __launch_bounds__(256, Ray::kMinBlocks)
+__global__ void __launch_bounds__(256, ONE ? Ray::kMinBlocks : Ray::kMinBlocksMulti)
     trace_persistent(const __grid_constant__ PassDesc pass, const __grid_constant__ View<T> one) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     // Block totals of the ray counters and each lane's record slot live in
