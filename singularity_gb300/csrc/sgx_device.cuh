@@ -795,8 +795,12 @@ __device__ __forceinline__ KSC<T> kerr_rhs_scs(const KSC<T>& y, const View<T>& v
 // 1/sqrt(x) at x = 1 (s^2 + c^2 stays within ~1e-6 of 1 between steps).
 template <class T> __device__ __forceinline__ void renormalise(KSC<T>& y) {
     const T n = DLIT(1.5) - DLIT(0.5) * (y.s * y.s + y.c * y.c);
-    y.s = y.s * n;
-    y.c = y.c * n;
+    if constexpr (std::is_same_v<T, float>) {
+        unf2(mul2(f2(y.s, y.c), f2(n, n)), y.s, y.c);
+    } else {
+        y.s = y.s * n;
+        y.c = y.c * n;
+    }
 }
 
 // Carter constant at the camera (geodesic_kernel.cu:340-344).
@@ -881,21 +885,28 @@ __device__ __forceinline__ C error_norm(const KSC<T>& y, const KAttempt<T>& a, f
 
 // The same norm with one approximate reciprocal per component and a single
 // scale at the end: max_i |k4_i - k5_i| / (1 + max(|y_i|, |y4_i|)) * |h/6| / tol.
-// Equal to error_norm up to rounding (a few ulp), for the FP32 fast path.
-template <class T>
-__device__ __forceinline__ T error_norm_fast(const KSC<T>& y, const KAttempt<T>& a, float tol_f) {
-    auto one = [&](T yv, T y4v, T k4v, T k5v) {
-        const T m = DM<T>::fmax_(absv(yv), absv(y4v));
-        return absv(k4v - k5v) * DM<T>::rcp_fast(DLIT(1.0) + m);
+// Equal to error_norm up to rounding (a few ulp), for the FP32 fast path; the
+// subtractions, sums and products run on component pairs, k4 - k5 as
+// fma(k5, -1, k4) (one rounding, as the subtraction) and |d| / (1 + m) as
+// |d / (1 + m)|.
+__device__ __forceinline__ float error_norm_fast(const KSC<float>& y, const KAttempt<float>& a, float tol_f) {
+    const F2 one2 = f2(1.0f, 1.0f), neg1 = f2(-1.0f, -1.0f);
+    float q[6];
+    auto pair = [&](float ya, float yb, float y4a, float y4b, float k4a, float k4b, float k5a, float k5b, float& qa,
+                    float& qb) {
+        const F2 d = fma2(f2(k5a, k5b), neg1, f2(k4a, k4b));
+        float da, db;
+        unf2(add2(one2, f2(fmaxf(absv(ya), absv(y4a)), fmaxf(absv(yb), absv(y4b)))), da, db);
+        unf2(mul2(d, f2(DM<float>::rcp_fast(da), DM<float>::rcp_fast(db))), qa, qb);
     };
-    T e = one(y.r, a.y4.r, a.k4.r, a.k5.r);
-    e = DM<T>::fmax_(e, one(y.s, a.y4.s, a.k4.s, a.k5.s));
-    e = DM<T>::fmax_(e, one(y.c, a.y4.c, a.k4.c, a.k5.c));
-    e = DM<T>::fmax_(e, one(y.ph, a.y4.ph, a.k4.ph, a.k5.ph));
-    e = DM<T>::fmax_(e, one(y.pr, a.y4.pr, a.k4.pr, a.k5.pr));
-    e = DM<T>::fmax_(e, one(y.pth, a.y4.pth, a.k4.pth, a.k5.pth));
-    e = e * (absv(a.h6) * DM<T>::rcp_fast(T(tol_f)));
-    if (!(e <= DLIT(1e30))) e = DLIT(1e30);
+    pair(y.r, y.ph, a.y4.r, a.y4.ph, a.k4.r, a.k4.ph, a.k5.r, a.k5.ph, q[0], q[3]);
+    pair(y.s, y.c, a.y4.s, a.y4.c, a.k4.s, a.k4.c, a.k5.s, a.k5.c, q[1], q[2]);
+    pair(y.pr, y.pth, a.y4.pr, a.y4.pth, a.k4.pr, a.k4.pth, a.k5.pr, a.k5.pth, q[4], q[5]);
+    float e = absv(q[0]);
+#pragma unroll
+    for (int i = 1; i < 6; ++i) e = fmaxf(e, absv(q[i]));
+    e = e * (absv(a.h6) * DM<float>::rcp_fast(tol_f));
+    if (!(e <= 1e30f)) e = 1e30f;
     return e;
 }
 

@@ -291,7 +291,7 @@ template <class T, int FL> struct KerrAdaptive {
             accept = e <= 1.0;
             h = h * step_factor_fast(float(e));
         } else if constexpr (FAST && std::is_same_v<T, float>) {
-            const T e = error_norm_fast<T>(y, at, pass.tol);
+            const T e = error_norm_fast(y, at, pass.tol);
             accept = e <= DLIT(1.0);
             h = h * step_factor_fast(e);
         } else {
