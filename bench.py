@@ -255,14 +255,18 @@ def precision_study(S, N, O, lib, r, u, d_out, stream, torch, main_opts) -> dict
     return out
 
 
-def batch_study(S, N, r, torch, launches: int = 3, rank: int = 0, world: int = 1) -> dict:
+def batch_study(S, N, r, torch, launches: int = 3, rank: int = 0, world: int = 1, sample_cap: int = 0) -> dict:
     """Batched views: the 64 views of workloads.batch_64_views(0) in one persistent
     launch per batch, replayed from a CUDA graph, launch shape from the
     autotuner (timed on the views with samples capped at 4).  Under N ranks
     the views are split by cost (singularity_gb300.dist.split_by_cost) and the
-    rate is all ranks' rays over the slowest rank's time."""
+    rate is all ranks' rays over the slowest rank's time.  sample_cap > 0
+    caps every view's samples (a small case for kernel profiling)."""
     from singularity_gb300 import dist as D
     views_all = S.workloads.batch_64_views(0)
+    if sample_cap > 0:
+        for v in views_all:
+            v.supersample = max(1, min(v.supersample, sample_cap))
     parts = D.split_by_cost([D.view_cost(v.width, v.height, v.supersample) for v in views_all], world)
     views = [views_all[i] for i in parts[rank]]
     rays = sum(v.width * v.height * v.supersample for v in views)
@@ -293,6 +297,8 @@ def batch_study(S, N, r, torch, launches: int = 3, rank: int = 0, world: int = 1
         out["steps_per_ray"] = steps / max(1, rays)
     out["note"] = ("one graph replay renders all 64 views (every sample); adaptive FP32, tol 1e-6; device time; "
                    "gsteps_s = integrator attempts per second, comparable across workloads")
+    if sample_cap > 0:
+        out["note"] += f"; samples capped at {sample_cap} per view (small case)"
     return out
 
 
@@ -555,7 +561,8 @@ def main() -> None:
     # the batch shards its views across ranks: every rank takes part
     batch = None
     if not args.no_batch_study and args.precision != "fp64" and integ == N.INTEGRATOR_ADAPTIVE:
-        batch = batch_study(S, N, r, torch, rank=rank, world=world)
+        batch = batch_study(S, N, r, torch, rank=rank, world=world,
+                            sample_cap=2 if args.workload == "small" else 0)
 
     if rank != 0:
         if world > 1:
