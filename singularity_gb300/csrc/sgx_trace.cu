@@ -835,12 +835,19 @@ cudaError_t launch_accumulate(int precision, const ViewSet& vs, const void* resu
                               bool finalize, std::uint32_t format, void* out, cudaStream_t st) {
     const unsigned threads = 256;
     const std::uint64_t blocks = (vs.total_pix + threads - 1) / threads;
+    // a set of many FP64 views needs more than the default 48 KB of shared memory
     if (precision == SGX_PRECISION_FP64) {
         const std::size_t smem = set_smem_bytes<double>(vs.n, 0);
+        cudaError_t e = cudaFuncSetAttribute(accumulate_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             int(smem));
+        if (e != cudaSuccess) return e;
         accumulate_kernel<double><<<unsigned(blocks), threads, smem, st>>>(
             vs, static_cast<const Rec<double>*>(results), acc, first, finalize, format, out);
     } else {
         const std::size_t smem = set_smem_bytes<float>(vs.n, 0);
+        cudaError_t e = cudaFuncSetAttribute(accumulate_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             int(smem));
+        if (e != cudaSuccess) return e;
         accumulate_kernel<float><<<unsigned(blocks), threads, smem, st>>>(
             vs, static_cast<const Rec<float>*>(results), acc, first, finalize, format, out);
     }

@@ -116,3 +116,26 @@ def test_autotune_picks_a_valid_shape(renderer, sgx):
     for i in range(3):
         _assert_parity(b.capture(i), renderer.render_image(views[i], base), f"tuned view {i}")
     b.close()
+
+
+def test_batch_of_128_fp64_views(renderer, sgx):
+    """The largest batch in FP64: 128 views whose view set takes more than the
+    default 48 KB of shared memory in the trace and the accumulation."""
+    rng = np.random.default_rng(21)
+    views = []
+    for i in range(128):
+        side = 16 + 8 * (i % 3)
+        spin = float(rng.uniform(0, 0.998))
+        sc = sgx.Scene(spin_a_over_M=spin, disc_inner_M=sgx.kerr_isco_prograde(1.0, spin), disc_outer_M=30.0,
+                       disc_peak_T_K=1e4, render_supersample=1 + i % 2)
+        cam = sgx.build_orbital_camera(float(rng.uniform(20, 60)), float(np.radians(rng.uniform(5, 80))), 0.0, 30.0)
+        views.append(sgx.pack_uniforms(sc, cam, side, side))
+    opts = sgx.default_opts(integrator=1, precision=2)
+    b = sgx.Batch(renderer, views, opts)
+    b.launch()
+    st = b.wait()
+    assert st.rays == sum(v.width * v.height * v.supersample for v in views)
+    for i in range(0, 128, 16):
+        _assert_parity(b.capture(i), renderer.render_image(views[i], opts), f"fp64 view {i}")
+    b.close()
+
