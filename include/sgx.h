@@ -174,7 +174,7 @@ sgx_scene_status sgx_scene_config_load_file(const char* path, sgx_scene_config* 
                                             size_t errbuf_len);
 sgx_scene_status sgx_scene_config_load_string(const char* text, sgx_scene_config* out, int* line,
                                               char* errbuf, size_t errbuf_len);
-/* kerr_isco_prograde (core/include/physics/kerr.hpp:97-121). */
+/* kerr_isco_prograde (core/include/physics/kerr.hpp:85-104). */
 float sgx_kerr_isco_prograde(float mass, float spin);
 
 /* ---- context: CudaBackend lifecycle ----------------------------------- */

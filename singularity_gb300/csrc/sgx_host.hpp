@@ -87,7 +87,7 @@ void build_orbital_camera(CameraState& cam, float distance_M, float elevation_ra
 sgx_uniforms pack_uniforms(const Scene& scene, const CameraState& cam, std::uint32_t w, std::uint32_t h,
                            float time_sec);
 
-// Prograde ISCO (core/include/physics/kerr.hpp:97-121), float as the reference.
+// Prograde ISCO (core/include/physics/kerr.hpp:85-104), float as the reference.
 float kerr_isco_prograde(float mass, float spin);
 
 // C-ABI <-> C++ conversions.
