@@ -216,7 +216,7 @@ sgx_status sgx_trace_samples(sgx_context* ctx, const sgx_uniforms* u, const sgx_
 
 /* ---- HDR bloom and display transform ------------------------------------------ */
 /* The realtime backends' post-process (render/vulkan/shaders/bloom.hlsl:8-77,
- * blit.hlsl:120-134), which the reference's CUDA path lacks: on the last frame,
+ * blit.hlsl:43-57), which the reference's CUDA path lacks: on the last frame,
  * rendered in SGX_FORMAT_RGBA16F_HDR (the per-pixel mean HDR colour), a
  * half-resolution Karis-weighted extract with a soft-knee threshold, a
  * separable blur, and the compose hdr + bloom * strength, times exposure,

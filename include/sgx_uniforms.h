@@ -2,13 +2,13 @@
  * sgx_uniforms.h — the per-launch parameter block of the geodesic tracer.
  *
  * Byte-for-byte the same layout as the reference's `Uniforms`
- * (shared_shader/uniforms.h:122-163): 160 bytes, 16-byte aligned, every
+ * (shared_shader/uniforms.h:54-95): 160 bytes, 16-byte aligned, every
  * 3-vector stored as four floats (w unused).  A caller that already packs the
  * reference struct can hand its bytes to this library unchanged; the static
  * asserts below pin every offset.
  *
  * Flag bits and metric selectors keep the reference values
- * (shared_shader/uniforms.h:108-120).
+ * (shared_shader/uniforms.h:41-52).
  */
 #ifndef SGX_UNIFORMS_H
 #define SGX_UNIFORMS_H

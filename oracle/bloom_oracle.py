@@ -3,7 +3,7 @@
 A numpy restatement (float32 arithmetic, float16 storage between stages, as
 the reference's rgba16f targets) of the realtime backends' post-process:
 render/vulkan/shaders/bloom.hlsl:19-77 (Karis extract with soft knee, 7-tap
-separable blur with clamp-to-edge) and blit.hlsl:120-134 (hdr + bloom *
+separable blur with clamp-to-edge) and blit.hlsl:43-57 (hdr + bloom *
 strength, exposure, ACES).  The blur takes either the reference's weights or
 a normalised Gaussian of sigma_px / 2 half-resolution texels.  Only tests/
 use it, as the checker of singularity_gb300/csrc/sgx_post.cu.

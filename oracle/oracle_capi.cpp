@@ -5,7 +5,7 @@
 // into the product.
 //
 // Every entry takes the 160-byte uniform block of the reference
-// (shared_shader/uniforms.h:122-163) and runs the restatement in
+// (shared_shader/uniforms.h:54-95) and runs the restatement in
 // geodesic_oracle.hpp (FP32, FP64 or op-counting) across `threads` host
 // threads, pixels or rays handed out through an atomic counter the way the
 // reference CPU renderer hands out rows (cli/main.cpp:739-872).

@@ -46,7 +46,7 @@ class Vec4(C.Structure):
 
 
 class Uniforms(C.Structure):
-    """sgx_uniforms — the reference's 160-byte Uniforms (shared_shader/uniforms.h:122-163)."""
+    """sgx_uniforms — the reference's 160-byte Uniforms (shared_shader/uniforms.h:54-95)."""
 
     _fields_ = [
         ("cam_pos", Vec4), ("cam_fwd", Vec4), ("cam_right", Vec4), ("cam_up", Vec4),

@@ -2,7 +2,7 @@
 //
 // HDR bloom and display transform of a frame rendered in SGX_FORMAT_RGBA16F_HDR
 // — the realtime backends' post-process (render/vulkan/shaders/bloom.hlsl:8-77
-// and blit.hlsl:120-134, the same in Metal and WGSL), restated as CUDA kernels
+// and blit.hlsl:43-57, the same in Metal and WGSL), restated as CUDA kernels
 // because the reference's CUDA path has none (geodesic_kernel.cu:12-15):
 //   1. extract: each texel of a half-resolution target is the Karis-weighted
 //      average (weights 1 / (1 + luma)) of a 2x2 block of the HDR frame,
