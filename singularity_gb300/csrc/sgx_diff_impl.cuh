@@ -126,20 +126,50 @@ __device__ __forceinline__ void step_g(const S* y, const S& E, const S& L, const
     const S hh = S(T(0.5)) * he;
     S k1[7], k2[7], k3[7], k4[7], t[NS];
     t[5] = y[5];
-    rhs_g7(y, E, L, a, M, k1);
+    if constexpr (std::is_same_v<S, float>) {
+        // FP32: the same fused multiply-adds on pairs of state slots (0, 1),
+        // (2, 3), (6, 7) (derivative slots (0, 1), (2, 3), (5, 6)), slot 4 alone
+        auto axpy = [&](const float* k, float f) {
+            const F2 ff = f2(f, f);
+            unf2(fma2(f2(k[0], k[1]), ff, f2(y[0], y[1])), t[0], t[1]);
+            unf2(fma2(f2(k[2], k[3]), ff, f2(y[2], y[3])), t[2], t[3]);
+            unf2(fma2(f2(k[5], k[6]), ff, f2(y[6], y[7])), t[6], t[7]);
+            t[4] = fmaf(k[4], f, y[4]);
+        };
+        rhs_g7(y, E, L, a, M, k1);
+        axpy(k1, hh);
+        rhs_g7(t, E, L, a, M, k2);
+        axpy(k2, hh);
+        rhs_g7(t, E, L, a, M, k3);
+        axpy(k3, he);
+        rhs_g7(t, E, L, a, M, k4);
+        const float h6 = he / 6.0f;
+        const F2 two = f2(2.0f, 2.0f), hp = f2(h6, h6);
+        auto comb = [&](int i, int j, int si, int sj) {
+            const F2 sum = add2(fma2(f2(k2[i], k2[j]), two, f2(k1[i], k1[j])),
+                                fma2(f2(k3[i], k3[j]), two, f2(k4[i], k4[j])));
+            unf2(fma2(sum, hp, f2(y[si], y[sj])), o[si], o[sj]);
+        };
+        comb(0, 1, 0, 1);
+        comb(2, 3, 2, 3);
+        comb(5, 6, 6, 7);
+        o[4] = fmaf(fmaf(k2[4], 2.0f, k1[4]) + fmaf(k3[4], 2.0f, k4[4]), h6, y[4]);
+    } else {
+        rhs_g7(y, E, L, a, M, k1);
 #pragma unroll
-    for (int i = 0; i < 7; ++i) t[sgxa::sidx(i)] = y[sgxa::sidx(i)] + k1[i] * hh;
-    rhs_g7(t, E, L, a, M, k2);
+        for (int i = 0; i < 7; ++i) t[sgxa::sidx(i)] = y[sgxa::sidx(i)] + k1[i] * hh;
+        rhs_g7(t, E, L, a, M, k2);
 #pragma unroll
-    for (int i = 0; i < 7; ++i) t[sgxa::sidx(i)] = y[sgxa::sidx(i)] + k2[i] * hh;
-    rhs_g7(t, E, L, a, M, k3);
+        for (int i = 0; i < 7; ++i) t[sgxa::sidx(i)] = y[sgxa::sidx(i)] + k2[i] * hh;
+        rhs_g7(t, E, L, a, M, k3);
 #pragma unroll
-    for (int i = 0; i < 7; ++i) t[sgxa::sidx(i)] = y[sgxa::sidx(i)] + k3[i] * he;
-    rhs_g7(t, E, L, a, M, k4);
-    const S h6 = he / S(T(6));
+        for (int i = 0; i < 7; ++i) t[sgxa::sidx(i)] = y[sgxa::sidx(i)] + k3[i] * he;
+        rhs_g7(t, E, L, a, M, k4);
+        const S h6 = he / S(T(6));
 #pragma unroll
-    for (int i = 0; i < 7; ++i)
-        o[sgxa::sidx(i)] = y[sgxa::sidx(i)] + ((k1[i] + k2[i] * S(T(2))) + (k3[i] * S(T(2)) + k4[i])) * h6;
+        for (int i = 0; i < 7; ++i)
+            o[sgxa::sidx(i)] = y[sgxa::sidx(i)] + ((k1[i] + k2[i] * S(T(2))) + (k3[i] * S(T(2)) + k4[i])) * h6;
+    }
     const S n = S(T(1.5)) - S(T(0.5)) * (o[6] * o[6] + o[7] * o[7]);
     o[6] = o[6] * n;
     o[7] = o[7] * n;
