@@ -15,9 +15,11 @@
 #pragma once
 
 #include <cmath>
+#include <type_traits>
 
 #if defined(__CUDACC__)
 #define SGX_HD __host__ __device__ __forceinline__
+#include "sgx_device.cuh"  // packed FP32 pairs (device only)
 #else
 #define SGX_HD inline
 #endif
@@ -44,6 +46,43 @@ SGX_HD double hrcp(double x) { return 1.0 / x; }
 // dphi, dp_r, dp_theta, ds, dc.  theta is integrated for the swept angle and
 // the emission's path length; the right-hand side reads (s, c).
 SGX_HD constexpr int sidx(int i) { return i < 5 ? i : i + 1; }  // state index of derivative i
+
+// o = y + k f over the seven integrated state slots (derivative i -> state
+// sidx(i)); on the device in FP32 the same fused multiply-adds run on the
+// pairs of state slots (0, 1), (2, 3), (6, 7).
+template <class T> SGX_HD void stage7(const T* y, const T* k, T f, T* o) {
+#if defined(__CUDA_ARCH__)
+    if constexpr (std::is_same_v<T, float>) {
+        using namespace sgxd;
+        const F2 ff = f2(f, f);
+        unf2(fma2(f2(k[0], k[1]), ff, f2(y[0], y[1])), o[0], o[1]);
+        unf2(fma2(f2(k[2], k[3]), ff, f2(y[2], y[3])), o[2], o[3]);
+        unf2(fma2(f2(k[5], k[6]), ff, f2(y[6], y[7])), o[6], o[7]);
+        o[4] = fmaf(k[4], f, y[4]);
+        return;
+    }
+#endif
+    for (int i = 0; i < 7; ++i) o[sidx(i)] = y[sidx(i)] + k[i] * f;
+}
+
+// ks = (k1 + 2 k2) + (2 k3 + k4), the RK4 weights' sum (pairs on the device in FP32).
+template <class T> SGX_HD void ksum7(const T* k1, const T* k2, const T* k3, const T* k4, T* ks) {
+#if defined(__CUDA_ARCH__)
+    if constexpr (std::is_same_v<T, float>) {
+        using namespace sgxd;
+        const F2 two = f2(2.0f, 2.0f);
+        for (int i = 0; i < 6; i += 2) {
+            const int j = i < 4 ? i : 5;  // pairs (0, 1), (2, 3), (5, 6)
+            unf2(add2(fma2(f2(k2[j], k2[j + 1]), two, f2(k1[j], k1[j + 1])),
+                      fma2(f2(k3[j], k3[j + 1]), two, f2(k4[j], k4[j + 1]))),
+                 ks[j], ks[j + 1]);
+        }
+        ks[4] = fmaf(k2[4], 2.0f, k1[4]) + fmaf(k3[4], 2.0f, k4[4]);
+        return;
+    }
+#endif
+    for (int i = 0; i < 7; ++i) ks[i] = (k1[i] + k2[i] * T(2)) + (k3[i] * T(2) + k4[i]);
+}
 
 // The right-hand side in Carter's separated form (the same Hamiltonian as
 // kerr_hamilton.h:97-155): with P = (r^2 + a^2) E - a L, W = L - a E s2,
@@ -260,15 +299,15 @@ template <class T> SGX_HD void step_vjp(const T* y, T E, T L, T a, T M, T h, boo
     T k1[7], k2[7], k3[7], k4[7], y2[8], y3[8], y4[8];
     y2[5] = y3[5] = y4[5] = y[5];
     rhs7(y, E, L, a, M, k1);
-    for (int i = 0; i < 7; ++i) y2[sidx(i)] = y[sidx(i)] + k1[i] * hh;
+    stage7(y, k1, hh, y2);
     rhs7(y2, E, L, a, M, k2);
-    for (int i = 0; i < 7; ++i) y3[sidx(i)] = y[sidx(i)] + k2[i] * hh;
+    stage7(y, k2, hh, y3);
     rhs7(y3, E, L, a, M, k3);
-    for (int i = 0; i < 7; ++i) y4[sidx(i)] = y[sidx(i)] + k3[i] * he;
+    stage7(y, k3, he, y4);
     rhs7(y4, E, L, a, M, k4);
     const T h6 = he / T(6);
     T ks[7];
-    for (int i = 0; i < 7; ++i) ks[i] = (k1[i] + k2[i] * T(2)) + (k3[i] * T(2) + k4[i]);
+    ksum7(k1, k2, k3, k4, ks);
     // RK4 output before and after the renormalisation of (s, c)
     const T s_hat = y[6] + ks[5] * h6, c_hat = y[7] + ks[6] * h6;
     const T n = T(1.5) - T(0.5) * (s_hat * s_hat + c_hat * c_hat);
