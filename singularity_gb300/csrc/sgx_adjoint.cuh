@@ -65,6 +65,82 @@ template <class T> SGX_HD void stage7(const T* y, const T* k, T f, T* o) {
     for (int i = 0; i < 7; ++i) o[sidx(i)] = y[sidx(i)] + k[i] * f;
 }
 
+// The reverse pass's accumulations over the seven integrated slots, on the
+// device in FP32 as packed pairs (derivative slots (0, 1), (2, 3), (5, 6),
+// state slots (0, 1), (2, 3), (6, 7)); a dot product is then summed as two
+// pair lanes, so its last bits can differ from the sequential sum.
+// ly[sidx(i)] += g[sidx(i)], lk[i] += f g[sidx(i)], acc += g[sidx(i)] k[i]:
+template <class T> SGX_HD void vjp_accum7(const T* g, T f, const T* k, T* ly, T* lk, T& acc) {
+#if defined(__CUDA_ARCH__)
+    if constexpr (std::is_same_v<T, float>) {
+        using namespace sgxd;
+        const F2 ff = f2(f, f);
+        F2 dot = f2(0.0f, 0.0f);
+        for (int p = 0; p < 3; ++p) {
+            const int j = p < 2 ? 2 * p : 5, q = p < 2 ? 2 * p : 6;
+            const F2 gp = f2(g[q], g[q + 1]);
+            unf2(add2(f2(ly[q], ly[q + 1]), gp), ly[q], ly[q + 1]);
+            unf2(fma2(gp, ff, f2(lk[j], lk[j + 1])), lk[j], lk[j + 1]);
+            dot = fma2(gp, f2(k[j], k[j + 1]), dot);
+        }
+        float d0, d1;
+        unf2(dot, d0, d1);
+        ly[4] += g[4];
+        lk[4] = fmaf(f, g[4], lk[4]);
+        acc = fmaf(g[4], k[4], acc + (d0 + d1));
+        return;
+    }
+#endif
+    for (int i = 0; i < 7; ++i) {
+        const T gi = g[sidx(i)];
+        ly[sidx(i)] += gi;
+        lk[i] += f * gi;
+        acc += gi * k[i];
+    }
+}
+
+// From the output adjoint lo: ly[sidx(i)] += l, lk1 = lk4 = l h6,
+// lk2 = lk3 = l 2 h6, acc += l ks[i] (l = lo[sidx(i)]).
+template <class T>
+SGX_HD void vjp_out7(const T* lo, T h6, const T* ks, T* ly, T* lk1, T* lk2, T* lk3, T* lk4, T& acc) {
+#if defined(__CUDA_ARCH__)
+    if constexpr (std::is_same_v<T, float>) {
+        using namespace sgxd;
+        const F2 hp = f2(h6, h6), h2p = f2(2.0f * h6, 2.0f * h6);
+        F2 dot = f2(0.0f, 0.0f);
+        for (int p = 0; p < 3; ++p) {
+            const int j = p < 2 ? 2 * p : 5, q = p < 2 ? 2 * p : 6;
+            const F2 lp = f2(lo[q], lo[q + 1]);
+            unf2(add2(f2(ly[q], ly[q + 1]), lp), ly[q], ly[q + 1]);
+            unf2(mul2(lp, hp), lk1[j], lk1[j + 1]);
+            unf2(mul2(lp, h2p), lk2[j], lk2[j + 1]);
+            lk3[j] = lk2[j];
+            lk3[j + 1] = lk2[j + 1];
+            lk4[j] = lk1[j];
+            lk4[j + 1] = lk1[j + 1];
+            dot = fma2(lp, f2(ks[j], ks[j + 1]), dot);
+        }
+        float d0, d1;
+        unf2(dot, d0, d1);
+        const float l = lo[4];
+        ly[4] += l;
+        lk1[4] = lk4[4] = l * h6;
+        lk2[4] = lk3[4] = l * (2.0f * h6);
+        acc = fmaf(l, ks[4], acc + (d0 + d1));
+        return;
+    }
+#endif
+    for (int i = 0; i < 7; ++i) {
+        const T l = lo[sidx(i)];
+        ly[sidx(i)] += l;
+        lk1[i] = l * h6;
+        lk2[i] = l * (T(2) * h6);
+        lk3[i] = l * (T(2) * h6);
+        lk4[i] = l * h6;
+        acc += l * ks[i];
+    }
+}
+
 // ks = (k1 + 2 k2) + (2 k3 + k4), the RK4 weights' sum (pairs on the device in FP32).
 template <class T> SGX_HD void ksum7(const T* k1, const T* k2, const T* k3, const T* k4, T* ks) {
 #if defined(__CUDA_ARCH__)
@@ -342,44 +418,21 @@ template <class T> SGX_HD void step_vjp(const T* y, T E, T L, T a, T M, T h, boo
     // o = y + ks h6
     T lk1[7], lk2[7], lk3[7], lk4[7];
     T l_he = T(0);
-    for (int i = 0; i < 7; ++i) {
-        const T l = lo[sidx(i)];
-        ly[sidx(i)] += l;
-        lk1[i] = l * h6;
-        lk2[i] = l * (T(2) * h6);
-        lk3[i] = l * (T(2) * h6);
-        lk4[i] = l * h6;
-        l_he += l * ks[i];
-    }
+    vjp_out7(lo, h6, ks, ly, lk1, lk2, lk3, lk4, l_he);
     l_he *= T(1) / T(6);
     ly[1] += l_y1_psi;
     ly[2] += l_y2_psi;
     T g[8];
     // k4 = f(y4), y4 = y + he k3
     rhs_vjp7(y4, E, L, a, M, lk4, g, gc);
-    for (int i = 0; i < 7; ++i) {
-        const T gi = g[sidx(i)];
-        ly[sidx(i)] += gi;
-        lk3[i] += he * gi;
-        l_he += gi * k3[i];
-    }
+    vjp_accum7(g, he, k3, ly, lk3, l_he);
     T l_hh = T(0);
     // k3 = f(y3), y3 = y + hh k2
     rhs_vjp7(y3, E, L, a, M, lk3, g, gc);
-    for (int i = 0; i < 7; ++i) {
-        const T gi = g[sidx(i)];
-        ly[sidx(i)] += gi;
-        lk2[i] += hh * gi;
-        l_hh += gi * k2[i];
-    }
+    vjp_accum7(g, hh, k2, ly, lk2, l_hh);
     // k2 = f(y2), y2 = y + hh k1
     rhs_vjp7(y2, E, L, a, M, lk2, g, gc);
-    for (int i = 0; i < 7; ++i) {
-        const T gi = g[sidx(i)];
-        ly[sidx(i)] += gi;
-        lk1[i] += hh * gi;
-        l_hh += gi * k1[i];
-    }
+    vjp_accum7(g, hh, k1, ly, lk1, l_hh);
     // k1 = f(y)
     rhs_vjp7(y, E, L, a, M, lk1, g, gc);
     for (int i = 0; i < 7; ++i) ly[sidx(i)] += g[sidx(i)];
