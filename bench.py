@@ -5,20 +5,19 @@ its 4K x 256 spp Kerr claim): Kerr a/M = 0.94, 3840x2160, 256 samples per
 pixel with Halton(2,3) jitter, observer at r = 40 M, inclination 75 deg
 (elevation 0.261799 rad), vertical FOV 30 deg, disc from the prograde ISCO to
 30 M, peak temperature 1e4 K, disc-band phase of turbulence seed 7 (time
-7/30 s), reference defaults otherwise.  Integrated in
-the precision form: the error-controlled Kerr RK4 at tolerance 1e-6 in FP32,
-with the constants of motion and the step control within 0.05 M of the
-photon orbit or the horizon in FP64 (`--precision fp32 | fp64` for the other
-forms).  One bench step is one progressive pass of 16 samples per pixel over
-the full frame (132,710,400 rays); 16 steps make the 256-spp frame.
-
-Studies in the same line (N = 1): precision forms (FP32 / mixed / FP64 speed,
-errors against the FP64 CPU oracle, Carter and null-condition drift), 64
-batched views in a CUDA graph, 1080p HDR + bloom, and the adjoint at
-512x512x4 (grad/s, central differences, FP64 gradient, 200 Adam steps).
+7/30 s), reference defaults otherwise.  Integrated in the precision form: the
+error-controlled Kerr RK4 at tolerance 1e-6 in FP32, with the constants of
+motion and the step control within 0.05 M of the photon orbit or the horizon
+in FP64, p_theta projected back onto each ray's Carter constant after every
+accepted step (`--precision fp32 | fp64` for the other forms, `--integrator
+fixed` for the reference's fixed step).  One bench step is one progressive
+pass of 16 samples per pixel over the full frame (132,710,400 rays); 16 steps
+make the 256-spp frame.  Under N ranks the frame is split into N slices of
+interleaved 8-row bands (strong scaling: the frame stays the same, each GPU
+traces 1/N of it) and the e2e leg gathers the slices to rank 0.
 
   value   Mrays/s, device time (CUDA events on the launching stream) over the
-          K timed steps, inputs resident; max over ranks.
+          K timed steps, inputs resident; rays of all ranks / the slowest rank.
   e2e     the same metric through the public C ABI with host buffers: per
           step a full 16-spp frame (uniforms host->device, RGBA8 frame
           device->host into pinned memory), wall clock.
@@ -26,13 +25,22 @@ batched views in a CUDA graph, 1080p HDR + bloom, and the adjoint at
           algorithmic FLOPs (the reference formulas' operation count per
           integrator step, counted by the CPU oracle, times the steps the GPU
           took) / the kernel's event-timed duration.
-  cpu_baseline  the CPU oracle (a restatement of the reference kernel,
-          bit-exact with it on the host) on all host cores, on a bounded
-          sample of the same workload.
+  cpu_baseline  the reference's own kernel source compiled for the host CPU
+          (oracle/_ref) on all host cores, on a bounded random sample of the
+          workload's rays, with the reference's fixed step.
+  same_algorithm  the reference's own CUDA kernel (PTX compiled from its
+          source) against our fixed-step kernel, both the reference's
+          algorithm, on this GPU, one 16-spp 4K pass each, device-timed.
+  precision_study  FP32 / mixed / FP64 speed, per-channel error and Carter /
+          null-condition drift of the rays the GPU traced, against the FP64
+          CPU oracle (last in the line).
 
-`--impl reference` times the reference algorithm on the host cores (the CPU
-oracle; the reference's own sources are not present on the GPU host) on the
-same workload and prints the same line with "impl": "reference".
+`--impl reference` times the reference's own CPU implementation of the path
+(its kernel source compiled for the host, oracle/_ref, from the reference
+checkout or the snapshot `make -C oracle snapshot` keeps) on all host cores,
+with the reference's own uniform packing (fixed step h = 0.4, 2500 steps), on
+a bounded random sample of the workload per step, and prints the same line
+with "impl": "reference".  It loads nothing of this package.
 """
 
 from __future__ import annotations
@@ -40,6 +48,7 @@ from __future__ import annotations
 import argparse
 import ctypes as C
 import json
+import math
 import os
 import subprocess
 import sys
@@ -53,18 +62,42 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 WIDTH, HEIGHT, SPP, SPP_PER_STEP = 3840, 2160, 256, 16
-# Headline integrator: the error-controlled RK4 at tolerance 1e-6.
 METRIC = "Kerr geodesic Mrays/s at 4K x 256spp"
 # `--workload small`: the same scene at 1280x720 (profiling captures only).
 SMALL = (1280, 720)
+ELEVATION = 0.261799  # inclination 75 deg
+TURB_TIME = 7.0 / 30.0  # the band phase of turbulence seed 7
+SLICE_BAND = 8  # rows per band of a frame split over ranks
+
+
+def scene_name() -> str:
+    return f"kerr_a0.94_r40_i75_fov30_isco-30M_T1e4_{WIDTH}x{HEIGHT}_256spp"
 
 
 def workload_uniforms(S, spp=SPP):
     isco = S.kerr_isco_prograde(1.0, 0.94)
     scene = S.Scene(spin_a_over_M=0.94, disc_inner_M=isco, disc_outer_M=30.0, disc_peak_T_K=1e4,
                     render_supersample=spp)
-    cam = S.build_orbital_camera(40.0, 0.261799, 0.0, 30.0)
-    return S.pack_uniforms(scene, cam, WIDTH, HEIGHT, S.workloads.turbulence_time())
+    cam = S.build_orbital_camera(40.0, ELEVATION, 0.0, 30.0)
+    return S.pack_uniforms(scene, cam, WIDTH, HEIGHT, TURB_TIME)
+
+
+def sig(x, n: int = 4):
+    """x with floats rounded to n significant digits (dicts and lists recursively)."""
+    if isinstance(x, float):
+        return float(f"{x:.{n}g}") if math.isfinite(x) else None
+    if isinstance(x, dict):
+        return {k: sig(v, n) for k, v in x.items()}
+    if isinstance(x, (list, tuple)):
+        return [sig(v, n) for v in x]
+    return x
+
+
+def stats4(a) -> dict:
+    a = np.asarray(a, dtype=np.float64)
+    a = a[np.isfinite(a)]
+    return {"median": float(np.median(a)), "mean": float(a.mean()), "p99": float(np.percentile(a, 99)),
+            "max": float(a.max())}
 
 
 class ClockSampler:
@@ -112,30 +145,37 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def cpu_baseline(S, O, u, seconds: float = 12.0, seed: int = 0) -> dict:
-    """The CPU oracle on a random pixel subset with the step's 16 samples."""
+def _sample_rays(rng, npix: int, width: int, n_pix: int, pass_index: int):
+    """n_pix random pixels, each with the 16 Halton samples of progressive pass `pass_index`."""
+    pix = rng.choice(npix, n_pix, replace=False).astype(np.uint32)
+    gx = np.repeat(pix % width, SPP_PER_STEP).astype(np.uint32)
+    gy = np.repeat(pix // width, SPP_PER_STEP).astype(np.uint32)
+    s = np.tile(np.arange(SPP_PER_STEP, dtype=np.uint32) + np.uint32(pass_index * SPP_PER_STEP), n_pix)
+    return gx, gy, s
+
+
+def reference_cpu_rate(O, u_ref, seconds: float = 12.0, seed: int = 0) -> dict:
+    """The reference's kernel source compiled for the host (oracle/_ref) on all
+    host cores: random pixels x 16 samples of the workload, sized to ~`seconds`."""
     threads = os.cpu_count() or 1
     rng = np.random.default_rng(seed)
-    npix = u.width * u.height
+    npix = u_ref.width * u_ref.height
 
     def run(n):
-        pix = rng.choice(npix, n, replace=False).astype(np.uint32)
-        gx = np.repeat(pix % u.width, SPP_PER_STEP)
-        gy = np.repeat(pix // u.width, SPP_PER_STEP)
-        s = np.tile(np.arange(SPP_PER_STEP, dtype=np.uint32), n)
+        gx, gy, s = _sample_rays(rng, npix, u_ref.width, n, 0)
         t0 = time.perf_counter()
-        O.trace(u, gx, gy, s, threads=threads)
+        O.ref_trace(u_ref, gx, gy, s, threads=threads)
         return gx.size, time.perf_counter() - t0
 
-    rays, dt = run(256)
+    _, dt = run(256)
     n = int(max(256, min(2_000_000, 256 * seconds / max(dt, 1e-3))))
     rays, dt = run(n)
-    return {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
-            "sample": f"{n} random pixels x {SPP_PER_STEP} Halton samples of the workload ({rays} rays, "
-                      f"{dt:.1f} s), FP32 oracle"}
+    return {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "reference",
+            "sample": f"{n} random pixels x {SPP_PER_STEP} Halton samples ({rays} rays, {dt:.1f} s) through the "
+                      "reference's geodesic_kernel.cu compiled for the host, fixed step h=0.4"}
 
 
-def ops_per_step(S, O, u, n: int = 1024, seed: int = 1, adaptive=None) -> tuple[float, float]:
+def ops_per_step(O, u, n: int = 1024, seed: int = 1, adaptive=None) -> tuple[float, float]:
     """Reference-formula FP32 ops per integrator step (ratio estimator over a
     random sample of the workload's rays) and mean steps per ray."""
     rng = np.random.default_rng(seed)
@@ -147,38 +187,51 @@ def ops_per_step(S, O, u, n: int = 1024, seed: int = 1, adaptive=None) -> tuple[
 
 
 def run_reference(args, rank: int) -> None:
+    """The reference arm: its own code, nothing of singularity_gb300."""
     if rank != 0:
         return
-    import singularity_gb300 as S
     from oracle import pyoracle as O
-    O.build(ref=False)
-    u = workload_uniforms(S)
+    try:
+        O.build(ref=True)
+    except Exception as e:  # noqa: BLE001
+        print(json.dumps({"impl": "reference", "unavailable": f"building the reference for this host failed: {e}"}))
+        return
+    if not O.ref_available():
+        print(json.dumps({"impl": "reference", "unavailable": "no reference sources (checkout or the "
+                                                              "oracle/_ref/src snapshot) on this machine"}))
+        return
+    u = O.ref_headline_uniforms(WIDTH, HEIGHT, SPP, TURB_TIME)
     threads = os.cpu_count() or 1
     rng = np.random.default_rng(0)
     npix = u.width * u.height
-    n_pix = 2048  # bounded sample per step: 2048 pixels x 16 samples
+    n_pix = 8192  # bounded sample per step: 8192 random pixels x the step's 16 samples
+    passes = SPP // SPP_PER_STEP
+    k = [0]
 
     def step():
-        pix = rng.choice(npix, n_pix, replace=False).astype(np.uint32)
-        gx = np.repeat(pix % u.width, SPP_PER_STEP)
-        gy = np.repeat(pix // u.width, SPP_PER_STEP)
-        s = np.tile(np.arange(SPP_PER_STEP, dtype=np.uint32), n_pix)
-        O.trace(u, gx, gy, s, threads=threads)
+        gx, gy, s = _sample_rays(rng, npix, u.width, n_pix, k[0] % passes)
+        k[0] += 1
+        O.ref_trace(u, gx, gy, s, threads=threads)
         return gx.size
 
     for _ in range(args.warmup):
         step()
+    k[0] = 0
     t0 = time.perf_counter()
     rays = sum(step() for _ in range(args.steps))
     dt = time.perf_counter() - t0
     v = rays / dt / 1e6
+    sample = f"{n_pix} random pixels x the step's {SPP_PER_STEP} Halton samples per step"
     line = {"metric": METRIC, "value": v, "unit": "Mrays/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-            "config": {"workload": "kerr_a0.94_r40_i75_fov30_3840x2160_256spp_fixed_h0.4",
-                       "sample_per_step": f"{n_pix} random pixels x {SPP_PER_STEP} samples"},
-            "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": threads, "kind": "port",
-                             "sample": f"{n_pix} random pixels x {SPP_PER_STEP} Halton samples per step"},
+            "scaling": "strong", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": {"workload": scene_name() + "_fixed_h0.4_max2500_f32",
+                       "integrator": "the reference's fixed-step RK4, h = 0.4, at most 2500 steps "
+                                     "(render/cuda/cuda_backend.cu:35-36)",
+                       "code": "render/cuda/kernels/geodesic_kernel.cu compiled for the host (oracle/_ref), "
+                               "uniforms by the reference's camera and Scene defaults",
+                       "sample_per_step": sample},
+            "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": threads, "kind": "reference", "sample": sample},
             "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -197,61 +250,96 @@ def timed_pass(lib, N, r, u, opts, d_out, stream, torch) -> tuple[float, object]
     return e0.elapsed_time(e1), r.stats()
 
 
-def precision_study(S, N, O, lib, r, u, d_out, stream, torch, main_opts) -> dict:
-    """Precision forms: FP32 vs FP64 GPU forms at equal tolerance, and
-    errors against the FP64 CPU oracle on 4096 pixels drawn with
-    numpy.random.default_rng(0).choice(W*H, 4096, replace=False)."""
+def same_algorithm_study(S, N, lib, r, u, d_out, stream, torch) -> dict:
+    """The reference's algorithm (fixed-step RK4, h = 0.4) on this GPU, one
+    16-spp pass of the 4K frame each: the reference's own CUDA kernel
+    (geodesic_kernel.cu:462, PTX compiled from its source, launched as
+    CudaBackend::render_frame does) against our fixed-step kernel."""
+    npix = u.width * u.height
+    rays = npix * SPP_PER_STEP
+    out = {}
+    for key, form in (("ours_fixed_mrays_s", 0), ("ours_fixed_form2_mrays_s", 2)):
+        o = S.default_opts(sample_count=SPP_PER_STEP, rhs_form=form)
+        timed_pass(lib, N, r, u, o, d_out, stream, torch)
+        ms, st = timed_pass(lib, N, r, u, o, d_out, stream, torch)
+        out[key] = rays / (ms / 1e3) / 1e6
+        if form == 0:
+            out["fixed_steps_per_ray"] = st.steps / max(1, st.rays)
+    from oracle import ref_gpu
+    if not ref_gpu.available():
+        out["reference_cuda_kernel"] = "unavailable: reference PTX not built"
+        return out
+    k = ref_gpu.RefKernel()
+    try:
+        u16 = u.copy()
+        u16.supersample = SPP_PER_STEP  # Halton samples 1..16, the first pass
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        k.launch(d_out.data_ptr(), u16, stream.cuda_stream)
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(2):
+            e0.record(stream)
+            k.launch(d_out.data_ptr(), u16, stream.cuda_stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        out["reference_cuda_kernel_mrays_s"] = rays / (min(ms) / 1e3) / 1e6
+    finally:
+        k.close()
+    out["ours_fixed_over_reference"] = out["ours_fixed_mrays_s"] / out["reference_cuda_kernel_mrays_s"]
+    return out
+
+
+def _aces(x):
+    # Narkowicz's ACES fit, as the reference applies it per sample (geodesic_kernel.cu:413-419)
+    a, b, c, d, e = 2.51, 0.03, 2.43, 0.59, 0.14
+    return np.clip((x * (a * x + b)) / (x * (c * x + d) + e), 0.0, 1.0)
+
+
+def precision_study(S, N, O, lib, r, u, d_out, stream, torch) -> dict:
+    """FP32 / mixed / FP64 forms of the error-controlled integrator: speed of
+    one 16-spp 4K pass each; on the seeded 4096 pixels
+    (numpy.random.default_rng(0).choice(W*H, 4096, replace=False)) at all 256
+    samples (1,048,576 rays), the per-channel error of each GPU form against
+    the FP64 CPU oracle, and the Carter-constant and null-condition drift of
+    the rays the GPU traced, beside the FP64 oracle's."""
     out = {}
     npix = u.width * u.height
     rays = npix * SPP_PER_STEP
-    # speed of each form on one 16-spp pass
-    for name, prec in (("fp32", N.PRECISION_FP32), ("mixed", N.PRECISION_MIXED), ("fp64", N.PRECISION_FP64)):
+    forms = (("fp32", N.PRECISION_FP32), ("mixed", N.PRECISION_MIXED), ("fp64", N.PRECISION_FP64))
+    for name, prec in forms:
         o = S.default_opts(integrator=N.INTEGRATOR_ADAPTIVE, precision=prec, sample_count=SPP_PER_STEP)
         timed_pass(lib, N, r, u, o, d_out, stream, torch)  # warm
         ms, st = timed_pass(lib, N, r, u, o, d_out, stream, torch)
         out[f"{name}_mrays_s"] = rays / (ms / 1e3) / 1e6
         out[f"{name}_steps_per_ray"] = st.steps / max(1, st.rays)
-        if name == "mixed":
-            out["mixed_zone_step_frac"] = st.zone_steps / max(1, st.steps)
     out["fp32_over_fp64"] = out["fp32_mrays_s"] / out["fp64_mrays_s"]
     out["mixed_over_fp64"] = out["mixed_mrays_s"] / out["fp64_mrays_s"]
-    # reference algorithm (fixed-step RK4, h = 0.4) through the same kernels
-    o = S.default_opts(sample_count=SPP_PER_STEP)
-    timed_pass(lib, N, r, u, o, d_out, stream, torch)
-    ms, st = timed_pass(lib, N, r, u, o, d_out, stream, torch)
-    out["reference_fixed_step_mrays_s"] = rays / (ms / 1e3) / 1e6
-    out["reference_fixed_step_steps_per_ray"] = st.steps / max(1, st.rays)
-    # accuracy at 4096 seeded pixels, full 256 spp
     rng = np.random.default_rng(0)
     pix = rng.choice(npix, 4096, replace=False).astype(np.uint32)
-    imgs = {}
-    for name, prec in (("fp32", N.PRECISION_FP32), ("mixed", N.PRECISION_MIXED)):
-        o = S.default_opts(integrator=N.INTEGRATOR_ADAPTIVE, precision=prec, format=N.FORMAT_RGBA32F)
-        r.render(u, o)
-        imgs[name] = r.capture(N.FORMAT_RGBA32F).reshape(-1, 4)[pix, :3].astype(np.float64)
+    gx = np.repeat(pix % u.width, SPP).astype(np.uint32)
+    gy = np.repeat(pix // u.width, SPP).astype(np.uint32)
+    s = np.tile(np.arange(SPP, dtype=np.uint32), pix.size)
     ad64 = O.adaptive_opts()
     _, ldr64 = O.render(u, "f64", pixels=pix, adaptive=ad64)
-    for name, img in imgs.items():
-        d = np.abs(img - ldr64)
-        out[f"{name}_vs_fp64_oracle_mean_channel_err"] = float(d.mean())
-        out[f"{name}_vs_fp64_oracle_max_channel_err"] = float(d.max())
-    # Carter constant drift of the same integrator (CPU oracle, 1 sample per pixel)
-    gx, gy = (pix % u.width).astype(np.uint32), (pix // u.width).astype(np.uint32)
-    s = np.zeros_like(gx)
-    for prec, key in (("f32", "fp32"), ("f64", "fp64")):
-        _, _, term, d = O.trace(u, gx, gy, s, precision=prec, adaptive=ad64, diag=True)
-        ok = term != 5
-        dq = np.array([abs(x.Q_end - x.Q0) / x.norm_Q for x in d])[ok]
-        out[f"carter_drift_{key}"] = {"median": float(np.median(dq)), "mean": float(dq.mean()),
-                                      "p99": float(np.percentile(dq, 99)), "max": float(dq.max())}
-        dh = np.array([abs(x.H2_end) / max(1e-30, x.E * x.E) for x in d])[ok]
-        out[f"null_condition_drift_{key}"] = {"median": float(np.median(dh)), "mean": float(dh.mean()),
-                                              "p99": float(np.percentile(dh, 99)), "max": float(dh.max())}
-    out["note"] = ("speeds: one 16-spp 4K pass each; errors: full 256-spp frame, RGBA32F LDR mean, units of "
-                   "full scale; Carter drift |Q_end-Q0|/(|Q0|+L^2+a^2E^2) and null-condition drift |2H_end|/E^2 "
-                   "from the CPU oracle of the same integrator; E and L_z are constants of the Hamiltonian form "
-                   "(held exactly, zero drift by construction); rhs_form 2 (sin/cos of theta in the state) "
-                   "coincides with form 0 here: the error-controlled form always carries them")
+    for name, prec in forms:
+        o = S.default_opts(integrator=N.INTEGRATOR_ADAPTIVE, precision=prec)
+        hdr, _, _ = r.trace_samples(u, gx, gy, s, o)
+        ldr = _aces(hdr.astype(np.float64).reshape(pix.size, SPP, 3) * float(u.exposure)).mean(axis=1)
+        d = np.abs(ldr - ldr64)
+        out[f"{name}_err_vs_fp64_oracle"] = {"mean": float(d.mean()), "max": float(d.max())}
+        inv, _ = r.trace_invariants(u, gx, gy, s, o)
+        out[f"{name}_carter_drift_gpu"] = stats4(S.carter_drift(inv, u.spin_a))
+        if name == "mixed":
+            h2 = np.abs(inv[:, 4]) / inv[:, 0] ** 2
+            out["mixed_null_drift_gpu"] = {"median": float(np.nanmedian(h2)), "p99": float(np.nanpercentile(h2, 99))}
+            o.projection = 0
+            inv0, _ = r.trace_invariants(u, gx, gy, s, o)
+            out["mixed_carter_drift_gpu_no_projection"] = stats4(S.carter_drift(inv0, u.spin_a))
+    _, _, term, dg = O.trace(u, gx, gy, s, precision="f64", adaptive=ad64, diag=True)
+    dq = np.array([abs(x.Q_end - x.Q0) / x.norm_Q for x in dg])[term != 5]
+    out["fp64_oracle_carter_drift"] = stats4(dq)
     return out
 
 
@@ -271,14 +359,9 @@ def batch_study(S, N, r, torch, launches: int = 3, rank: int = 0, world: int = 1
     views = [views_all[i] for i in parts[rank]]
     rays = sum(v.width * v.height * v.supersample for v in views)
     base = S.default_opts(integrator=N.INTEGRATOR_ADAPTIVE)
-    t0 = time.perf_counter()
     best, tune_ms = S.autotune(r, views, base, sample_cap=4)
-    tune_s = time.perf_counter() - t0
-    out = {"views": len(views_all), "views_this_rank": len(views),
-           "pixels": sum(v.width * v.height for v in views_all),
-           "rays": sum(v.width * v.height * v.supersample for v in views_all),
-           "autotune": {"block_threads": best.block_threads, "refill_interval": best.refill_interval,
-                        "tile": [best.tile_w, best.tile_h], "probe_ms": tune_ms, "wall_s": tune_s}}
+    out = {"rays": sum(v.width * v.height * v.supersample for v in views_all),
+           "autotune": [best.block_threads, best.refill_interval, best.tile_w, best.tile_h]}
     for name, opts in (("autotuned", best), ("default", base)):
         b = S.Batch(r, views, opts)
         b.launch()
@@ -291,20 +374,19 @@ def batch_study(S, N, r, torch, launches: int = 3, rank: int = 0, world: int = 1
             ms.append(st.total_ms)
             steps = st.steps
         b.close()
-        out[f"{name}_ms_per_batch"] = D.max_over_ranks(float(np.median(ms)), "cuda")
         out[f"{name}_mrays_s"] = D.whole_job_rate(rays, float(np.median(ms)) / 1e3, "cuda") / 1e6
-        out[f"{name}_gsteps_s"] = D.whole_job_rate(steps, float(np.median(ms)) / 1e3, "cuda") / 1e9
-        out["steps_per_ray"] = steps / max(1, rays)
-    out["note"] = ("one graph replay renders all 64 views (every sample); adaptive FP32, tol 1e-6; device time; "
-                   "gsteps_s = integrator attempts per second, comparable across workloads")
+        if name == "autotuned":
+            out["ms_per_batch"] = D.max_over_ranks(float(np.median(ms)), "cuda")
+            out["gsteps_s"] = D.whole_job_rate(steps, float(np.median(ms)) / 1e3, "cuda") / 1e9
+            out["steps_per_ray"] = steps / max(1, rays)
     if sample_cap > 0:
-        out["note"] += f"; samples capped at {sample_cap} per view (small case)"
+        out["samples_capped_at"] = sample_cap
     return out
 
 
 def hdr_bloom_study(S, N, r, torch, reps: int = 3) -> dict:
     """HDR + bloom: Kerr a=0.94 1920x1080, 16 spp, adaptive tol 1e-6, half-float HDR,
-    bloom sigma 8 px, ACES -> RGBA8; device time of render + post-process."""
+    bloom sigma 8 px, ACES -> RGBA8; device time of the render + wall time of the post-process."""
     u = S.workloads.kerr_1080p_16spp()
     opts = S.default_opts(integrator=N.INTEGRATOR_ADAPTIVE, format=N.FORMAT_RGBA16F_HDR)
     bo = N.BloomOpts(C.sizeof(N.BloomOpts), 8.0, -1.0, -1.0, N.FORMAT_RGBA8_SRGB)
@@ -314,7 +396,6 @@ def hdr_bloom_study(S, N, r, torch, reps: int = 3) -> dict:
     t_render, t_post = [], []
     for _ in range(reps):
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
         r.render(u, opts)
         t1 = time.perf_counter()
         st = lib.sgx_bloom(r.handle, C.byref(bo))
@@ -325,9 +406,8 @@ def hdr_bloom_study(S, N, r, torch, reps: int = 3) -> dict:
         t_post.append((t2 - t1) * 1e3)
     rays = u.width * u.height * u.supersample
     ms = float(np.median(t_render)) + float(np.median(t_post))
-    return {"rays": rays, "render_ms": float(np.median(t_render)), "bloom_ms_wall": float(np.median(t_post)),
-            "mrays_s_incl_post": rays / (ms / 1e3) / 1e6,
-            "note": "render device time (trace + HDR accumulation) + bloom sigma 8 px/ACES wall time (synchronous)"}
+    return {"render_ms": float(np.median(t_render)), "bloom_ms": float(np.median(t_post)),
+            "mrays_s_incl_post": rays / (ms / 1e3) / 1e6}
 
 
 def diff_study(S, N, r, torch, adam_steps: int = 200, fd_eps: float = 1e-3) -> dict:
@@ -337,7 +417,7 @@ def diff_study(S, N, r, torch, adam_steps: int = 200, fd_eps: float = 1e-3) -> d
     T-scale 0.8; loss = mean squared image error to the FP64 target image.
     grad/s = forward + adjoint per second (synchronous calls, wall clock);
     the adjoints against central differences (eps 1e-3) of the FP64 forward at
-    full size; FP32 against FP64 adjoint; Adam from the guess."""
+    full size; FP32 against FP64 adjoint; 200 Adam steps from the guess."""
     from singularity_gb300 import diff as D
     W = S.workloads
     base = W.differentiation_base(512, 512, 4)
@@ -346,8 +426,7 @@ def diff_study(S, N, r, torch, adam_steps: int = 200, fd_eps: float = 1e-3) -> d
     dr = D.DiffRenderer(r)
     o32, o64 = D.DiffOptions(precision=N.PRECISION_FP32), D.DiffOptions(precision=N.PRECISION_FP64)
     target = dr.forward(base, tgt, o64).clone()
-    out = {"rays_per_render": base.width * base.height * base.supersample,
-           "checkpoint_interval": 64, "model": "slab"}
+    out = {"model": "slab"}
 
     def loss_grad(img):
         return 2.0 * (img - target) / img.numel()
@@ -367,11 +446,10 @@ def diff_study(S, N, r, torch, adam_steps: int = 200, fd_eps: float = 1e-3) -> d
             tf.append(t1 - t0)
             tb.append(t2 - t1)
         grads[name] = g
-        out[f"{name}_forward_ms"] = 1e3 * float(np.median(tf))
-        out[f"{name}_backward_ms"] = 1e3 * float(np.median(tb))
+        if name == "fp32":
+            out["fp32_forward_ms"] = 1e3 * float(np.median(tf))
+            out["fp32_backward_ms"] = 1e3 * float(np.median(tb))
         out[f"{name}_grad_per_s"] = 1.0 / (float(np.median(tf)) + float(np.median(tb)))
-        out[f"{name}_steps_per_ray"] = dr.stats()["steps"] / out["rays_per_render"]
-        out[f"{name}_grad"] = [float(x) for x in g]
     fd = np.zeros(4)
     for k in range(4):
         lp, lm = [], []
@@ -381,19 +459,13 @@ def diff_study(S, N, r, torch, adam_steps: int = 200, fd_eps: float = 1e-3) -> d
             img = dr.forward(base, p, o64)
             acc.append(float(torch.mean((img.double() - target.double()) ** 2)))
         fd[k] = (lp[0] - lm[0]) / (2 * fd_eps)
-    out["fd_eps"] = fd_eps
-    out["fd_grad_fp64_forward"] = [float(x) for x in fd]
-    for name in ("fp32", "fp64"):
-        out[f"{name}_adjoint_vs_fd_rel"] = [float(x) for x in np.abs(grads[name] - fd) / np.abs(fd)]
-    out["fp32_vs_fp64_adjoint_rel"] = [float(x) for x in np.abs(grads["fp32"] - grads["fp64"]) / np.abs(grads["fp64"])]
+    out["fp32_adjoint_vs_fd_rel"] = [float(x) for x in np.abs(grads["fp32"] - fd) / np.abs(fd)]
+    out["fp64_adjoint_vs_fd_rel"] = [float(x) for x in np.abs(grads["fp64"] - fd) / np.abs(fd)]
+    out["fp32_vs_fp64_adjoint_rel_max"] = float(np.max(np.abs(grads["fp32"] - grads["fp64"]) / np.abs(grads["fp64"])))
     res = D.fit(dr, base, target, guess, steps=adam_steps, opts=o32)
-    out["adam"] = {"steps": adam_steps, "seconds": res.seconds, "grad_per_s": adam_steps / res.seconds,
-                   "loss_first": float(res.loss[0]), "loss_last": float(res.loss[-1]),
-                   "params_last": [float(x) for x in res.params[-1]], "target": [float(x) for x in tgt],
-                   "abs_err_last": [float(x) for x in np.abs(res.params[-1] - np.array(tgt))],
-                   "abs_err_first": [float(x) for x in np.abs(np.array(guess) - np.array(tgt))]}
-    out["note"] = ("params (spin, incl rad, r_in M, t_scale); Adam FP32, constant per-parameter lr "
-                   "(0.02, 0.02, 0.1, 0.02); grad/s includes the image-loss seed kernel launched by torch")
+    out["adam"] = {"steps": adam_steps, "grad_per_s": adam_steps / res.seconds,
+                   "loss": [float(res.loss[0]), float(res.loss[-1])],
+                   "abs_err_last": [float(x) for x in np.abs(res.params[-1] - np.array(tgt))]}
     return out
 
 
@@ -414,8 +486,7 @@ def cli_study(reps: int = 1) -> dict:
     cli = ROOT / "singularity_gb300" / "_build" / "singularity_cuda_cli"
     if not cli.exists():
         return {"unavailable": "CLI not built"}
-    out = {"command": "singularity_cuda_cli --res 3840x2160 --samples-per-pixel 256 --scene kerr_a094.scene "
-                      "--output <png>", "reference_published_s": 162.0}
+    out = {"reference_published_s": 162.0}
     with tempfile.TemporaryDirectory() as td:
         scene = Path(td) / "kerr_a094.scene"
         scene.write_text(KERR_A094_SCENE)
@@ -431,7 +502,6 @@ def cli_study(reps: int = 1) -> dict:
                 if r.returncode != 0:
                     return {"unavailable": f"CLI exit {r.returncode}: {r.stderr[-200:]}"}
             out[f"{name}_s"] = float(min(ts))
-            out[f"{name}_vs_published"] = 162.0 / float(min(ts))
     return out
 
 
@@ -447,6 +517,7 @@ def main() -> None:
     ap.add_argument("--no-batch-study", action="store_true")
     ap.add_argument("--no-diff-study", action="store_true")
     ap.add_argument("--no-cli-study", action="store_true")
+    ap.add_argument("--no-same-algorithm", action="store_true")
     ap.add_argument("--adam-steps", type=int, default=200)
     ap.add_argument("--rhs-form", type=int, default=0)
     ap.add_argument("--integrator", choices=["adaptive", "fixed"], default="adaptive")
@@ -476,24 +547,24 @@ def main() -> None:
 
     import singularity_gb300 as S
     from singularity_gb300 import _native as N
+    from singularity_gb300 import dist as D
 
     lib = N.load()
-    # Weak scaling: each rank renders its own view (camera azimuth offset per rank).
-    isco = S.kerr_isco_prograde(1.0, 0.94)
-    from singularity_gb300 import dist as D
-    cam = S.build_orbital_camera(40.0, 0.261799, D.view_azimuth(rank, world), 30.0)
-    u = S.pack_uniforms(S.Scene(spin_a_over_M=0.94, disc_inner_M=isco, disc_outer_M=30.0, disc_peak_T_K=1e4,
-                                render_supersample=SPP), cam, WIDTH, HEIGHT, S.workloads.turbulence_time())
+    u = workload_uniforms(S)
     npix = u.width * u.height
+    # strong scaling: rank r traces slice r of the frame (interleaved 8-row bands)
+    rows = D.slice_rows(u.height, SLICE_BAND, world, rank)
     r = S.Renderer(local)
     stream = torch.cuda.Stream()
     d_out = torch.empty(npix * 4, dtype=torch.uint8, device="cuda")
     integ = N.INTEGRATOR_ADAPTIVE if args.integrator == "adaptive" else N.INTEGRATOR_FIXED
     prec = {"fp32": N.PRECISION_FP32, "mixed": N.PRECISION_MIXED, "fp64": N.PRECISION_FP64}[args.precision]
-    opts = S.default_opts(sample_count=SPP_PER_STEP, rhs_form=args.rhs_form, integrator=integ, precision=prec)
+    slices = dict(slice_count=world, slice_index=rank, slice_band=SLICE_BAND) if world > 1 else {}
+    opts = S.default_opts(sample_count=SPP_PER_STEP, rhs_form=args.rhs_form, integrator=integ, precision=prec,
+                          **slices)
     passes = SPP // SPP_PER_STEP
     step_idx = [0]
-    stats_acc = {"steps": 0, "rays": 0, "trace_ms": [], "budget": 0, "rejected": 0}
+    stats_acc = {"steps": 0, "rays": 0, "trace_ms": [], "budget": 0}
 
     def step(record=True):
         k = step_idx[0] % passes
@@ -508,7 +579,6 @@ def main() -> None:
             stats_acc["steps"] += s.steps
             stats_acc["rays"] += s.rays
             stats_acc["budget"] += s.budget_hits
-            stats_acc["rejected"] += s.rejected
             stats_acc["trace_ms"].append(s.trace_ms)
 
     for _ in range(args.warmup):
@@ -536,16 +606,26 @@ def main() -> None:
     if args.e2e_steps > 0:
         u16 = u.copy()
         u16.supersample = SPP_PER_STEP
-        host = torch.empty(npix * 4, dtype=torch.uint8, pin_memory=True)
-        e2e_opts = S.default_opts(rhs_form=args.rhs_form, integrator=integ, precision=prec)
+        host = torch.empty(npix * 4, dtype=torch.uint8, pin_memory=True) if rank == 0 else None
+        e2e_opts = S.default_opts(rhs_form=args.rhs_form, integrator=integ, precision=prec, **slices)
+        d_slice = torch.empty(u.width * rows * 4, dtype=torch.uint8, device="cuda")
 
         def e2e_step():
-            st = lib.sgx_render(r.handle, C.byref(u16), C.byref(e2e_opts))
+            if world == 1:
+                st = lib.sgx_render(r.handle, C.byref(u16), C.byref(e2e_opts))
+                if st == 0:
+                    st = lib.sgx_capture(r.handle, C.c_void_p(host.data_ptr()), host.numel(), N.FORMAT_RGBA8_SRGB)
+                if st != 0:
+                    raise RuntimeError(lib.sgx_last_error(r.handle).decode())
+                return
+            # the split frame: each rank its slice, gathered to rank 0, then to host
+            st = lib.sgx_render_device(r.handle, C.byref(u16), C.byref(e2e_opts), C.c_void_p(d_slice.data_ptr()),
+                                       N.FORMAT_RGBA8_SRGB, C.c_void_p(stream.cuda_stream))
             if st != 0:
                 raise RuntimeError(lib.sgx_last_error(r.handle).decode())
-            st = lib.sgx_capture(r.handle, C.c_void_p(host.data_ptr()), host.numel(), N.FORMAT_RGBA8_SRGB)
-            if st != 0:
-                raise RuntimeError(lib.sgx_last_error(r.handle).decode())
+            frame = D.gather_frame(d_slice.view(rows, u.width, 4), u.height, SLICE_BAND)
+            if rank == 0:
+                host.copy_(frame.reshape(-1))
         e2e_step()
         if world > 1:
             dist.barrier()
@@ -553,16 +633,16 @@ def main() -> None:
         for _ in range(args.e2e_steps):
             e2e_step()
         dt = D.max_over_ranks(time.perf_counter() - t0, "cuda")
-        e2e = {"value": npix * SPP_PER_STEP * args.e2e_steps * world / dt / 1e6, "unit": "Mrays/s",
-               "h2d_bytes_per_step": C.sizeof(N.Uniforms), "d2h_bytes_per_step": npix * 4,
-               "note": "per step sgx_render (a full 16-spp frame) + sgx_capture RGBA8 into pinned host memory, "
-                       "wall clock"}
+        e2e = {"value": npix * SPP_PER_STEP * args.e2e_steps / dt / 1e6, "unit": "Mrays/s",
+               "h2d_bytes_per_step": C.sizeof(N.Uniforms) * world, "d2h_bytes_per_step": npix * 4,
+               "note": ("per step sgx_render + sgx_capture of a full 16-spp frame into pinned host memory"
+                        if world == 1 else "per step every rank's sgx_render_device slice, NCCL gather to rank 0, "
+                                           "copy to pinned host memory") + ", wall clock"}
 
     # the batch shards its views across ranks: every rank takes part
     batch = None
     if not args.no_batch_study and args.precision != "fp64" and integ == N.INTEGRATOR_ADAPTIVE:
-        batch = batch_study(S, N, r, torch, rank=rank, world=world,
-                            sample_cap=2 if args.workload == "small" else 0)
+        batch = batch_study(S, N, r, torch, rank=rank, world=world, sample_cap=2 if args.workload == "small" else 0)
 
     if rank != 0:
         if world > 1:
@@ -571,25 +651,25 @@ def main() -> None:
 
     # --- roofline of the trace kernel ---
     from oracle import pyoracle as O
-    O.build(ref=False)
+    O.build(ref=not args.no_cpu_baseline and world == 1)
     ad = O.adaptive_opts() if integ == N.INTEGRATOR_ADAPTIVE else None
     if ad is not None and args.precision == "mixed":
         ad = O.adaptive_opts(mixed=True)
-    ops_step, mean_steps_cpu = ops_per_step(S, O, u, adaptive=ad)
+    ops_step, mean_steps_cpu = ops_per_step(O, u, adaptive=ad)
     trace_ms = np.array(stats_acc["trace_ms"])
     per_launch_ms = float(trace_ms.mean())
     steps_per_launch = stats_acc["steps"] / max(1, len(trace_ms))
     achieved = ops_step * steps_per_launch / (per_launch_ms * 1e-3) / 1e12
     peak = C.c_double(0)
     lib.sgx_measure_fp32_peak(local, 20000, C.byref(peak))
-    # DRAM bytes of the trace kernel per launch: ncu dram__bytes_read.sum +
-    # dram__bytes_write.sum of one 4K 16-spp launch of the adaptive precision form
-    # (16.6 MB + 2072.5 MB for 132,710,400 rays; the 16-byte hit record per ray,
-    # part of it still in L2 when the kernel ends), in
-    # profiles/trace_persistent_kerr_adaptive_1280x720.md; other workloads: null
+    # DRAM bytes of the trace kernel per launch from one ncu capture of a full
+    # 4K 16-spp launch of the adaptive precision form (dram__bytes_read.sum +
+    # dram__bytes_write.sum = 2,089,191,680 B for 132,710,400 rays: the 16-byte
+    # hit record per ray, part of it still in L2 when the kernel ends), scaled
+    # by this rank's rays; other workloads: null
     traffic = None
     if args.integrator == "adaptive" and args.workload == "4k" and args.precision == "mixed":
-        traffic = 2089191680 / 132710400 * npix * SPP_PER_STEP
+        traffic = 2089191680 / 132710400 * u.width * rows * SPP_PER_STEP
     roof = {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
             "frac": achieved / peak.value if peak.value else None, "traffic": traffic,
             "peak_source": "of measured: register-resident FMA ceiling (sgx_measure_fp32_peak) on this GPU; "
@@ -597,50 +677,57 @@ def main() -> None:
             "ops_per_step": ops_step, "kernel_ms_per_launch": per_launch_ms,
             "gpu_steps_per_ray": stats_acc["steps"] / max(1, stats_acc["rays"]),
             "gsteps_s": stats_acc["steps"] / (float(trace_ms.sum()) * 1e-3) / 1e9,
-            "cpu_oracle_steps_per_ray": mean_steps_cpu,
-            "ops_rule": "reference formulas, add/sub/mul/div/sqrt/min/max/transcendental = 1 each"}
+            "cpu_oracle_steps_per_ray": mean_steps_cpu}
 
-    # single-GPU properties (precision forms, HDR post-process, adjoint, CPU
-    # baseline) are measured at N = 1 only; under N ranks only the sharded
-    # batch runs, so the timed work stays short while N GPUs are held
+    # single-GPU properties (precision forms, same-algorithm comparison, HDR
+    # post-process, adjoint, CPU baseline) are measured at N = 1 only; under N
+    # ranks only the sharded batch runs, so the timed work stays short while N
+    # GPUs are held
     single = world == 1
+    adaptive_main = args.precision != "fp64" and integ == N.INTEGRATOR_ADAPTIVE
     study = None
-    if single and not args.no_precision_study and args.precision != "fp64" and integ == N.INTEGRATOR_ADAPTIVE:
-        study = precision_study(S, N, O, lib, r, u, d_out, stream, torch, opts)
-    hdr = None
-    if single and not args.no_batch_study and args.precision != "fp64" and integ == N.INTEGRATOR_ADAPTIVE:
-        hdr = hdr_bloom_study(S, N, r, torch)
-    diff = None
-    if single and not args.no_diff_study and args.precision != "fp64" and integ == N.INTEGRATOR_ADAPTIVE:
-        diff = diff_study(S, N, r, torch, adam_steps=args.adam_steps)
-    cli = None
-    if single and not args.no_cli_study and args.workload == "4k":
-        cli = cli_study()
-    cpu = None if (args.no_cpu_baseline or rank != 0 or not single) else cpu_baseline(S, O, u)
+    if single and not args.no_precision_study and adaptive_main:
+        study = precision_study(S, N, O, lib, r, u, d_out, stream, torch)
+    same = None
+    if single and not args.no_same_algorithm and args.workload == "4k":
+        same = same_algorithm_study(S, N, lib, r, u, d_out, stream, torch)
+        if study is not None:
+            same["adaptive_steps_per_ray"] = study["mixed_steps_per_ray"]
+    hdr = hdr_bloom_study(S, N, r, torch) if single and not args.no_batch_study and adaptive_main else None
+    diff = (diff_study(S, N, r, torch, adam_steps=args.adam_steps)
+            if single and not args.no_diff_study and adaptive_main else None)
+    cli = cli_study() if single and not args.no_cli_study and args.workload == "4k" else None
+    cpu = None
+    if single and not args.no_cpu_baseline:
+        cpu = (reference_cpu_rate(O, O.ref_headline_uniforms(WIDTH, HEIGHT, SPP, TURB_TIME))
+               if O.ref_available() else None)
     clocks = clk.summary()
-    wl = (f"kerr_a0.94_r40_i75_fov30_isco-30M_T1e4_{WIDTH}x{HEIGHT}_256spp_"
-          + ("adaptive_tol1e-6" if integ == N.INTEGRATOR_ADAPTIVE else "fixed_h0.4_max2500") + f"_{args.precision}")
+    algo = ("adaptive_tol1e-6_projected" if integ == N.INTEGRATOR_ADAPTIVE else "fixed_h0.4_max2500")
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "strong",
         "vs_baseline": value / 13.1, "dtype": "f32" if args.precision != "fp64" else "f64", "data": "synthetic",
-        "config": {"workload": wl, "spp_per_step": SPP_PER_STEP, "rays_per_step": npix * SPP_PER_STEP,
-                   "integrator": ("error-controlled RK4, FSAL 3rd-order estimate, tol 1e-6"
-                                  if integ == N.INTEGRATOR_ADAPTIVE else "fixed-step RK4 (reference algorithm)"),
+        "config": {"workload": f"{scene_name()}_{algo}_{args.precision}", "spp_per_step": SPP_PER_STEP,
+                   "rays_per_step": npix * SPP_PER_STEP,
+                   "integrator": ("error-controlled RK4, FSAL 3rd-order estimate, tol 1e-6, p_theta projected "
+                                  "onto Q" if integ == N.INTEGRATOR_ADAPTIVE
+                                  else "fixed-step RK4 h = 0.4 (the reference's algorithm)"),
                    "precision": args.precision, "rhs_form": args.rhs_form,
+                   "parallelism": f"frame split in {world} slices of 8-row bands" if world > 1 else "1 GPU",
                    "l2": "each step writes a 2.1 GB per-sample buffer (> 129 MB L2); no extra flush",
                    "vs_baseline_basis": "13.1 Mrays/s: 4K Kerr a/M=0.94 256 spp in 162 s on an RTX 3090 "
                                         "(README.md:39,130), wall clock incl. PNG, fixed step h=0.4"},
-        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+        "roofline": sig(roof, 5), "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
         "gpu_launches": 3 * args.steps,
         "budget_exhausted_rays": stats_acc["budget"],
-        "precision_study": study,
-        "batched_views": batch,
-        "hdr_bloom_1080p": hdr,
-        "adjoint_512x512x4": diff,
-        "cli_4k_256spp": cli,
+        "batched_views": sig(batch),
+        "hdr_bloom_1080p": sig(hdr),
+        "adjoint_512x512x4": sig(diff, 3),
+        "cli_4k_256spp": sig(cli),
+        "same_algorithm_4k_16spp": sig(same),
+        "precision_study": sig(study, 3),
     }
-    print(json.dumps(line), flush=True)
+    print(json.dumps(line, separators=(",", ":")), flush=True)
     if world > 1:
         dist.destroy_process_group()
 

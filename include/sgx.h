@@ -85,7 +85,17 @@ typedef struct sgx_render_opts {
                                     integrator always carries them, so there 2 equals 0) */
     uint32_t tile_w;         /* ray order: tiles of tile_w x tile_h pixels, samples innermost;  */
     uint32_t tile_h;         /*   0 = whole rows (tile_w = width, tile_h = 1)                  */
+    uint32_t projection;     /* adaptive: 1 = after every accepted step p_theta is projected
+                                back onto the ray's Carter constant (default), 0 = off */
+    uint32_t slice_count;    /* frame split (one frame over several GPUs): the rows are dealt in  */
+    uint32_t slice_index;    /*   bands of slice_band rows, band b to slice b % slice_count; the  */
+    uint32_t slice_band;     /*   render traces slice slice_index only and writes its rows packed
+                                  top to bottom: width x sgx_slice_rows(...) pixels, each equal to
+                                  the whole frame's pixel.  slice_count 0 or 1 = the whole frame;
+                                  slice_band 0 = SGX_SLICE_BAND_DEFAULT.  sgx_render_device only. */
 } sgx_render_opts;
+
+#define SGX_SLICE_BAND_DEFAULT 8u
 
 /* Counters of the last render (summed over its passes). */
 typedef struct sgx_render_stats {
@@ -176,6 +186,13 @@ sgx_scene_status sgx_scene_config_load_string(const char* text, sgx_scene_config
                                               char* errbuf, size_t errbuf_len);
 /* kerr_isco_prograde (core/include/physics/kerr.hpp:85-104). */
 float sgx_kerr_isco_prograde(float mass, float spin);
+/* Frame split (no counterpart in the reference, which renders a frame on one
+ * GPU, render/cuda/cuda_backend.cu:140-152): the rows of slice `index` of
+ * `count` (bands of `band` rows dealt round-robin; band 0 =
+ * SGX_SLICE_BAND_DEFAULT): how many, and the frame row of its local row
+ * `local` (UINT32_MAX when out of range). */
+uint32_t sgx_slice_rows(uint32_t height, uint32_t band, uint32_t count, uint32_t index);
+uint32_t sgx_slice_row(uint32_t height, uint32_t band, uint32_t count, uint32_t index, uint32_t local);
 
 /* ---- context: CudaBackend lifecycle ----------------------------------- */
 /* CudaBackend() + the device it runs on.  device < 0 -> the current device. */
@@ -213,6 +230,19 @@ sgx_status sgx_render_device(sgx_context* ctx, const sgx_uniforms* u, const sgx_
 sgx_status sgx_trace_samples(sgx_context* ctx, const sgx_uniforms* u, const sgx_render_opts* opts, uint64_t n,
                              const uint32_t* gx, const uint32_t* gy, const uint32_t* s, float* hdr3,
                              uint32_t* steps, uint32_t* term);
+
+/* Constants of motion of n samples traced as sgx_trace_samples traces them,
+ * for the error-controlled Kerr integrator (opts->integrator ADAPTIVE, Kerr
+ * uniforms; anything else is SGX_ERR_UNSUPPORTED).  No counterpart in the
+ * reference, whose Carter-constant claim (README.md:97) no code measures.
+ * inv5 (host, n x 5 doubles) gets per sample, evaluated in FP64: E, L_z, the
+ * Carter constant Q0 the ray started with (the FP32 form's FP32 value, the
+ * mixed and FP64 forms' FP64 value), the Carter constant of the ray's last
+ * state and 2H of that state (kerr_hamilton.h:37-60); a sample whose camera
+ * ray has no root gets NaNs.  term (may be NULL) as in sgx_trace_samples. */
+sgx_status sgx_trace_invariants(sgx_context* ctx, const sgx_uniforms* u, const sgx_render_opts* opts, uint64_t n,
+                                const uint32_t* gx, const uint32_t* gy, const uint32_t* s, double* inv5,
+                                uint32_t* term);
 
 /* ---- HDR bloom and display transform ------------------------------------------ */
 /* The realtime backends' post-process (render/vulkan/shaders/bloom.hlsl:8-77,
@@ -266,20 +296,21 @@ sgx_status sgx_autotune(sgx_context* ctx, const sgx_uniforms* views, uint32_t n,
 
 /* ---- allocation-free render ------------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device
- * memory — code issuing work while a stream is captured into a CUDA graph,
- * hosts whose device memory all belongs to their own pool, frame-paced callers
- * that cannot take cudaFree's device-wide synchronisation — this renders one
- * whole frame (all samples, fixed-step integrator, FP32 or FP64) into the
- * caller's device buffer d_out on the caller's stream without allocating
- * anything: its scratch is a fixed SGX_NOALLOC_SCRATCH_BYTES array inside the
- * library, held by every GPU that loads the library until exit.  A frame needs
- * 16 * width * height * (spp + 1) + 4096 bytes of it (FP64:
- * 16 * width * height * (2 * spp + 1) + 4096); larger frames return
- * SGX_ERR_INVALID_ARGUMENT with the reason in err (a caller buffer, may be
- * NULL).  The first call on a device does a one-time set-up (looks up the
- * array's device address) and should come before any stream capture.  Calls
- * share the array: calls whose GPU work overlaps race, so issue them on one
- * stream. */
+ * memory — host applications (game engines, plug-in renderers) that reserve
+ * the GPU's memory for their own pool at start-up and forbid allocations by
+ * libraries, and frame-paced callers that cannot take the device-wide
+ * synchronisation of cudaFree mid-frame — this renders one whole frame (all
+ * samples, fixed-step integrator, FP32 or FP64) into the caller's device
+ * buffer d_out on the caller's stream without allocating anything: its
+ * scratch is a fixed SGX_NOALLOC_SCRATCH_BYTES array inside the library, held
+ * by every GPU that loads the library until exit.  A frame needs
+ * 4096 + align256(16 * width * height) + R * width * height * spp bytes of it
+ * (R = 16 for FP32, 32 for FP64; align256 rounds up to a multiple of 256);
+ * larger frames return SGX_ERR_INVALID_ARGUMENT with the reason in err (a
+ * caller buffer, may be NULL).  The first call on a device does a one-time
+ * set-up (looks up the array's device address) and should come before any
+ * stream capture.  Calls share the array: calls whose GPU work overlaps race,
+ * so issue them on one stream. */
 #define SGX_NOALLOC_SCRATCH_BYTES (64ull << 20)
 sgx_status sgx_render_noalloc(const sgx_uniforms* u, const sgx_render_opts* opts, void* d_out, uint32_t format,
                               void* stream, char* err, size_t err_len);

@@ -71,7 +71,7 @@ struct AdaptiveOpts {
     std::uint32_t max_steps;  // attempt budget (accepted + rejected); 0 -> the uniforms' max_steps
     std::uint32_t mixed;      // 1: the mixed precision form (T = float only)
     std::uint32_t no_early_capture;  // 1: only the reference's horizon cut ends a captured ray (tests)
-    std::uint32_t pad1;
+    std::uint32_t no_projection;     // 1: leave p_theta as integrated (no projection onto Q)
 };
 
 // Per-ray diagnostics for the precision comparison.
@@ -114,6 +114,22 @@ inline double carter_Q(double theta, double p_theta, double E, double L, double 
 }
 
 template <class T> inline T abs_(T x) { return x < OLIT(0.0) ? -x : x; }
+
+// p_theta put back onto the ray's Carter constant after an accepted step
+// (a projection method, Hairer, Lubich & Wanner, Geometric Numerical
+// Integration, IV.4): |p_theta| = sqrt(Theta), Theta = Q - c^2 (L^2 / s^2 -
+// a^2 E^2) with s^2 guarded at 1e-10 as in the right-hand side, the sign of
+// p_theta kept; p_theta = 0 where truncation has carried the state past a
+// turning point (Theta < 0).  Q and L are exact constants of the flow, so
+// this removes the integrator's drift off the level set Q = Q0 without
+// touching r, theta, phi or p_r.
+template <class T> inline T project_p_theta(T pth, T s, T c, T Q, T L2, T a2E2) {
+    const T s2 = s * s;
+    const T safe = s2 < OLIT(1e-10) ? OLIT(1e-10) : s2;
+    const T th = Q - c * c * (L2 / safe - a2E2);
+    const T m = th > OLIT(0.0) ? M<T>::sqrt(th) : OLIT(0.0);
+    return pth < OLIT(0.0) ? -m : m;
+}
 
 // State of the error-controlled form: theta carried as (sin theta, cos theta).
 template <class T> struct SCState {
@@ -283,6 +299,9 @@ inline TraceOut<T> trace_kerr_adaptive(const CamRay<T>& cam, const Params<T>& u,
         r_cap = r_cap < u.r_in ? r_cap : u.r_in;
     }
 
+    // the projection's constants: Q in T (the mixed form's from its FP64 value)
+    const T Qp = mixed ? T(float(Qd)) : c.Q;
+    const T L2 = c.L * c.L, a2E2 = (u.spin_a * c.E) * (u.spin_a * c.E);
     T h = T(o.h_init_frac) * y.r;
     SCState<T> k1 = sc_rhs(y, c);
     std::uint32_t accepted = 0, rejected = 0, zone_steps = 0, steps = 0;
@@ -342,6 +361,7 @@ inline TraceOut<T> trace_kerr_adaptive(const CamRay<T>& cam, const Params<T>& u,
         const T n = OLIT(1.5) - OLIT(0.5) * (y.s * y.s + y.c * y.c);
         y.s = y.s * n;
         y.c = y.c * n;
+        if (o.no_projection == 0u) y.p_theta = project_p_theta(y.p_theta, y.s, y.c, Qp, L2, a2E2);
         k1 = at.k5;
     }
     if (diag != nullptr) {

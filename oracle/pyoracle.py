@@ -7,7 +7,14 @@ this module, and only as the checker.  It loads:
   adaptive_oracle.hpp), built by ``make -C oracle``;
 * ``oracle/_ref/libref_host.so`` — the reference's own kernel source compiled
   for the host CPU (``make -C oracle ref``), present only where the reference
-  tree is.
+  sources are.
+
+Where the reference sources are: ``reference_root()`` — the directory named by
+the environment variable SGX_REFERENCE_ROOT; else the reference checkout of
+this build environment, /root/reference; else the snapshot
+``oracle/_ref/src`` that ``make -C oracle snapshot`` leaves beside the
+builds (the reference files the recipes compile, so that a machine without the
+checkout, such as the GPU host, can build them).
 """
 
 from __future__ import annotations
@@ -23,19 +30,42 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libref_host.so"
-REFERENCE_ROOT = Path(os.environ.get("SGX_REFERENCE_ROOT", "/root/reference"))
+SNAPSHOT = HERE / "_ref" / "src"
+_CHECKOUT = Path("/root/reference")  # the reference checkout of this build environment
+
+
+def _has_sources(root: Path) -> bool:
+    return (root / "render" / "cuda" / "kernels" / "geodesic_kernel.cu").exists()
+
+
+def reference_checkout() -> Path | None:
+    """A full checkout of the reference, if this machine has one."""
+    env = os.environ.get("SGX_REFERENCE_ROOT")
+    for root in ([Path(env)] if env else []) + [_CHECKOUT]:
+        if _has_sources(root):
+            return root
+    return None
+
+
+def reference_root() -> Path | None:
+    """The reference sources to compile: a checkout, else the snapshot, else None."""
+    root = reference_checkout()
+    if root is not None:
+        return root
+    return SNAPSHOT if _has_sources(SNAPSHOT) else None
 
 
 class AdaptiveOpts(C.Structure):
     _fields_ = [("tol", C.c_float), ("h_init_frac", C.c_float), ("h_max_frac", C.c_float), ("zone", C.c_float),
                 ("max_steps", C.c_uint32), ("mixed", C.c_uint32), ("no_early_capture", C.c_uint32),
-                ("pad1", C.c_uint32)]
+                ("no_projection", C.c_uint32)]
 
 
 def adaptive_opts(tol=1e-6, h_init_frac=0.02, h_max_frac=0.1, zone=0.05, max_steps=0, mixed=False,
-                  early_capture=True) -> "AdaptiveOpts":
+                  early_capture=True, projection=True) -> "AdaptiveOpts":
     """The adaptive integrator's options (defaults = the library's defaults)."""
-    return AdaptiveOpts(tol, h_init_frac, h_max_frac, zone, max_steps, int(bool(mixed)), int(not early_capture), 0)
+    return AdaptiveOpts(tol, h_init_frac, h_max_frac, zone, max_steps, int(bool(mixed)), int(not early_capture),
+                        int(not projection))
 
 
 class RayDiag(C.Structure):
@@ -175,10 +205,29 @@ def crossing(th_prev: float, th_curr: float):
 
 
 def build(ref: bool = True) -> None:
-    """Compile the oracle (and the reference host build when its sources exist)."""
+    """Compile the oracle, and with ref=True the reference's own kernel source
+    for the host and as PTX when its sources exist (refreshing the snapshot
+    from a checkout)."""
     subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
-    if ref and (REFERENCE_ROOT / "render" / "cuda" / "kernels" / "geodesic_kernel.cu").exists():
-        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REFERENCE_ROOT={REFERENCE_ROOT}"], check=True)
+    if not ref:
+        return
+    checkout = reference_checkout()
+    if checkout is not None:
+        subprocess.run(["make", "-s", "-C", str(HERE), "snapshot", f"REFERENCE_ROOT={checkout}"], check=True)
+    root = reference_root()
+    if root is not None:
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REFERENCE_ROOT={root}"], check=True)
+
+
+def build_relink() -> Path | None:
+    """The reference's unmodified cuda_cli/main.cpp compiled against this
+    library's CudaBackend shim and linked with libsgx.so (needs the library
+    built and the reference sources); None without the sources."""
+    root = reference_root()
+    if root is None:
+        return None
+    subprocess.run(["make", "-s", "-C", str(HERE), "relink", f"REFERENCE_ROOT={root}"], check=True)
+    return HERE / "_ref" / "ref_cuda_cli_relinked"
 
 
 _lib = None
@@ -301,6 +350,65 @@ def ref_trace(u, gx, gy, s, threads: int | None = None) -> np.ndarray:
     hdr = np.zeros((gx.size, 3), dtype=np.float32)
     ref_lib().ref_trace_hdr(_u(u), C.c_int64(gx.size), _p(gx), _p(gy), _p(s), _p(hdr), C.c_int(threads))
     return hdr
+
+
+class RefUniforms(C.Structure):
+    """The reference's 160-byte Uniforms block (shared_shader/uniforms.h:54-95)."""
+
+    _fields_ = [("cam_pos", C.c_float * 4), ("cam_fwd", C.c_float * 4), ("cam_right", C.c_float * 4),
+                ("cam_up", C.c_float * 4), ("mass_M", C.c_float), ("spin_a", C.c_float), ("rs", C.c_float),
+                ("tan_half_fov", C.c_float), ("disc_r_inner", C.c_float), ("disc_r_outer", C.c_float),
+                ("disc_peak_T", C.c_float), ("aspect", C.c_float), ("h_step", C.c_float), ("escape_r", C.c_float),
+                ("horizon_cut", C.c_float), ("time_sec", C.c_float), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("metric_type", C.c_uint32), ("flags", C.c_uint32), ("max_steps", C.c_uint32),
+                ("frame_index", C.c_uint32), ("supersample", C.c_uint32), ("pad_b", C.c_uint32),
+                ("exposure", C.c_float), ("bloom_threshold", C.c_float), ("bloom_strength", C.c_float),
+                ("disc_turbulence", C.c_float)]
+
+
+# field order of the reference's Scene (render/include/render_backend.hpp:46-82)
+REF_SCENE_FIELDS = ("metric", "mass_solar", "spin_a_over_M", "disc_inner_M", "disc_outer_M", "disc_doppler_on",
+                    "disc_redshift_on", "disc_texture_on", "show_overlay", "render_supersample", "exposure",
+                    "bloom_threshold", "bloom_strength", "disc_turbulence", "disc_peak_T_K", "max_steps", "h_step")
+
+
+def ref_scene(**fields) -> np.ndarray:
+    """The reference's Scene{} defaults with `fields` replaced (metric: 1 Kerr, 0 Schwarzschild)."""
+    sc = np.zeros(17, dtype=np.float32)
+    ref_lib().ref_scene_default(_p(sc))
+    for k, v in fields.items():
+        sc[REF_SCENE_FIELDS.index(k)] = float(v)
+    return sc
+
+
+def ref_isco_prograde(mass: float, spin: float) -> float:
+    fn = ref_lib().ref_kerr_isco_prograde
+    fn.restype = C.c_float
+    fn.argtypes = [C.c_float, C.c_float]
+    return float(fn(mass, spin))
+
+
+def ref_pack_uniforms(scene17: np.ndarray, cam13: np.ndarray, width: int, height: int,
+                      time_sec: float = 0.0) -> RefUniforms:
+    """The uniform block CudaBackend::render_frame packs (render/cuda/cuda_backend.cu:45-101)."""
+    u = RefUniforms()
+    sc = np.ascontiguousarray(scene17, dtype=np.float32)
+    cam = np.ascontiguousarray(cam13, dtype=np.float32)
+    ref_lib().ref_pack_uniforms(_p(sc), _p(cam), C.c_uint32(width), C.c_uint32(height), C.c_float(time_sec),
+                                C.byref(u))
+    return u
+
+
+def ref_headline_uniforms(width: int = 3840, height: int = 2160, spp: int = 256,
+                          time_sec: float = 7.0 / 30.0) -> RefUniforms:
+    """The Kerr a/M = 0.94 benchmark scene through the reference's own code: its
+    orbital camera at r = 40 M, elevation 0.261799 rad (inclination 75 deg),
+    azimuth 0, FOV 30 deg; disc from its prograde ISCO to 30 M at 1e4 K; its
+    uniform packing (fixed step h = 0.4, 2500 steps)."""
+    isco = ref_isco_prograde(1.0, 0.94)
+    sc = ref_scene(metric=1, spin_a_over_M=0.94, disc_inner_M=isco, disc_outer_M=30.0, disc_peak_T_K=1e4,
+                   render_supersample=spp)
+    return ref_pack_uniforms(sc, ref_orbital_camera(40.0, 0.261799, 0.0, 30.0), width, height, time_sec)
 
 
 def ref_orbital_camera(distance, elevation, azimuth, fov_deg) -> np.ndarray:

@@ -18,6 +18,7 @@
 #include <atomic>
 #include <sstream>
 #include <cstdint>
+#include <cstring>
 #include <thread>
 #include <vector>
 
@@ -37,6 +38,8 @@ static inline unsigned int min(unsigned int a, unsigned int b) { return a < b ? 
 #include SGX_REFERENCE_KERNEL
 
 static_assert(sizeof(Uniforms) == 160, "reference Uniforms layout");
+
+#include "physics/kerr.hpp"
 
 // The reference CLI translation unit, for its build_orbital_camera and the
 // scene loader it includes.  Its main() is renamed and never called; the
@@ -118,6 +121,91 @@ void ref_build_orbital_camera(float distance, float elevation, float azimuth, fl
     for (int i = 0; i < 3; ++i) out13[i] = cam.position[i];
     for (int i = 0; i < 9; ++i) out13[3 + i] = cam.basis[i];
     out13[12] = cam.fov_y_radians;
+}
+
+// The reference's Scene{} defaults (render/include/render_backend.hpp:46-82)
+// as the 17 floats ref_pack_uniforms takes.
+void ref_scene_default(float* scene17) {
+    const singularity::Scene sc{};
+    const float f[17] = {sc.metric == singularity::Scene::MetricType::Kerr ? 1.0f : 0.0f, sc.mass_solar,
+                         sc.spin_a_over_M, sc.disc_inner_M, sc.disc_outer_M, sc.disc_doppler_on ? 1.0f : 0.0f,
+                         sc.disc_redshift_on ? 1.0f : 0.0f, sc.disc_texture_on ? 1.0f : 0.0f,
+                         sc.show_overlay ? 1.0f : 0.0f, float(sc.render_supersample), sc.exposure,
+                         sc.bloom_threshold, sc.bloom_strength, sc.disc_turbulence, sc.disc_peak_T_K,
+                         float(sc.max_steps), sc.h_step};
+    for (int i = 0; i < 17; ++i) scene17[i] = f[i];
+}
+
+// kerr_isco_prograde (core/include/physics/kerr.hpp:85-104), the reference's own.
+float ref_kerr_isco_prograde(float mass, float spin) { return singularity::physics::kerr_isco_prograde(mass, spin); }
+
+// The uniform block CudaBackend::render_frame hands the kernel: the semantics
+// of pack_uniforms_cuda (render/cuda/cuda_backend.cu:45-101) restated over the
+// reference's own Scene, CameraState and Uniforms types — the camera basis
+// rows (right, up, -forward), tan of half the FOV and aspect in float, lengths
+// scaled by the mass, the backend's step defaults (h 0.4, 2500 steps) where
+// the scene leaves 0, escape at 200 M and capture at 1.02 r_s, the starfield
+// always on and the disc / Doppler / redshift bits from the scene.  scene17
+// holds the Scene fields in declaration order (bools and integers as floats);
+// cam13 the camera's position[3], basis[9] and fov_y_radians.
+void ref_pack_uniforms(const float* scene17, const float* cam13, std::uint32_t w, std::uint32_t h, float time_sec,
+                       void* out160) {
+    singularity::Scene sc{};
+    sc.metric = scene17[0] != 0.0f ? singularity::Scene::MetricType::Kerr : singularity::Scene::MetricType::Schwarzschild;
+    sc.mass_solar = scene17[1];
+    sc.spin_a_over_M = scene17[2];
+    sc.disc_inner_M = scene17[3];
+    sc.disc_outer_M = scene17[4];
+    sc.disc_doppler_on = scene17[5] != 0.0f;
+    sc.disc_redshift_on = scene17[6] != 0.0f;
+    sc.disc_texture_on = scene17[7] != 0.0f;
+    sc.show_overlay = scene17[8] != 0.0f;
+    sc.render_supersample = std::uint32_t(scene17[9]);
+    sc.exposure = scene17[10];
+    sc.bloom_threshold = scene17[11];
+    sc.bloom_strength = scene17[12];
+    sc.disc_turbulence = scene17[13];
+    sc.disc_peak_T_K = scene17[14];
+    sc.max_steps = std::uint32_t(scene17[15]);
+    sc.h_step = scene17[16];
+    singularity::CameraState cam{};
+    for (int i = 0; i < 3; ++i) cam.position[i] = cam13[i];
+    for (int i = 0; i < 9; ++i) cam.basis[i] = cam13[3 + i];
+    cam.fov_y_radians = cam13[12];
+
+    Uniforms u{};
+    const float* b = cam.basis;
+    u.cam_pos = {cam.position[0], cam.position[1], cam.position[2], 0.0f};
+    u.cam_right = {b[0], b[1], b[2], 0.0f};
+    u.cam_up = {b[3], b[4], b[5], 0.0f};
+    u.cam_fwd = {-b[6], -b[7], -b[8], 0.0f};
+    u.tan_half_fov = std::tan(0.5f * cam.fov_y_radians);
+    u.aspect = float(w) / float(h);
+    const float M = sc.mass_solar;
+    u.mass_M = M;
+    u.spin_a = sc.spin_a_over_M * M;
+    u.rs = 2.0f * M;
+    u.disc_r_inner = sc.disc_inner_M * M;
+    u.disc_r_outer = sc.disc_outer_M * M;
+    u.disc_peak_T = sc.disc_peak_T_K;
+    u.h_step = sc.h_step > 0.0f ? sc.h_step : 0.4f;
+    u.escape_r = 200.0f * M;
+    u.horizon_cut = 1.02f * u.rs;
+    u.time_sec = time_sec;
+    u.width = w;
+    u.height = h;
+    u.metric_type = sc.metric == singularity::Scene::MetricType::Kerr ? SING_METRIC_KERR : SING_METRIC_SCHWARZSCHILD;
+    u.flags = SING_FLAG_STARFIELD_ON | (sc.disc_texture_on ? SING_FLAG_DISC_ON : 0u) |
+              (sc.disc_doppler_on ? SING_FLAG_DOPPLER_ON : 0u) | (sc.disc_redshift_on ? SING_FLAG_REDSHIFT_ON : 0u);
+    u.max_steps = sc.max_steps != 0u ? sc.max_steps : 2500u;
+    u.frame_index = 0;
+    u.supersample = sc.render_supersample == 0u ? 1u : sc.render_supersample;
+    u.pad_b = 0;
+    u.exposure = sc.exposure;
+    u.bloom_threshold = sc.bloom_threshold;
+    u.bloom_strength = sc.bloom_strength;
+    u.disc_turbulence = sc.disc_turbulence;
+    std::memcpy(out160, &u, sizeof(u));
 }
 
 // load_scene_config_from_stream (core/include/scene/scene_config.hpp:134-191)

@@ -9,11 +9,11 @@ from . import _native, workloads
 from .backend import (Batch, CameraState, CudaBackend, ImageData, MetricType, RenderConfig, Renderer, Scene,
                       SceneConfig, SceneLoadResult, SceneLoadStatus, SgxError, build_orbital_camera,
                       default_opts, kerr_isco_prograde, load_scene_config_from_file,
-                      load_scene_config_from_string, pack_uniforms, autotune)
+                      load_scene_config_from_string, pack_uniforms, autotune, carter_drift)
 
 __all__ = [
     "Batch", "autotune", "workloads", "CameraState", "CudaBackend", "ImageData", "MetricType", "RenderConfig", "Renderer", "Scene",
     "SceneConfig", "SceneLoadResult", "SceneLoadStatus", "SgxError", "build_orbital_camera", "default_opts",
     "kerr_isco_prograde", "load_scene_config_from_file", "load_scene_config_from_string", "pack_uniforms",
-    "_native",
+    "carter_drift", "_native",
 ]

@@ -24,6 +24,7 @@ SGX_METRIC_KERR = 1
 
 SGX_OK = 0
 NOALLOC_SCRATCH_BYTES = 64 << 20
+SLICE_BAND_DEFAULT = 8
 STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory",
                 4: "no frame rendered", 5: "unsupported"}
 
@@ -78,7 +79,8 @@ class RenderOpts(C.Structure):
         ("fp64_zone", C.c_float),
         ("sample_begin", C.c_uint32), ("sample_count", C.c_uint32), ("block_threads", C.c_uint32),
         ("blocks_per_sm", C.c_uint32), ("refill_interval", C.c_uint32), ("rhs_form", C.c_uint32),
-        ("tile_w", C.c_uint32), ("tile_h", C.c_uint32),
+        ("tile_w", C.c_uint32), ("tile_h", C.c_uint32), ("projection", C.c_uint32),
+        ("slice_count", C.c_uint32), ("slice_index", C.c_uint32), ("slice_band", C.c_uint32),
     ]
 
 
@@ -187,6 +189,10 @@ SIGNATURES = [
     ("sgx_measure_fp32_peak", C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
     ("sgx_trace_samples", C.c_int, [_P, C.POINTER(Uniforms), C.POINTER(RenderOpts), C.c_uint64, _U32P, _U32P,
                                     _U32P, _F32P, _U32P, _U32P]),
+    ("sgx_trace_invariants", C.c_int, [_P, C.POINTER(Uniforms), C.POINTER(RenderOpts), C.c_uint64, _U32P, _U32P,
+                                       _U32P, C.POINTER(C.c_double), _U32P]),
+    ("sgx_slice_rows", C.c_uint32, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32]),
+    ("sgx_slice_row", C.c_uint32, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32]),
 ]
 
 _lib = None

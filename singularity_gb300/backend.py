@@ -285,6 +285,31 @@ class Renderer:
             hdr.ctypes.data_as(f32), steps.ctypes.data_as(u32), term.ctypes.data_as(u32)))
         return hdr, steps, term
 
+    def trace_invariants(self, u: N.Uniforms, gx, gy, s, opts: Optional[N.RenderOpts] = None):
+        """Constants of motion of listed samples of the error-controlled form:
+        (n, 5) float64 [E, L_z, Q0, Q_end, 2H_end] and the termination kinds."""
+        gx = np.ascontiguousarray(gx, dtype=np.uint32)
+        gy = np.ascontiguousarray(gy, dtype=np.uint32)
+        s = np.ascontiguousarray(s, dtype=np.uint32)
+        n = gx.size
+        inv = np.zeros((n, 5), dtype=np.float64)
+        term = np.zeros(n, dtype=np.uint32)
+        u32 = C.POINTER(C.c_uint32)
+        self._check(self._lib.sgx_trace_invariants(
+            self._h, C.byref(u), C.byref(opts) if opts is not None else None, n,
+            gx.ctypes.data_as(u32), gy.ctypes.data_as(u32), s.ctypes.data_as(u32),
+            inv.ctypes.data_as(C.POINTER(C.c_double)), term.ctypes.data_as(u32)))
+        return inv, term
+
+
+def carter_drift(inv: np.ndarray, spin_a: float) -> np.ndarray:
+    """|Q_end - Q0| / (|Q0| + L^2 + a^2 E^2) per sample from trace_invariants'
+    rows (NaN rows, samples without a camera root, dropped)."""
+    E, L, Q0, Q1 = inv[:, 0], inv[:, 1], inv[:, 2], inv[:, 3]
+    ok = np.isfinite(inv).all(axis=1)
+    norm = np.abs(Q0) + L * L + (spin_a * E) ** 2
+    return (np.abs(Q1 - Q0) / norm)[ok]
+
 
 class Batch:
     """Many views in one persistent launch replayed from a CUDA graph (sgx_batch)."""

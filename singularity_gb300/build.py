@@ -52,7 +52,8 @@ def _newer(target: Path, deps: list[Path]) -> bool:
 def build_library(force: bool = False, verbose: bool = False) -> Path:
     """Compile libsgx.so (and the CLI) if any source is newer than the output."""
     BUILD.mkdir(parents=True, exist_ok=True)
-    headers = list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.hpp")) + list(INCLUDE.glob("*.h"))
+    headers = (list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.hpp")) + list((CSRC / "render_api").glob("*.hpp"))
+               + list(INCLUDE.glob("*.h")))
     nvcc = _nvcc()
     cuda = Path(nvcc).resolve().parent.parent
     jobs = []
@@ -78,7 +79,7 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
     cli = BUILD / "singularity_cuda_cli"
     cli_srcs = [CSRC / "cuda_backend.cpp", CSRC / "cli_main.cpp"]
     if all(s.exists() for s in cli_srcs) and (force or not _newer(cli, cli_srcs + headers + [lib])):
-        _run(["g++", *CXX_FLAGS, "-pthread", f"-I{cuda / 'include'}", *map(str, cli_srcs),
+        _run(["g++", *CXX_FLAGS, f"-I{CSRC / 'render_api'}", "-pthread", f"-I{cuda / 'include'}", *map(str, cli_srcs),
               str(BUILD / "sgx_host.cpp.o"), "-o", str(cli), f"-L{BUILD}", "-lsgx", "-Wl,-rpath,$ORIGIN"])
     if verbose:
         print(f"built {lib}")

@@ -471,8 +471,12 @@ int main(int argc, char** argv) {
 
     for (std::uint32_t f = 0; f < frames; ++f) {
         const float az = camera_azimuth + (frames > 1 ? (kTwoPi * float(f) / float(frames)) : 0.0f);
+        sgx_camera cc{};
+        sgx_build_orbital_camera(&cc, camera_distance, camera_elevation, az, fov_y_deg);
         singularity::CameraState camera{};
-        sgx::build_orbital_camera(camera, camera_distance, camera_elevation, az, fov_y_deg);
+        for (int i = 0; i < 3; ++i) camera.position[i] = cc.position[i];
+        for (int i = 0; i < 9; ++i) camera.basis[i] = cc.basis[i];
+        camera.fov_y_radians = cc.fov_y_radians;
         backend.render_frame(scene, camera);  // overlaps the previous frame's write
         auto img = std::make_shared<singularity::ImageData>(backend.capture_frame());
         if (img->pixels_rgba.empty() || img->width == 0 || img->height == 0) {

@@ -9,6 +9,43 @@
 
 namespace singularity {
 
+namespace {
+
+// The interface's Scene and CameraState as the C ABI's structs (field for
+// field; the C struct keeps bools as 0/1).
+sgx_scene scene_to_c(const Scene& s) {
+    sgx_scene c{};
+    c.metric = static_cast<std::uint32_t>(s.metric);
+    c.mass_solar = s.mass_solar;
+    c.spin_a_over_M = s.spin_a_over_M;
+    c.disc_inner_M = s.disc_inner_M;
+    c.disc_outer_M = s.disc_outer_M;
+    c.disc_doppler_on = s.disc_doppler_on ? 1u : 0u;
+    c.disc_redshift_on = s.disc_redshift_on ? 1u : 0u;
+    c.disc_texture_on = s.disc_texture_on ? 1u : 0u;
+    c.show_overlay = s.show_overlay ? 1u : 0u;
+    c.render_supersample = s.render_supersample;
+    c.exposure = s.exposure;
+    c.bloom_threshold = s.bloom_threshold;
+    c.bloom_strength = s.bloom_strength;
+    c.disc_turbulence = s.disc_turbulence;
+    c.disc_peak_T_K = s.disc_peak_T_K;
+    c.max_steps = s.max_steps;
+    c.h_step = s.h_step;
+    c.adaptive_step_on = s.adaptive_step_on ? 1u : 0u;
+    return c;
+}
+
+sgx_camera camera_to_c(const CameraState& cam) {
+    sgx_camera c{};
+    for (int i = 0; i < 3; ++i) c.position[i] = cam.position[i];
+    for (int i = 0; i < 9; ++i) c.basis[i] = cam.basis[i];
+    c.fov_y_radians = cam.fov_y_radians;
+    return c;
+}
+
+}  // namespace
+
 CudaBackend::CudaBackend() = default;
 
 CudaBackend::~CudaBackend() { shutdown(); }
@@ -53,7 +90,10 @@ void CudaBackend::resize(std::uint32_t width, std::uint32_t height) {
 
 void CudaBackend::render_frame(const Scene& scene, const CameraState& camera) {
     if (ctx_ == nullptr) return;
-    const sgx_uniforms u = sgx::pack_uniforms(scene, camera, width_, height_, frame_time_sec_);
+    const sgx_scene sc = scene_to_c(scene);
+    const sgx_camera cc = camera_to_c(camera);
+    sgx_uniforms u{};
+    sgx_pack_uniforms(&sc, &cc, width_, height_, frame_time_sec_, &u);
     sgx_render_opts o;
     if (have_opts_) o = opts_;
     else sgx_render_opts_default(&o);

@@ -1,9 +1,17 @@
 // singularity_gb300/csrc/cuda_backend.hpp
 //
 // C++20 CudaBackend over the C ABI: the same class, members and behaviour as
-// the reference's render/cuda/cuda_backend.hpp:17-46 behind the abstract
-// RenderBackend of render/include/render_backend.hpp:107-132, so a caller of
-// the reference (its cuda_cli) compiles against this header unchanged.
+// the reference's render/cuda/cuda_backend.hpp:17-46, implementing the
+// abstract RenderBackend of render/include/render_backend.hpp:107-132.
+//
+// The interface types (Scene, CameraState, ImageData, WindowHandle,
+// RenderConfig, RenderBackend) come from "render_backend.hpp" on the include
+// path, never from this header: the reference's own header when a caller of
+// the reference (its cuda_cli/main.cpp, which includes both headers) is
+// relinked against this library, or this library's declaration of the same
+// interface (csrc/render_api/) in its own build.  Put this directory before
+// the reference's render/cuda on the include path so "cuda_backend.hpp"
+// resolves here.
 //
 // Behaviour kept from the reference: initialize() allocates the frame and
 // returns false on failure; render_frame() is a no-op without a frame,
@@ -13,49 +21,12 @@
 #pragma once
 
 #include <cstdint>
-#include <functional>
-#include <memory>
 #include <vector>
 
+#include "render_backend.hpp"
 #include "sgx.h"
-#include "sgx_host.hpp"
 
 namespace singularity {
-
-using Scene = sgx::Scene;
-using CameraState = sgx::CameraState;
-using ImageData = sgx::ImageData;
-
-struct WindowHandle {
-    void* native_window{nullptr};
-    void* native_view{nullptr};
-    std::function<void*(void*)> vulkan_create_surface{};
-};
-
-struct RenderConfig {
-    std::uint32_t width{1280};
-    std::uint32_t height{720};
-    bool vsync_enabled{true};
-};
-
-class RenderBackend {
-public:
-    virtual ~RenderBackend() = default;
-    RenderBackend(const RenderBackend&) = delete;
-    RenderBackend& operator=(const RenderBackend&) = delete;
-    RenderBackend(RenderBackend&&) = delete;
-    RenderBackend& operator=(RenderBackend&&) = delete;
-
-    virtual bool initialize(WindowHandle window, RenderConfig config) = 0;
-    virtual void shutdown() = 0;
-    virtual void resize(std::uint32_t width, std::uint32_t height) = 0;
-    virtual void render_frame(const Scene& scene, const CameraState& camera) = 0;
-    virtual ImageData capture_frame() = 0;
-    virtual const char* name() const = 0;
-
-protected:
-    RenderBackend() = default;
-};
 
 class CudaBackend : public RenderBackend {
 public:

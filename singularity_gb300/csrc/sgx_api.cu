@@ -110,7 +110,31 @@ sgx_status check_opts(sgx_context* c, const sgx_render_opts& o) {
     }
     if (o.precision == SGX_PRECISION_MIXED && o.integrator == SGX_INTEGRATOR_FIXED)
         return fail(c, SGX_ERR_INVALID_ARGUMENT, "the mixed precision form applies to the adaptive integrator");
+    if (o.projection > 1u) return fail(c, SGX_ERR_INVALID_ARGUMENT, "projection must be 0 or 1");
+    if (o.slice_count > 1u && (o.slice_index >= o.slice_count || o.slice_count > 65536u || o.slice_band > 65536u))
+        return fail(c, SGX_ERR_INVALID_ARGUMENT, "slice_index must be below slice_count (<= 65536), slice_band <= 65536");
     return SGX_OK;
+}
+
+sgxk::SliceSpec slice_of(const sgx_render_opts& o) {
+    sgxk::SliceSpec sl;
+    if (o.slice_count > 1u) {
+        sl.count = o.slice_count;
+        sl.index = o.slice_index;
+        sl.band = o.slice_band == 0u ? SGX_SLICE_BAND_DEFAULT : o.slice_band;
+    }
+    return sl;
+}
+
+// The integrator options of a probe launch.
+sgxk::PassDesc probe_opts(const sgx_render_opts& o) {
+    sgxk::PassDesc p{};
+    p.tol = o.tolerance;
+    p.h_init_frac = o.h_init_frac;
+    p.h_max_frac = o.h_max_frac;
+    p.zone = o.fp64_zone;
+    p.project = o.projection;
+    return p;
 }
 
 std::uint32_t clamp_spp(std::uint32_t ss) { return ss < 1u ? 1u : (ss > 1024u ? 1024u : ss); }
@@ -125,7 +149,11 @@ sgx_status render_impl(sgx_context* c, const sgx_uniforms* u, const sgx_render_o
         return fail(c, SGX_ERR_INVALID_ARGUMENT, "progressive passes must continue from the previous pass");
     const std::uint32_t count =
         o.sample_count == 0 ? spp - begin : std::min<std::uint32_t>(o.sample_count, spp - begin);
-    const std::uint32_t npix = u->width * u->height;
+    const sgxk::SliceSpec slice = slice_of(o);
+    const std::uint32_t rows = slice.count > 1u ? sgxk::slice_rows(u->height, slice.band, slice.count, slice.index)
+                                                : u->height;
+    if (rows == 0u) return fail(c, SGX_ERR_INVALID_ARGUMENT, "the frame slice has no rows");
+    const std::uint32_t npix = u->width * rows;
 
     // Pass size under the workspace budget.
     std::size_t free_b = 0, total_b = 0;
@@ -156,7 +184,7 @@ sgx_status render_impl(sgx_context* c, const sgx_uniforms* u, const sgx_render_o
         const std::uint32_t n = std::min(S, count - done);
         const std::uint32_t s0 = begin + done;
         sgxk::ViewPlan plan;
-        if (!sgxk::plan_views(u, 1, s0, n, tw, th, plan))
+        if (!sgxk::plan_views(u, 1, s0, n, tw, th, plan, slice))
             return fail(c, SGX_ERR_INVALID_ARGUMENT, "invalid pass or tile shape");
         SGX_CUDA(c, cudaMemcpyAsync(c->d_words, plan.words, plan.word_count * 8, cudaMemcpyHostToDevice, st));
         sgxk::PassDesc pass{};
@@ -168,6 +196,7 @@ sgx_status render_impl(sgx_context* c, const sgx_uniforms* u, const sgx_render_o
         pass.h_init_frac = o.h_init_frac;
         pass.h_max_frac = o.h_max_frac;
         pass.zone = o.fp64_zone;
+        pass.project = o.projection;
         SGX_CUDA(c, cudaEventRecord(c->ev_begin, st));
         SGX_CUDA(c, cudaMemsetAsync(c->d_counters, 0, sizeof(sgxk::PassCounters), st));
         SGX_CUDA(c, cudaEventRecord(c->ev_trace0, st));
@@ -236,6 +265,7 @@ void sgx_render_opts_default(sgx_render_opts* o) {
     o->h_init_frac = 0.02f;
     o->h_max_frac = 0.1f;
     o->fp64_zone = 0.05f;
+    o->projection = 1u;
 }
 
 sgx_status sgx_create(int device, sgx_context** out) {
@@ -298,6 +328,8 @@ sgx_status sgx_render(sgx_context* c, const sgx_uniforms* u, const sgx_render_op
     if (s != SGX_OK) return s;
     const sgx_render_opts o = resolve_opts(opts);
     if ((s = check_opts(c, o)) != SGX_OK) return s;
+    if (o.slice_count > 1u)
+        return fail(c, SGX_ERR_INVALID_ARGUMENT, "a frame slice renders through sgx_render_device");
     cudaSetDevice(c->device);
     if ((s = ensure_size(c, u->width, u->height)) != SGX_OK) return s;
     return render_impl(c, u, o, c->d_image, o.format, c->stream);
@@ -391,14 +423,69 @@ sgx_status sgx_trace_samples(sgx_context* c, const sgx_uniforms* u, const sgx_re
     if (e == cudaSuccess) e = sgxk::launch_setup_views(c->d_u, 1, c->d_view, int(o.precision), c->stream);
     if (e == cudaSuccess)
         e = sgxk::launch_probe(c->d_view, int(u->metric_type), int(o.precision), int(o.integrator), int(o.rhs_form), n, d_gx,
-                               d_gy, d_s, d_hdr, d_steps, d_term, o.tolerance, o.h_init_frac, o.h_max_frac,
-                               o.fp64_zone, c->stream);
+                               d_gy, d_s, d_hdr, d_steps, d_term, probe_opts(o), c->stream);
     if (e == cudaSuccess && hdr3) e = cudaMemcpyAsync(hdr3, d_hdr, n * 12, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess && steps) e = cudaMemcpyAsync(steps, d_steps, n * 4, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess && term) e = cudaMemcpyAsync(term, d_term, n * 4, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     cudaFree(d);
     if (e != cudaSuccess) return cuda_fail(c, e, "sgx_trace_samples");
+    return SGX_OK;
+}
+
+uint32_t sgx_slice_rows(uint32_t height, uint32_t band, uint32_t count, uint32_t index) {
+    if (band == 0u) band = SGX_SLICE_BAND_DEFAULT;
+    if (count <= 1u) return index == 0u ? height : 0u;
+    if (index >= count) return 0u;
+    return sgxk::slice_rows(height, band, count, index);
+}
+
+uint32_t sgx_slice_row(uint32_t height, uint32_t band, uint32_t count, uint32_t index, uint32_t local) {
+    if (band == 0u) band = SGX_SLICE_BAND_DEFAULT;
+    if (local >= sgx_slice_rows(height, band, count, index)) return UINT32_MAX;
+    if (count <= 1u) return local;
+    return sgxk::slice_row(band, count, index, local);
+}
+
+sgx_status sgx_trace_invariants(sgx_context* c, const sgx_uniforms* u, const sgx_render_opts* opts, uint64_t n,
+                                const uint32_t* gx, const uint32_t* gy, const uint32_t* s, double* inv5,
+                                uint32_t* term) {
+    if (c == nullptr) return SGX_ERR_INVALID_ARGUMENT;
+    sgx_status st = check_uniforms(c, u);
+    if (st != SGX_OK) return st;
+    const sgx_render_opts o = resolve_opts(opts);
+    if ((st = check_opts(c, o)) != SGX_OK) return st;
+    if (o.integrator != SGX_INTEGRATOR_ADAPTIVE || u->metric_type != SGX_METRIC_KERR)
+        return fail(c, SGX_ERR_UNSUPPORTED, "constants of motion are reported for the error-controlled Kerr form");
+    if (n == 0) return SGX_OK;
+    if (gx == nullptr || gy == nullptr || s == nullptr || inv5 == nullptr)
+        return fail(c, SGX_ERR_INVALID_ARGUMENT, "NULL sample or output arrays");
+    for (uint64_t i = 0; i < n; ++i)
+        if (gx[i] >= u->width || gy[i] >= u->height) return fail(c, SGX_ERR_INVALID_ARGUMENT, "pixel out of range");
+    cudaSetDevice(c->device);
+    // Device copies: inputs (3 words per sample), then 5 doubles and a word per sample.
+    const std::size_t in_b = (n * 3 * sizeof(uint32_t) + 7) / 8 * 8;
+    const std::size_t out_b = n * 5 * sizeof(double) + n * sizeof(uint32_t);
+    void* d = nullptr;
+    SGX_CUDA(c, cudaMalloc(&d, in_b + out_b));
+    uint32_t* d_gx = static_cast<uint32_t*>(d);
+    uint32_t* d_gy = d_gx + n;
+    uint32_t* d_s = d_gy + n;
+    double* d_inv = reinterpret_cast<double*>(static_cast<unsigned char*>(d) + in_b);
+    uint32_t* d_term = reinterpret_cast<uint32_t*>(d_inv + 5 * n);
+    cudaError_t e = cudaMemcpyAsync(d_gx, gx, n * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_gy, gy, n * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_s, s, n * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_u, u, sizeof(sgx_uniforms), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = sgxk::launch_setup_views(c->d_u, 1, c->d_view, int(o.precision), c->stream);
+    if (e == cudaSuccess)
+        e = sgxk::launch_invariants(c->d_view, int(o.precision), int(o.rhs_form), n, d_gx, d_gy, d_s, d_inv, d_term,
+                                    probe_opts(o), c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(inv5, d_inv, n * 40, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && term) e = cudaMemcpyAsync(term, d_term, n * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(c, e, "sgx_trace_invariants");
     return SGX_OK;
 }
 

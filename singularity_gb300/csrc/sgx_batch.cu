@@ -67,6 +67,7 @@ cudaError_t enqueue(sgx_batch* b, const sgx_render_opts& o, const sgxk::ViewPlan
     pass.h_init_frac = o.h_init_frac;
     pass.h_max_frac = o.h_max_frac;
     pass.zone = o.fp64_zone;
+    pass.project = o.projection;
     cudaError_t e = cudaMemsetAsync(b->d_counters, 0, sizeof(sgxk::PassCounters), st);
     if (e == cudaSuccess) e = sgxk::launch_setup_views(b->d_u, b->n, b->d_views, int(o.precision), st);
     if (e == cudaSuccess)
@@ -131,6 +132,7 @@ sgx_status sgx_batch_create(sgx_context* c, const sgx_uniforms* views, uint32_t 
         return fail(c, SGX_ERR_UNSUPPORTED, "batch output format must be RGBA8 sRGB or RGBA32F");
     if (o.sample_begin != 0 || o.sample_count != 0)
         return fail(c, SGX_ERR_INVALID_ARGUMENT, "a batch renders every sample of every view");
+    if (o.slice_count > 1u) return fail(c, SGX_ERR_INVALID_ARGUMENT, "a batch renders whole views (no frame slices)");
     cudaSetDevice(c->device);
     sgx_batch* b = new sgx_batch();
     b->ctx = c;

@@ -808,6 +808,53 @@ template <class T> __device__ __forceinline__ T carter_Q(const View<T>& v, T E, 
     return pth * pth + v.cos_th * v.cos_th * (L * L / DM<T>::fmax_(v.s2_c, DLIT(1e-6)) - v.a2 * E * E);
 }
 
+// The same in FP64 from the mixed form's FP64 constants (the camera's cos and
+// sin of theta are the view's T values).
+template <class T> __device__ __forceinline__ double carter_Q_fp64(const View<T>& v, double E, double L, double pth) {
+    const double ct = double(v.cos_th), st = double(v.sin_th), a = double(v.a);
+    const double s2 = st * st;
+    return pth * pth + ct * ct * (L * L / (s2 > 1e-6 ? s2 : 1e-6) - a * a * E * E);
+}
+
+// p_theta put back onto the ray's Carter constant after an accepted step (a
+// projection method; Hairer, Lubich & Wanner, Geometric Numerical
+// Integration, IV.4): |p_theta| = sqrt(Theta), Theta = Q - c^2 (L^2 / s^2 -
+// a^2 E^2), s^2 guarded at 1e-10 as in the right-hand side, the sign of
+// p_theta kept; 0 where truncation has carried the state past a turning point
+// (Theta < 0).  FP32 takes one approximate reciprocal and square root (PTX
+// rcp.approx / sqrt.approx, within 2 ulp of the IEEE results).
+template <class T> __device__ __forceinline__ T project_pth(T pth, T s, T c, T Q, const KC<T>& k) {
+    const T s2 = DM<T>::fmax_(s * s, DLIT(1e-10));
+    const T th = Q - c * c * (k.L * k.L * DM<T>::rcp_fast(s2) - k.aE * k.aE);
+    T m;
+    if constexpr (std::is_same_v<T, float>) {
+        const float x = fmaxf(th, 0.0f);
+        asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(m) : "f"(x));
+    } else {
+        m = th > 0.0 ? sqrt(th) : 0.0;
+    }
+    return pth < DLIT(0.0) ? -m : m;
+}
+
+// Constants of motion of a final state, in FP64 (diagnostics): the Carter
+// constant with theta from (s, c) and 2H in the reference's grouping
+// (kerr_hamilton.h:37-60; the CPU oracle's kerr_two_H).
+template <class T>
+__device__ __forceinline__ void kerr_invariants_fp64(const View<T>& v, double E, double L, double r, double s,
+                                                     double c, double pr, double pth, double& Q, double& H2) {
+    const double n2 = s * s + c * c;
+    const double st2 = s * s / n2, ct2 = c * c / n2;
+    const double a = double(v.a), Mm = double(v.M);
+    Q = pth * pth + ct2 * (L * L / (st2 > 1e-300 ? st2 : 1e-300) - a * a * E * E);
+    const double safe_s2 = st2 < 1e-10 ? 1e-10 : st2;
+    const double r2 = r * r, a2 = a * a;
+    const double Sigma = r2 + a2 * ct2, Delta = r2 - 2.0 * Mm * r + a2;
+    const double A = (r2 + a2) * (r2 + a2) - a2 * Delta * st2;
+    const double SD = Sigma * Delta;
+    H2 = -A * E * E / SD + 4.0 * Mm * r * a * E * L / SD + (Delta - a2 * safe_s2) * L * L / (SD * safe_s2) +
+         Delta * pr * pr / Sigma + pth * pth / Sigma;
+}
+
 template <class T> struct KAttempt {
     KSC<T> y4, k4, k5;
     T h6;

@@ -40,9 +40,30 @@ struct ViewSet {
     std::uint32_t s0;      // first Halton sample of the pass (progressive single view); 0 for batches
     std::uint32_t tile_w;  // ray-id order: tiles of tile_w x tile_h pixels, samples innermost; 0 = rows
     std::uint32_t tile_h;
+    // frame slice of a single view (slice_count > 1): the pass traces the
+    // slice_h rows of slice slice_index (bands of slice_band rows dealt
+    // round-robin to slice_count slices); its records, pixels and output rows
+    // are the slice's, packed
+    std::uint32_t slice_count, slice_index, slice_band, slice_h;
     std::uint64_t total_rays;
     std::uint64_t total_pix;
 };
+
+// Rows of slice `index` of `count` in a frame of `height` rows (bands of
+// `band` rows dealt round-robin), and the frame row of its local row `l`.
+__host__ __device__ inline std::uint32_t slice_rows(std::uint32_t height, std::uint32_t band, std::uint32_t count,
+                                                    std::uint32_t index) {
+    const std::uint32_t bands = (height + band - 1u) / band;
+    if (index >= bands) return 0u;
+    const std::uint32_t mine = (bands - index + count - 1u) / count;  // bands index, index + count, ...
+    const std::uint32_t last = index + (mine - 1u) * count;           // the slice's last band
+    return (mine - 1u) * band + (height - last * band < band ? height - last * band : band);
+}
+__host__ __device__ inline std::uint32_t slice_row(std::uint32_t band, std::uint32_t count, std::uint32_t index,
+                                                   std::uint32_t l) {
+    const std::uint32_t b = l / band;
+    return (b * count + index) * band + (l - b * band);
+}
 
 // Steps between warp refills when the caller leaves it to the library: the
 // 4K Kerr pass runs 1.6 % faster at 32 than at 16 (64: within 1 %; 8: 4 % slower).
@@ -57,6 +78,7 @@ struct PassDesc {
     PassCounters* counters;
     // adaptive options
     float tol, h_init_frac, h_max_frac, zone;
+    std::uint32_t project;  // 1: p_theta projected onto the Carter constant after accepted steps
 };
 
 struct LaunchShape {
@@ -67,14 +89,21 @@ struct LaunchShape {
 // Host plan of a ViewSet: the layout block's contents (to copy to the device
 // as one array of 64-bit words) and the totals.  S_pass == 0 -> every view's
 // own samples per pixel.
+struct SliceSpec {
+    std::uint32_t count = 0, index = 0, band = 0;  // count <= 1: the whole frame
+};
+
 struct ViewPlan {
     std::uint32_t n = 0, max_S = 0, s0 = 0, tile_w = 0, tile_h = 0;
+    SliceSpec slice{};
+    std::uint32_t slice_h = 0;
     std::uint64_t total_rays = 0, total_pix = 0, total_recs = 0;
     std::uint64_t words[4 * kMaxLaunchViews + 2] = {};  // ray_off | rec_off | pix_off | S (packed 2 per word)
     std::size_t word_count = 0;
 };
+// A slice (slice.count > 1) applies to a single view only.
 bool plan_views(const sgx_uniforms* u, std::uint32_t n, std::uint32_t s0, std::uint32_t S_pass, std::uint32_t tile_w,
-                std::uint32_t tile_h, ViewPlan& plan);
+                std::uint32_t tile_h, ViewPlan& plan, SliceSpec slice = {});
 // Device ViewSet over a layout block that holds plan.words at d_words and
 // the views at d_views.
 ViewSet make_view_set(const ViewPlan& plan, const void* d_views, const std::uint64_t* d_words);
@@ -90,11 +119,19 @@ cudaError_t launch_setup_views(const sgx_uniforms* d_u, std::uint32_t n, void* d
 cudaError_t launch_trace(int metric, int precision, int integrator, int rhs_form, const PassDesc& pass,
                          LaunchShape shape, cudaStream_t st, const void* h_view = nullptr);
 
-// Per-sample probe (parity tests) of a single view: n samples, device arrays.
+// Per-sample probe (parity tests) of a single view: n samples, device arrays;
+// the integrator options come from opts (tol, h_init_frac, h_max_frac, zone,
+// project).
 cudaError_t launch_probe(const void* d_view, int metric, int precision, int integrator, int rhs_form,
                          std::uint64_t n, const std::uint32_t* gx, const std::uint32_t* gy, const std::uint32_t* s,
-                         float* hdr3, std::uint32_t* steps, std::uint32_t* term, float tol, float h_init_frac,
-                         float h_max_frac, float zone, cudaStream_t st);
+                         float* hdr3, std::uint32_t* steps, std::uint32_t* term, const PassDesc& opts,
+                         cudaStream_t st);
+
+// Constants of motion (E, L, Q0, Q_end, 2H_end; FP64, 5 per sample) of n
+// samples of the error-controlled Kerr form of a single view.
+cudaError_t launch_invariants(const void* d_view, int precision, int rhs_form, std::uint64_t n,
+                              const std::uint32_t* gx, const std::uint32_t* gy, const std::uint32_t* s, double* inv5,
+                              std::uint32_t* term, const PassDesc& pass, cudaStream_t st);
 
 // Shades a pass's hit records and adds them in sample order into acc (float4
 // per pixel, packed over views); when `finalize`, also writes every view's

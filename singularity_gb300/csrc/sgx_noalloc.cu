@@ -2,14 +2,14 @@
 //
 // sgx_render_noalloc: a render entry point that allocates nothing.
 //
-// Who needs it.  Some callers cannot call cudaMalloc (or let a library do it
-// for them): code that is issuing work while a stream is being captured into
-// a CUDA graph, where allocation calls are not permitted; host applications
-// whose device memory is owned entirely by their own pool or arena and that
-// forbid third-party allocations; and frame-paced callers that cannot afford
-// the device-wide synchronisation cudaFree implies.  The context-based entry
-// points (sgx_create / sgx_render / sgx_render_device) allocate their images
-// and per-sample buffers, so those callers cannot use them.
+// Who needs it.  Some callers of this library cannot call cudaMalloc, or let
+// a library call it for them: host applications (game engines, renderers
+// embedded as plug-ins) that reserve all of a GPU's memory for their own pool
+// or arena at start-up and forbid third-party allocations after it; and
+// frame-paced callers that cannot take the device-wide synchronisation that
+// cudaFree implies in the middle of a frame.  The context-based entry points
+// (sgx_create / sgx_render / sgx_render_device) allocate their images and
+// per-sample buffers, so those callers cannot use them.
 //
 // How.  The per-sample results, the per-pixel accumulator, the pass counters,
 // the uniform block and the per-view constants live in one file-scope device
@@ -19,10 +19,11 @@
 // it, so results are identical.
 //
 // Rules for callers:
-//   * A frame needs 16 * width * height * (spp + 1) bytes of scratch plus a
-//     4 KiB header (FP64: 16 * width * height * (2 * spp + 1)); larger requests
-//     are rejected with SGX_ERR_INVALID_ARGUMENT and a message saying so.  spp
-//     is the clamped samples per pixel.
+//   * A frame needs 4096 + align256(16 * width * height) + R * width * height *
+//     spp bytes of scratch (R = 16 for FP32, 32 for FP64; align256 rounds up
+//     to a multiple of 256); larger requests are rejected with
+//     SGX_ERR_INVALID_ARGUMENT and a message saying so.  spp is the clamped
+//     samples per pixel.
 //   * The first call on each device looks up the array's device address
 //     (cudaGetSymbolAddress) with that device current; make that first call
 //     before any stream capture begins.
@@ -120,6 +121,14 @@ extern "C" sgx_status sgx_render_noalloc(const sgx_uniforms* u, const sgx_render
         set_err(err, err_len, "sgx_render_noalloc: block_threads must be 0 or a multiple of 32 up to 256");
         return SGX_ERR_INVALID_ARGUMENT;
     }
+    if ((o.tile_w == 0) != (o.tile_h == 0) || o.tile_w > 4096 || o.tile_h > 4096) {
+        set_err(err, err_len, "sgx_render_noalloc: tile_w and tile_h must both be 0 or both in [1, 4096]");
+        return SGX_ERR_INVALID_ARGUMENT;
+    }
+    if (o.slice_count > 1u) {
+        set_err(err, err_len, "sgx_render_noalloc: renders whole frames only (no frame slices)");
+        return SGX_ERR_INVALID_ARGUMENT;
+    }
     const std::uint32_t spp = u->supersample < 1u ? 1u : (u->supersample > 1024u ? 1024u : u->supersample);
     if (o.sample_begin != 0 || (o.sample_count != 0 && o.sample_count != spp)) {
         set_err(err, err_len, "sgx_render_noalloc: renders whole frames only (sample_begin 0, all samples)");
@@ -127,12 +136,16 @@ extern "C" sgx_status sgx_render_noalloc(const sgx_uniforms* u, const sgx_render
     }
     const std::uint64_t npix = std::uint64_t(u->width) * u->height;
     const std::uint64_t rec = sgxk::record_bytes(int(o.precision));
-    const std::uint64_t need = kHeaderBytes + 16ull * npix + rec * npix * std::uint64_t(spp);
+    // the hit records start on a 256-byte boundary (an FP64 record is a
+    // 32-byte aligned type, and 16 * npix need not be a multiple of 32)
+    const std::uint64_t acc_bytes = (16ull * npix + 255ull) / 256ull * 256ull;
+    const std::uint64_t need = kHeaderBytes + acc_bytes + rec * npix * std::uint64_t(spp);
     if (need > SGX_NOALLOC_SCRATCH_BYTES) {
-        char buf[256];
+        char buf[320];
         std::snprintf(buf, sizeof(buf),
-                      "sgx_render_noalloc: frame needs %llu bytes of scratch (16*w*h + %llu*w*h*spp + 4096) but "
-                      "the fixed scratch holds %llu; use fewer pixels or samples, or the allocating entry points",
+                      "sgx_render_noalloc: frame needs %llu bytes of scratch (4096 + align256(16*w*h) + "
+                      "%llu*w*h*spp) but the fixed scratch holds %llu; use fewer pixels or samples, or the "
+                      "allocating entry points",
                       (unsigned long long)need, (unsigned long long)rec,
                       (unsigned long long)SGX_NOALLOC_SCRATCH_BYTES);
         set_err(err, err_len, buf);
@@ -154,11 +167,11 @@ extern "C" sgx_status sgx_render_noalloc(const sgx_uniforms* u, const sgx_render
     void* d_view = base + kViewOff;
     auto* d_words = reinterpret_cast<std::uint64_t*>(base + kWordsOff);
     auto* acc = reinterpret_cast<float4*>(base + kHeaderBytes);
-    void* results = acc + npix;
+    void* results = base + kHeaderBytes + acc_bytes;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
 
     sgxk::ViewPlan plan;
-    if (!sgxk::plan_views(u, 1, 0, spp, 0, 0, plan)) {
+    if (!sgxk::plan_views(u, 1, 0, spp, o.tile_w, o.tile_h, plan)) {
         set_err(err, err_len, "sgx_render_noalloc: invalid frame");
         return SGX_ERR_INVALID_ARGUMENT;
     }
@@ -171,6 +184,7 @@ extern "C" sgx_status sgx_render_noalloc(const sgx_uniforms* u, const sgx_render
     pass.h_init_frac = o.h_init_frac;
     pass.h_max_frac = o.h_max_frac;
     pass.zone = o.fp64_zone;
+    pass.project = o.projection;
     sgxk::LaunchShape shape{int(o.block_threads), int(o.blocks_per_sm)};
 
     e = cudaMemcpyAsync(d_u, u, sizeof(sgx_uniforms), cudaMemcpyHostToDevice, st);

@@ -222,6 +222,7 @@ template <class T, int FL> struct KerrAdaptive {
     static constexpr int kMinBlocksMulti = sizeof(T) == 4 ? 3 : 1;
     KSC<T> y, k1;  // theta carried as (sin theta, cos theta)
     KC<T> c;
+    T Q;           // Carter constant the projection holds p_theta to
     T h, r_c;
     T r_cap;  // early capture: inside min(r_c - 0.05 M, r_in) moving inward (0: never)
     T t0, t1, t2;
@@ -246,12 +247,15 @@ template <class T, int FL> struct KerrAdaptive {
             L = float(Ld);
             y.pr = float(prd);
             y.pth = float(pthd);
+            Q = float(carter_Q_fp64(v, Ed, Ld, pthd));
+        } else {
+            Q = carter_Q(v, E, L, y.pth);
         }
         // a photon from outside inside its spherical photon orbit radius r_c(xi) has no
         // radial turning point left (Teo 2003); inside r_in it cannot reach the disc
         r_c = photon_orbit_radius(v, L / E);
         r_cap = DLIT(0.0);
-        if (finite_(r_c) && carter_Q(v, E, L, y.pth) >= DLIT(0.0))
+        if (finite_(r_c) && carter_Q(v, E, L, y0.pth) >= DLIT(0.0))
             r_cap = DM<T>::fmin_(r_c - DLIT(0.05) * v.M, v.r_in);
         c = make_kc(v, E, L);
         h = T(pass.h_init_frac) * y.r;
@@ -319,6 +323,7 @@ template <class T, int FL> struct KerrAdaptive {
             }
             y = at.y4;
             renormalise(y);
+            if (pass.project) y.pth = project_pth(y.pth, y.s, y.c, Q, c);
             k1 = at.k5;
         }
         if (steps >= v.max_steps) {
@@ -507,10 +512,15 @@ __global__ void __launch_bounds__(256, ONE ? Ray::kMinBlocks : Ray::kMinBlocksMu
                         const std::uint32_t ty = tile / tiles_x;
                         const std::uint32_t wy = within / tw;
                         const std::uint32_t gx = (tile - ty * tiles_x) * tw + (within - wy * tw);
-                        const std::uint32_t gy = ty * th + wy;
-                        if (gx < v.width && gy < v.height) {
-                            s_rec[threadIdx.x] = m.rec_off[vid] + std::uint64_t(sl) * (std::uint64_t(v.width) * v.height) +
-                                                 std::uint64_t(gy) * v.width + gx;
+                        // a frame slice traces its own rows, numbered locally
+                        const bool sliced = vs.slice_count > 1u;
+                        const std::uint32_t vh = sliced ? vs.slice_h : v.height;
+                        const std::uint32_t gyl = ty * th + wy;
+                        if (gx < v.width && gyl < vh) {
+                            s_rec[threadIdx.x] = m.rec_off[vid] + std::uint64_t(sl) * (std::uint64_t(v.width) * vh) +
+                                                 std::uint64_t(gyl) * v.width + gx;
+                            const std::uint32_t gy =
+                                sliced ? slice_row(vs.slice_band, vs.slice_count, vs.slice_index, gyl) : gyl;
                             const T ox = v.spp == 1u ? DLIT(0.5) : m.off_x[sl];
                             const T oy = v.spp == 1u ? DLIT(0.5) : m.off_y[sl];
                             const CamDir<T> cd = camera_dir(v, gx, gy, ox, oy);
@@ -570,6 +580,59 @@ __global__ void __launch_bounds__(128) trace_probe(const View<T>* __restrict__ g
     if (term != nullptr) term[i] = ray.term;
 }
 
+// Constants of motion of single samples of the error-controlled form
+// (diagnostics): E, L_z and the Carter constant the ray started with, and the
+// Carter constant and 2H of its last state, all in FP64.  The starting values
+// are recomputed from the camera ray exactly as the policy's init computed
+// them (FP32 Q for the FP32 form, FP64 E, L, Q for the mixed form).
+template <class T, int FL>
+__global__ void __launch_bounds__(128) trace_invariants(const View<T>* __restrict__ g_view, std::uint64_t n,
+                                                        const std::uint32_t* gx, const std::uint32_t* gy,
+                                                        const std::uint32_t* s, double* inv5, std::uint32_t* term,
+                                                        PassDesc pass) {
+    using Ray = KerrAdaptive<T, FL>;
+    __shared__ View<T> v;
+    load_view(v, g_view);
+    __syncthreads();
+    const std::uint64_t i = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    T ox, oy;
+    sample_offset<T>(v.spp, s[i], ox, oy);
+    const CamDir<T> cd = camera_dir(v, gx[i], gy[i], ox, oy);
+    Ray ray;
+    if (ray.init(v, cd, pass)) {
+        while (!ray.step(v, pass)) {
+        }
+    }
+    double* o = inv5 + 5 * i;
+    if (ray.term == TERM_NO_ROOT) {
+        for (int k = 0; k < 5; ++k) o[k] = __longlong_as_double(0x7ff8000000000000ll);  // NaN
+    } else {
+        KS<T> y0;
+        T Ef, Lf;
+        kerr_init(v, cd, y0, Ef, Lf);
+        double E, L, Q0;
+        if constexpr (Ray::MIXED) {
+            double prd, pthd;
+            kerr_init_fp64_constants(v, cd, E, L, prd, pthd);
+            Q0 = carter_Q_fp64(v, E, L, pthd);
+        } else {
+            E = double(Ef);
+            L = double(Lf);
+            Q0 = double(carter_Q(v, Ef, Lf, y0.pth));
+        }
+        double Q, H2;
+        kerr_invariants_fp64(v, E, L, double(ray.y.r), double(ray.y.s), double(ray.y.c), double(ray.y.pr),
+                             double(ray.y.pth), Q, H2);
+        o[0] = E;
+        o[1] = L;
+        o[2] = Q0;
+        o[3] = Q;
+        o[4] = H2;
+    }
+    if (term != nullptr) term[i] = ray.term;
+}
+
 template <class T> __global__ void setup_views(const sgx_uniforms* u, std::uint32_t n, View<T>* out) {
     const std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = make_view<T>(u[i]);
@@ -615,7 +678,7 @@ __global__ void __launch_bounds__(256) accumulate_kernel(ViewSet vs, const Rec<T
     const std::uint32_t vid = vs.n == 1u ? 0u : find_view(m.pix_off, vs.n, p);
     const View<T>& v = m.views[vid];
     const std::uint64_t pix = p - m.pix_off[vid];
-    const std::uint64_t npix = std::uint64_t(v.width) * v.height;
+    const std::uint64_t npix = std::uint64_t(v.width) * (vs.slice_count > 1u ? vs.slice_h : v.height);
     const std::uint64_t base = m.rec_off[vid] + pix;
     const std::uint32_t S = m.S[vid];
     float4 sum = first ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : acc[p];
@@ -740,13 +803,20 @@ std::size_t format_bytes(std::uint32_t format) {
 }
 
 bool plan_views(const sgx_uniforms* u, std::uint32_t n, std::uint32_t s0, std::uint32_t S_pass, std::uint32_t tile_w,
-                std::uint32_t tile_h, ViewPlan& plan) {
+                std::uint32_t tile_h, ViewPlan& plan, SliceSpec slice) {
     if (n == 0 || n > kMaxLaunchViews || (tile_w != 0 && tile_h == 0)) return false;
+    const bool sliced = slice.count > 1u;
+    if (sliced && (n != 1u || slice.index >= slice.count || slice.band == 0u)) return false;
     plan = ViewPlan{};
     plan.n = n;
     plan.s0 = s0;
     plan.tile_w = tile_w;
     plan.tile_h = tile_h;
+    if (sliced) {
+        plan.slice = slice;
+        plan.slice_h = slice_rows(u[0].height, slice.band, slice.count, slice.index);
+        if (plan.slice_h == 0u) return false;
+    }
     std::uint64_t* ray_off = plan.words;
     std::uint64_t* rec_off = ray_off + (n + 1);
     std::uint64_t* pix_off = rec_off + n;
@@ -756,7 +826,7 @@ bool plan_views(const sgx_uniforms* u, std::uint32_t n, std::uint32_t s0, std::u
         const std::uint32_t spp = u[i].supersample < 1u ? 1u : (u[i].supersample > 1024u ? 1024u : u[i].supersample);
         const std::uint32_t Sv = S_pass == 0 ? spp : S_pass;
         if (Sv == 0 || Sv > kMaxPassSamplesHost) return false;
-        const std::uint64_t w = u[i].width, h = u[i].height;
+        const std::uint64_t w = u[i].width, h = sliced ? plan.slice_h : u[i].height;
         // tile_w == 0: whole rows of each view, no padding.
         const std::uint64_t tw = tile_w == 0 ? w : tile_w, th = tile_w == 0 ? 1 : tile_h;
         const std::uint64_t padded = ((w + tw - 1) / tw) * tw * (((h + th - 1) / th) * th);
@@ -791,6 +861,12 @@ ViewSet make_view_set(const ViewPlan& plan, const void* d_views, const std::uint
     vs.s0 = plan.s0;
     vs.tile_w = plan.tile_w;
     vs.tile_h = plan.tile_h;
+    if (plan.slice.count > 1u) {
+        vs.slice_count = plan.slice.count;
+        vs.slice_index = plan.slice.index;
+        vs.slice_band = plan.slice.band;
+        vs.slice_h = plan.slice_h;
+    }
     vs.total_rays = plan.total_rays;
     vs.total_pix = plan.total_pix;
     return vs;
@@ -818,17 +894,43 @@ cudaError_t launch_trace(int metric, int precision, int integrator, int rhs_form
 
 cudaError_t launch_probe(const void* d_view, int metric, int precision, int integrator, int rhs_form,
                          std::uint64_t n, const std::uint32_t* gx, const std::uint32_t* gy, const std::uint32_t* s,
-                         float* hdr3, std::uint32_t* steps, std::uint32_t* term, float tol, float h_init_frac,
-                         float h_max_frac, float zone, cudaStream_t st) {
+                         float* hdr3, std::uint32_t* steps, std::uint32_t* term, const PassDesc& opts,
+                         cudaStream_t st) {
     PassDesc pass{};
-    pass.tol = tol;
-    pass.h_init_frac = h_init_frac;
-    pass.h_max_frac = h_max_frac;
-    pass.zone = zone;
+    pass.tol = opts.tol;
+    pass.h_init_frac = opts.h_init_frac;
+    pass.h_max_frac = opts.h_max_frac;
+    pass.zone = opts.zone;
+    pass.project = opts.project;
     return dispatch(metric, precision, integrator, rhs_form,
                     [&]<class T, template <class, int> class Policy, int FL>() {
                         return run_probe<T, Policy, FL>(d_view, n, gx, gy, s, hdr3, steps, term, pass, st);
                     });
+}
+
+cudaError_t launch_invariants(const void* d_view, int precision, int rhs_form, std::uint64_t n,
+                              const std::uint32_t* gx, const std::uint32_t* gy, const std::uint32_t* s, double* inv5,
+                              std::uint32_t* term, const PassDesc& pass, cudaStream_t st) {
+    const unsigned threads = 128;
+    const std::uint64_t blocks = (n + threads - 1) / threads;
+    if (blocks == 0) return cudaSuccess;
+    const bool ref = rhs_form == 1;
+    const unsigned b = unsigned(blocks);
+    if (precision == SGX_PRECISION_FP64) {
+        const auto* vw = static_cast<const View<double>*>(d_view);
+        if (ref) trace_invariants<double, 0><<<b, threads, 0, st>>>(vw, n, gx, gy, s, inv5, term, pass);
+        else trace_invariants<double, FL_FAST><<<b, threads, 0, st>>>(vw, n, gx, gy, s, inv5, term, pass);
+    } else {
+        const auto* vw = static_cast<const View<float>*>(d_view);
+        if (precision == SGX_PRECISION_MIXED) {
+            if (ref) trace_invariants<float, FL_MIXED><<<b, threads, 0, st>>>(vw, n, gx, gy, s, inv5, term, pass);
+            else trace_invariants<float, FL_FAST | FL_MIXED><<<b, threads, 0, st>>>(vw, n, gx, gy, s, inv5, term, pass);
+        } else {
+            if (ref) trace_invariants<float, 0><<<b, threads, 0, st>>>(vw, n, gx, gy, s, inv5, term, pass);
+            else trace_invariants<float, FL_FAST><<<b, threads, 0, st>>>(vw, n, gx, gy, s, inv5, term, pass);
+        }
+    }
+    return cudaGetLastError();
 }
 
 cudaError_t launch_accumulate(int precision, const ViewSet& vs, const void* results, float4* acc, bool first,

@@ -1,8 +1,9 @@
 """Generate the committed golden fixtures from the reference tree.
 
-Run here, where the reference sources are (default /root/reference, or
-$SGX_REFERENCE_ROOT).  Nothing at test time reads the reference tree; the
-tests read only the files this script writes:
+Run where a full reference checkout is (oracle.pyoracle.reference_checkout():
+$SGX_REFERENCE_ROOT, else the build environment's checkout).  Nothing at test
+time reads the reference tree; the tests read only the files this script
+writes:
 
 * ``reference_cuda_goldens.npz`` — the reference's own CUDA golden images
   (verification/golden/cuda/{schw,kerr_a05,kerr_a094}.png, 256x256 RGBA8, made
@@ -31,7 +32,15 @@ HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent.parent
 sys.path.insert(0, str(ROOT))
 
-REF = Path(os.environ.get("SGX_REFERENCE_ROOT", "/root/reference"))
+def _checkout() -> Path:
+    from oracle import pyoracle
+    root = pyoracle.reference_checkout()
+    if root is None:
+        raise SystemExit("no reference checkout: set SGX_REFERENCE_ROOT")
+    return root
+
+
+REF = _checkout()
 
 
 def decode_png_rgba8(path: Path) -> np.ndarray:

@@ -42,10 +42,13 @@ def test_struct_layouts(sgx):
             "disc_turbulence": 156}
     for k, v in offs.items():
         assert getattr(N.Uniforms, k).offset == v, k
-    assert C.sizeof(N.RenderOpts) == 64
+    assert C.sizeof(N.RenderOpts) == 80
+    assert N.RenderOpts.projection.offset == 64 and N.RenderOpts.slice_band.offset == 76
     o = sgx.default_opts()
-    assert o.struct_size == 64 and o.precision == 0 and o.integrator == 0 and o.format == 0
+    assert o.struct_size == 80 and o.precision == 0 and o.integrator == 0 and o.format == 0
     assert abs(o.tolerance - 1e-6) < 1e-12 and o.sample_count == 0
+    # the projection belongs to the (opt-in) error-controlled integrator; no frame slice
+    assert o.projection == 1 and o.slice_count == 0 and o.slice_index == 0 and o.slice_band == 0
 
 
 def test_host_helpers_without_gpu(sgx):

@@ -179,3 +179,42 @@ def test_cli_rhs_form(cli, tmp_path, sgx, renderer):
     np.testing.assert_array_equal(img, renderer.render_image(u, sgx.default_opts(rhs_form=2)))
     f0 = renderer.render_image(u, sgx.default_opts())
     assert (np.abs(img.astype(int) - f0.astype(int)).max(axis=-1) <= 1).mean() >= 0.99
+
+
+SCENE_WITH_CAMERA_AND_STEPS = ("mass = 1.0\nspin = 0.9\ndisc_r_inner = 2.5\ndisc_r_outer = 25.0\n"
+                               "camera_distance = 22.0\ncamera_elevation = 0.4\ncamera_fov_deg = 45.0\n"
+                               "h_step = 0.25\nmax_steps = 900\n")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("use_camera,use_integrator", [(False, False), (True, False), (False, True), (True, True)])
+def test_cli_scene_opt_ins(cli, sgx, renderer, tmp_path, use_camera, use_integrator):
+    """--use-scene-camera / --use-scene-integrator (extensions, off by default):
+    the .scene file's camera_distance, camera_elevation, camera_fov_deg and
+    h_step, max_steps keys reach the render only when asked for; by default
+    they are ignored as the reference's cuda_cli ignores them
+    (cuda_cli/main.cpp:209-217) and the CLI's default camera (30 M, 0.15 rad,
+    60 deg) and the backend's step (0.4, 2500 steps) apply.  The PNG equals
+    the library render of the uniforms those choices imply."""
+    scene = tmp_path / "s.scene"
+    scene.write_text(SCENE_WITH_CAMERA_AND_STEPS)
+    args = ["--output", tmp_path / "o.png", "--res", "96x64", "--scene", scene]
+    if use_camera:
+        args.append("--use-scene-camera")
+    if use_integrator:
+        args.append("--use-scene-integrator")
+    r = run(cli, *args)
+    assert r.returncode == 0, r.stderr
+    img = read_png(tmp_path / "o.png")
+    sc = sgx.Scene(spin_a_over_M=0.9, disc_inner_M=2.5, disc_outer_M=25.0,
+                   h_step=0.25 if use_integrator else 0.0, max_steps=900 if use_integrator else 0)
+    cam = (sgx.build_orbital_camera(22.0, 0.4, 0.0, 45.0) if use_camera
+           else sgx.build_orbital_camera(30.0, 0.15, 0.0, 60.0))
+    u = sgx.pack_uniforms(sc, cam, 96, 64)
+    assert abs(u.h_step - (0.25 if use_integrator else 0.4)) < 1e-7
+    assert u.max_steps == (900 if use_integrator else 2500)
+    np.testing.assert_array_equal(img, renderer.render_image(u))
+    if use_camera or use_integrator:
+        plain = run(cli, "--output", tmp_path / "p.png", "--res", "96x64", "--scene", scene)
+        assert plain.returncode == 0
+        assert not np.array_equal(read_png(tmp_path / "p.png"), img)

@@ -122,3 +122,76 @@ def test_adaptive_rejects_bad_options(renderer, sgx):
     o = sgx.default_opts(precision=1)  # mixed form needs the adaptive integrator
     with pytest.raises(sgx.SgxError):
         renderer.render(u, o)
+
+
+def _seeded_pixels(u, n_pix=4096, spp_used=16):
+    """The 4096 pixels of numpy.random.default_rng(0).choice(W*H, 4096,
+    replace=False), each with its first `spp_used` samples."""
+    rng = np.random.default_rng(0)
+    pix = rng.choice(u.width * u.height, n_pix, replace=False).astype(np.uint32)
+    gx = np.repeat(pix % u.width, spp_used).astype(np.uint32)
+    gy = np.repeat(pix // u.width, spp_used).astype(np.uint32)
+    s = np.tile(np.arange(spp_used, dtype=np.uint32), n_pix)
+    return gx, gy, s
+
+
+@pytest.mark.parametrize("prec", ["f32", "mixed", "f64"])
+def test_carter_drift_on_the_gpu(renderer, oracle, sgx, prec):
+    """Relative drift of Carter's constant, |Q_end - Q0| / (|Q0| + L^2 + a^2 E^2),
+    of the rays the GPU traced in the 4K Kerr a = 0.94 workload (the seeded
+    4096 pixels x 16 samples): <= 1e-6 at the 99th percentile and at the
+    maximum, with p_theta projected back onto Q after each accepted step
+    (the default).  Without the projection the integrator's own drift
+    exceeds 1e-6 in the tail, as the CPU oracle of the same integrator shows;
+    E, L_z and Q0 equal the oracle's."""
+    u = sgx.workloads.kerr_4k_256spp()
+    gx, gy, s = _seeded_pixels(u)
+    inv, term = renderer.trace_invariants(u, gx, gy, s, _opts(sgx, prec))
+    dq = sgx.carter_drift(inv, u.spin_a)
+    assert dq.size >= 0.99 * gx.size
+    p50, p99, mx = np.median(dq), np.percentile(dq, 99), dq.max()
+    h2 = np.abs(inv[:, 4]) / inv[:, 0] ** 2
+    print(f"{prec}: Carter drift median {p50:.2e} p99 {p99:.2e} max {mx:.2e}; "
+          f"|2H|/E^2 median {np.nanmedian(h2):.2e} p99 {np.nanpercentile(h2, 99):.2e}")
+    assert p99 <= 1e-6 and mx <= 1e-6
+    # the oracle of the same integrator: the same constants at launch
+    o_prec = "f64" if prec == "f64" else "f32"
+    n = 8192
+    _, _, o_term, diag = oracle.trace(u, gx[:n], gy[:n], s[:n], precision=o_prec,
+                                      adaptive=_oracle_opts(oracle, prec), diag=True)
+    E = np.array([d.E for d in diag])
+    L = np.array([d.L for d in diag])
+    Q0 = np.array([d.Q0 for d in diag])
+    ok = o_term != 5
+    np.testing.assert_allclose(inv[:n, 0][ok], E[ok], rtol=2e-6)
+    np.testing.assert_allclose(inv[:n, 1][ok], L[ok], rtol=2e-6, atol=2e-6)
+    norm = np.abs(Q0) + L * L + (u.spin_a * E) ** 2
+    assert np.max(np.abs(inv[:n, 2] - Q0)[ok] / norm[ok]) <= 2e-6
+    # projection off: the plain integrator's tail drift, as in the oracle
+    o = _opts(sgx, prec)
+    o.projection = 0
+    inv0, _ = renderer.trace_invariants(u, gx, gy, s, o)
+    dq0 = sgx.carter_drift(inv0, u.spin_a)
+    _, _, _, d0 = oracle.trace(u, gx, gy, s, precision=o_prec,
+                               adaptive=oracle.adaptive_opts(mixed=(prec == "mixed"), projection=False), diag=True)
+    dq0_cpu = np.array([abs(d.Q_end - d.Q0) / d.norm_Q for d in d0])
+    print(f"{prec} no projection: GPU p99 {np.percentile(dq0, 99):.2e}, oracle p99 "
+          f"{np.nanpercentile(dq0_cpu, 99):.2e}")
+    assert np.percentile(dq0, 99) > 1e-6
+    assert 0.5 <= np.percentile(dq0, 99) / np.nanpercentile(dq0_cpu, 99) <= 2.0
+
+
+def test_projection_keeps_the_image(renderer, oracle, sgx):
+    """The projection moves p_theta by the integrator's truncation error only:
+    the frame with it and without it agree to the parity bar, and both
+    match the FP64 oracle to <= 1e-3 mean per-channel error."""
+    N = sgx._native
+    u = _scene(sgx, 96, 54, spp=4)
+    on = renderer.render_image(u, _opts(sgx, "mixed"), fmt=N.FORMAT_RGBA32F)[..., :3].astype(np.float64)
+    o = _opts(sgx, "mixed")
+    o.projection = 0
+    off = renderer.render_image(u, o, fmt=N.FORMAT_RGBA32F)[..., :3].astype(np.float64)
+    _, ldr64 = oracle.render(u, "f64", adaptive=oracle.adaptive_opts())
+    print(f"mean |on - off| {np.abs(on - off).mean():.2e}, on vs fp64 oracle {np.abs(on - ldr64).mean():.2e}")
+    assert np.abs(on - off).mean() <= 1e-3
+    assert np.abs(on - ldr64).mean() <= 1e-3 and np.abs(off - ldr64).mean() <= 1e-3

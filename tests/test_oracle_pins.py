@@ -132,3 +132,26 @@ def test_isco_known_answers(sgx):
     assert sgx.kerr_isco_prograde(1.0, 0.94) == pytest.approx(2.023593, abs=2e-5)
     assert sgx.kerr_isco_prograde(1.0, 0.7) == pytest.approx(3.393129, abs=2e-5)
     assert sgx.kerr_isco_prograde(2.0, 0.0) == pytest.approx(12.0, abs=1e-4)
+
+
+def test_reference_arm_uniforms_equal_the_product_packing(sgx, oracle):
+    """The reference arm of bench.py builds its uniform block with the
+    reference's own orbital camera, ISCO and Scene defaults and the harness's
+    restatement of pack_uniforms_cuda (render/cuda/cuda_backend.cu:45-101), no
+    product code; it is byte-identical to the product's sgx_pack_uniforms for
+    the benchmark scene and for the reference's default scene."""
+    import ctypes as C
+    if not oracle.ref_available():
+        pytest.skip("the host build of the reference kernel is not present")
+    ref = oracle.ref_headline_uniforms(3840, 2160, 256, 7.0 / 30.0)
+    isco = sgx.kerr_isco_prograde(1.0, 0.94)
+    assert oracle.ref_isco_prograde(1.0, 0.94) == isco
+    prod = sgx.pack_uniforms(sgx.Scene(spin_a_over_M=0.94, disc_inner_M=isco, disc_outer_M=30.0,
+                                       disc_peak_T_K=1e4, render_supersample=256),
+                             sgx.build_orbital_camera(40.0, 0.261799, 0.0, 30.0), 3840, 2160, 7.0 / 30.0)
+    assert bytes(C.string_at(C.byref(ref), 160)) == prod.to_bytes()
+    cam = oracle.ref_orbital_camera(30.0, 0.15, 0.0, 60.0)
+    for w, h in ((256, 256), (1280, 720)):
+        ref = oracle.ref_pack_uniforms(oracle.ref_scene(), cam, w, h)
+        prod = sgx.pack_uniforms(sgx.Scene(), sgx.build_orbital_camera(30.0, 0.15, 0.0, 60.0), w, h)
+        assert bytes(C.string_at(C.byref(ref), 160)) == prod.to_bytes()

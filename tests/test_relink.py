@@ -1,0 +1,84 @@
+"""The drop-in relink: the reference's own, unmodified cuda_cli/main.cpp
+compiled against this library's CudaBackend shim
+(singularity_gb300/csrc/cuda_backend.hpp, which takes Scene, CameraState,
+ImageData, WindowHandle, RenderConfig and RenderBackend from the reference's
+render/include/render_backend.hpp) and linked with libsgx.so
+(`make -C oracle relink`, oracle/pyoracle.py build_relink).
+
+CPU: it compiles and links with no source change, binds libsgx.so, and
+behaves as the reference CLI does without a GPU.  GPU: on the reference's
+three golden commands its PNG equals singularity_cuda_cli's.
+"""
+
+from __future__ import annotations
+
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from imgmetrics import read_png
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+@pytest.fixture(scope="session")
+def relinked(sgx, oracle):
+    p = oracle.build_relink()
+    if p is None:
+        pytest.skip("no reference sources (checkout or oracle/_ref/src snapshot) on this machine")
+    return p
+
+
+def run(exe, *args, timeout=120):
+    return subprocess.run([str(exe), *map(str, args)], capture_output=True, text=True, timeout=timeout)
+
+
+def test_reference_cli_relinks_against_the_shim(relinked):
+    # the executable binds this library, not the reference's kernel
+    maps = subprocess.run(["ldd", str(relinked)], capture_output=True, text=True).stdout
+    assert "libsgx.so" in maps
+    syms = subprocess.run(["nm", "-C", str(relinked)], capture_output=True, text=True).stdout
+    assert "singularity_geodesic_kernel" not in syms
+    assert "singularity::CudaBackend::render_frame" in syms
+    r = run(relinked, "--help")
+    assert r.returncode == 0 and "--samples-per-pixel" in r.stdout
+    r = run(relinked, "--bogus")
+    assert r.returncode == 2 and "unknown argument: --bogus" in r.stderr
+
+
+def test_relinked_cli_without_gpu(relinked, tmp_path):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    r = run(relinked, "--res", "8x8", "--output", tmp_path / "x.png")
+    assert r.returncode == 1 and "backend initialize failed" in r.stderr
+
+
+GOLDEN_SCENES = {
+    "schw": None,
+    "kerr_a05": "mass = 1.0\nspin = 0.5\ndisc_r_inner = 4.0\ndisc_r_outer = 30.0\n",
+    "kerr_a094": "mass = 1.0\nspin = 0.94\ndisc_r_inner = 1.7\ndisc_r_outer = 30.0\ndisc_doppler_on = 1\n"
+                 "disc_redshift_on = 1\n",
+}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", list(GOLDEN_SCENES))
+def test_relinked_cli_png_equals_ours(relinked, tmp_path, name):
+    """verification/test_cuda_goldens.py's commands (`--res 256x256 [--scene
+    scenes/<name>.scene]`) through the relinked reference CLI and through
+    singularity_cuda_cli: the same pixels."""
+    ours = ROOT / "singularity_gb300" / "_build" / "singularity_cuda_cli"
+    args = ["--res", "256x256"]
+    if GOLDEN_SCENES[name] is not None:
+        scene = tmp_path / f"{name}.scene"
+        scene.write_text(GOLDEN_SCENES[name])
+        args += ["--scene", scene]
+    a = run(relinked, *args, "--output", tmp_path / "ref.png")
+    b = run(ours, *args, "--output", tmp_path / "ours.png")
+    assert a.returncode == 0, a.stderr
+    assert b.returncode == 0, b.stderr
+    assert "(256x256, CUDA)" in a.stdout
+    np.testing.assert_array_equal(read_png(tmp_path / "ref.png"), read_png(tmp_path / "ours.png"))
