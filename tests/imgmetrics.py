@@ -100,5 +100,37 @@ def read_png(path) -> np.ndarray:
         pos += 12 + ln
     raw = np.frombuffer(zlib.decompress(idat), dtype=np.uint8).reshape(h, w * ch + 1)
     filt = raw[:, 0]
-    assert np.all(filt == 0), "only filter type 0 is supported here"
-    return raw[:, 1:].reshape(h, w, ch).copy()
+    if np.all(filt == 0):
+        return raw[:, 1:].reshape(h, w, ch).copy()
+    # the five PNG row filters (None, Sub, Up, Average, Paeth; PNG spec 9.2),
+    # as stb_image_write (the reference CLI's writer) uses them
+    out = np.zeros((h, w * ch), dtype=np.uint8)
+    prev = np.zeros(w * ch, dtype=np.int32)
+    for y in range(h):
+        line = raw[y, 1:].astype(np.int32)
+        f = int(filt[y])
+        if f == 0:
+            cur = line
+        elif f == 2:
+            cur = (line + prev) & 255
+        else:
+            cur = np.zeros(w * ch, dtype=np.int32)
+            ln, pv = line.tolist(), prev.tolist()
+            cl = [0] * (w * ch)
+            for x in range(w * ch):
+                a = cl[x - ch] if x >= ch else 0
+                b = pv[x]
+                c = pv[x - ch] if x >= ch else 0
+                if f == 1:
+                    pred = a
+                elif f == 3:
+                    pred = (a + b) >> 1
+                else:
+                    p = a + b - c
+                    pa, pb, pc = abs(p - a), abs(p - b), abs(p - c)
+                    pred = a if (pa <= pb and pa <= pc) else (b if pb <= pc else c)
+                cl[x] = (ln[x] + pred) & 255
+            cur = np.array(cl, dtype=np.int32)
+        out[y] = cur
+        prev = cur
+    return out.reshape(h, w, ch)

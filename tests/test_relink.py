@@ -82,3 +82,40 @@ def test_relinked_cli_png_equals_ours(relinked, tmp_path, name):
     assert b.returncode == 0, b.stderr
     assert "(256x256, CUDA)" in a.stdout
     np.testing.assert_array_equal(read_png(tmp_path / "ref.png"), read_png(tmp_path / "ours.png"))
+
+
+def test_png_reader_handles_every_row_filter(tmp_path):
+    """The test-side PNG reader decodes all five row filters (the reference
+    CLI's stb_image_write picks one per row)."""
+    import struct
+    import zlib
+    rng = np.random.default_rng(0)
+    img = rng.integers(0, 256, (5, 7, 4), dtype=np.uint8)
+    rows = img.reshape(5, 28).astype(np.int32)
+    raw = b""
+    prev = np.zeros(28, dtype=np.int32)
+    for y, f in enumerate((0, 1, 2, 3, 4)):
+        cur = rows[y]
+        left = np.concatenate([np.zeros(4, np.int32), cur[:-4]])
+        upleft = np.concatenate([np.zeros(4, np.int32), prev[:-4]])
+        if f == 0:
+            enc = cur
+        elif f == 1:
+            enc = cur - left
+        elif f == 2:
+            enc = cur - prev
+        elif f == 3:
+            enc = cur - ((left + prev) >> 1)
+        else:
+            p = left + prev - upleft
+            pa, pb, pc = np.abs(p - left), np.abs(p - prev), np.abs(p - upleft)
+            enc = cur - np.where((pa <= pb) & (pa <= pc), left, np.where(pb <= pc, prev, upleft))
+        raw += bytes([f]) + (enc & 255).astype(np.uint8).tobytes()
+        prev = cur
+
+    def chunk(t, b):
+        return struct.pack(">I", len(b)) + t + b + struct.pack(">I", zlib.crc32(t + b) & 0xFFFFFFFF)
+    path = tmp_path / "f.png"
+    path.write_bytes(b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", 7, 5, 8, 6, 0, 0, 0))
+                     + chunk(b"IDAT", zlib.compress(raw)) + chunk(b"IEND", b""))
+    np.testing.assert_array_equal(read_png(path), img)
