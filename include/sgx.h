@@ -85,8 +85,12 @@ typedef struct sgx_render_opts {
                                     integrator always carries them, so there 2 equals 0) */
     uint32_t tile_w;         /* ray order: tiles of tile_w x tile_h pixels, samples innermost;  */
     uint32_t tile_h;         /*   0 = whole rows (tile_w = width, tile_h = 1)                  */
-    uint32_t projection;     /* adaptive: 1 = after every accepted step p_theta is projected
-                                back onto the ray's Carter constant (default), 0 = off */
+    uint32_t projection;     /* adaptive: after every accepted step p_theta is projected back
+                                onto the ray's Carter constant; renders always do (1, the
+                                default); 0 turns it off in sgx_trace_samples and
+                                sgx_trace_invariants only (a diagnostic of the plain
+                                integrator's drift); a render given 0 returns
+                                SGX_ERR_UNSUPPORTED */
     uint32_t slice_count;    /* frame split (one frame over several GPUs): the rows are dealt in  */
     uint32_t slice_index;    /*   bands of slice_band rows, band b to slice b % slice_count; the  */
     uint32_t slice_band;     /*   render traces slice slice_index only and writes its rows packed

@@ -119,16 +119,16 @@ template <class T> inline T abs_(T x) { return x < OLIT(0.0) ? -x : x; }
 // (a projection method, Hairer, Lubich & Wanner, Geometric Numerical
 // Integration, IV.4): |p_theta| = sqrt(Theta), Theta = Q - c^2 (L^2 / s^2 -
 // a^2 E^2) with s^2 guarded at 1e-10 as in the right-hand side, the sign of
-// p_theta kept; p_theta = 0 where truncation has carried the state past a
-// turning point (Theta < 0).  Q and L are exact constants of the flow, so
-// this removes the integrator's drift off the level set Q = Q0 without
-// touching r, theta, phi or p_r.
+// p_theta kept (copysign); p_theta = +-0 where truncation has carried the
+// state past a turning point (Theta < 0).  Q and L are exact constants of
+// the flow, so this removes the integrator's drift off the level set Q = Q0
+// without touching r, theta, phi or p_r.
 template <class T> inline T project_p_theta(T pth, T s, T c, T Q, T L2, T a2E2) {
     const T s2 = s * s;
     const T safe = s2 < OLIT(1e-10) ? OLIT(1e-10) : s2;
     const T th = Q - c * c * (L2 / safe - a2E2);
     const T m = th > OLIT(0.0) ? M<T>::sqrt(th) : OLIT(0.0);
-    return pth < OLIT(0.0) ? -m : m;
+    return M<T>::copysign(m, pth);
 }
 
 // State of the error-controlled form: theta carried as (sin theta, cos theta).

@@ -76,6 +76,7 @@ template <> struct M<float> {
     static float log(float x) { return ::logf(x); }
     static float fmin(float a, float b) { return ::fminf(a, b); }
     static float fmax(float a, float b) { return ::fmaxf(a, b); }
+    static float copysign(float m, float s) { return std::copysign(m, s); }
     static bool isfinite(float x) { return std::isfinite(x); }
     static float lit(float f, double) { return f; }
 };
@@ -90,6 +91,7 @@ template <> struct M<double> {
     static double log(double x) { return std::log(x); }
     static double fmin(double a, double b) { return std::fmin(a, b); }
     static double fmax(double a, double b) { return std::fmax(a, b); }
+    static double copysign(double m, double s) { return std::copysign(m, s); }
     static bool isfinite(double x) { return std::isfinite(x); }
     static double lit(float, double d) { return d; }
 };
@@ -104,6 +106,7 @@ template <> struct M<Counted> {
     static C log(C x) { ++g_ops; return C(::logf(x.v)); }
     static C fmin(C a, C b) { ++g_ops; return C(::fminf(a.v, b.v)); }
     static C fmax(C a, C b) { ++g_ops; return C(::fmaxf(a.v, b.v)); }
+    static C copysign(C m, C s) { return C(std::copysign(m.v, s.v)); }  // a sign transfer, no arithmetic
     static bool isfinite(C x) { return std::isfinite(x.v); }
     static C lit(float f, double) { return C(f); }
 };

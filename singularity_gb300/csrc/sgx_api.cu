@@ -111,6 +111,15 @@ sgx_status check_opts(sgx_context* c, const sgx_render_opts& o) {
     if (o.precision == SGX_PRECISION_MIXED && o.integrator == SGX_INTEGRATOR_FIXED)
         return fail(c, SGX_ERR_INVALID_ARGUMENT, "the mixed precision form applies to the adaptive integrator");
     if (o.projection > 1u) return fail(c, SGX_ERR_INVALID_ARGUMENT, "projection must be 0 or 1");
+    return SGX_OK;
+}
+
+// Renders (and batches) always project; turning the projection off is a
+// diagnostic of the two probes.
+sgx_status check_render_projection(sgx_context* c, const sgx_render_opts& o) {
+    if (o.integrator == SGX_INTEGRATOR_ADAPTIVE && o.projection == 0u)
+        return fail(c, SGX_ERR_UNSUPPORTED,
+                    "projection = 0 applies to sgx_trace_samples and sgx_trace_invariants; renders always project");
     if (o.slice_count > 1u && (o.slice_index >= o.slice_count || o.slice_count > 65536u || o.slice_band > 65536u))
         return fail(c, SGX_ERR_INVALID_ARGUMENT, "slice_index must be below slice_count (<= 65536), slice_band <= 65536");
     return SGX_OK;
@@ -235,7 +244,8 @@ sgx_status render_impl(sgx_context* c, const sgx_uniforms* u, const sgx_render_o
 
 sgx_status sgx_internal::resolve_and_check(sgx_context* ctx, const sgx_render_opts* in, sgx_render_opts& out) {
     out = resolve_opts(in);
-    return check_opts(ctx, out);
+    const sgx_status s = check_opts(ctx, out);
+    return s != SGX_OK ? s : check_render_projection(ctx, out);
 }
 
 extern "C" {
@@ -328,6 +338,7 @@ sgx_status sgx_render(sgx_context* c, const sgx_uniforms* u, const sgx_render_op
     if (s != SGX_OK) return s;
     const sgx_render_opts o = resolve_opts(opts);
     if ((s = check_opts(c, o)) != SGX_OK) return s;
+    if ((s = check_render_projection(c, o)) != SGX_OK) return s;
     if (o.slice_count > 1u)
         return fail(c, SGX_ERR_INVALID_ARGUMENT, "a frame slice renders through sgx_render_device");
     cudaSetDevice(c->device);
@@ -344,6 +355,7 @@ sgx_status sgx_render_device(sgx_context* c, const sgx_uniforms* u, const sgx_re
     sgx_render_opts o = resolve_opts(opts);
     o.format = format;
     if ((s = check_opts(c, o)) != SGX_OK) return s;
+    if ((s = check_render_projection(c, o)) != SGX_OK) return s;
     cudaSetDevice(c->device);
     if ((s = ensure_size(c, u->width, u->height)) != SGX_OK) return s;
     cudaStream_t st = stream != nullptr ? static_cast<cudaStream_t>(stream) : c->stream;

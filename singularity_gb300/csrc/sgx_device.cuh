@@ -820,9 +820,9 @@ template <class T> __device__ __forceinline__ double carter_Q_fp64(const View<T>
 // projection method; Hairer, Lubich & Wanner, Geometric Numerical
 // Integration, IV.4): |p_theta| = sqrt(Theta), Theta = Q - c^2 (L^2 / s^2 -
 // a^2 E^2), s^2 guarded at 1e-10 as in the right-hand side, the sign of
-// p_theta kept; 0 where truncation has carried the state past a turning point
-// (Theta < 0).  FP32 takes one approximate reciprocal and square root (PTX
-// rcp.approx / sqrt.approx, within 2 ulp of the IEEE results).
+// p_theta kept (copysign); +-0 where truncation has carried the state past a
+// turning point (Theta < 0).  FP32 takes one approximate reciprocal and square
+// root (PTX rcp.approx / sqrt.approx, within 2 ulp of the IEEE results).
 template <class T> __device__ __forceinline__ T project_pth(T pth, T s, T c, T Q, const KC<T>& k) {
     const T s2 = DM<T>::fmax_(s * s, DLIT(1e-10));
     const T th = Q - c * c * (k.L * k.L * DM<T>::rcp_fast(s2) - k.aE * k.aE);
@@ -830,10 +830,11 @@ template <class T> __device__ __forceinline__ T project_pth(T pth, T s, T c, T Q
     if constexpr (std::is_same_v<T, float>) {
         const float x = fmaxf(th, 0.0f);
         asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(m) : "f"(x));
+        return copysignf(m, pth);
     } else {
         m = th > 0.0 ? sqrt(th) : 0.0;
+        return copysign(m, pth);
     }
-    return pth < DLIT(0.0) ? -m : m;
 }
 
 // Constants of motion of a final state, in FP64 (diagnostics): the Carter

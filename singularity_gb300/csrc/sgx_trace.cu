@@ -64,6 +64,9 @@ __device__ __forceinline__ std::uint32_t pack_meta(std::uint32_t term, std::uint
 constexpr int FL_FAST = 1;    // separated-form Kerr RHS
 constexpr int FL_SC = 4;      // fixed step: sin/cos of theta carried in the state
 constexpr int FL_MIXED = 2;
+// error-controlled form: the Carter projection taken from PassDesc::project at
+// run time (the probes) instead of always (the render kernels)
+constexpr int FL_RTPROJ = 8;
 
 // Kerr, fixed step (geodesic_kernel.cu:303-403).
 template <class T, int FL> struct KerrFixed {
@@ -215,6 +218,7 @@ template <class T, int FL> struct KerrAdaptive {
     static constexpr bool FAST = (FL & FL_FAST) != 0;
     static constexpr int FORM = FAST ? RHS_SEP : RHS_REF;
     static constexpr bool MIXED = (FL & FL_MIXED) != 0;
+    static constexpr bool RTPROJ = (FL & FL_RTPROJ) != 0;
     static constexpr int kMinBlocks = sizeof(T) == 4 ? 4 : 1;
     // Multi-view passes hold their view's constants in shared memory and
     // registers rather than the constant bank: 80 registers (3 blocks) beat
@@ -323,7 +327,12 @@ template <class T, int FL> struct KerrAdaptive {
             }
             y = at.y4;
             renormalise(y);
-            if (pass.project) y.pth = project_pth(y.pth, y.s, y.c, Q, c);
+            // the render kernels always project (a run-time flag costs 0.6-1.2 %
+            // of the 4K pass as a select or a branch); the probes honour
+            // PassDesc::project
+            const T pp = project_pth(y.pth, y.s, y.c, Q, c);
+            if constexpr (RTPROJ) y.pth = pass.project ? pp : y.pth;
+            else y.pth = pp;
             k1 = at.k5;
         }
         if (steps >= v.max_steps) {
@@ -758,21 +767,22 @@ cudaError_t run_probe(const void* d_view, std::uint64_t n, const std::uint32_t* 
 // rhs_form: 0 the separated form, 1 the reference's divisions, 2 the
 // separated form with sin/cos of theta carried in the fixed-step state (FP32;
 // FP64 runs form 0; the error-controlled form always carries them).
-template <class F>
+// XF: extra policy flags of the error-controlled form (FL_RTPROJ for the probes).
+template <int XF = 0, class F>
 cudaError_t dispatch(int metric, int precision, int integrator, int rhs_form, F&& f) {
     const bool adaptive = integrator == SGX_INTEGRATOR_ADAPTIVE;
     const bool ref = rhs_form == 1, hw = rhs_form == 2;
     if (metric == SGX_METRIC_KERR && adaptive) {
         if (precision == SGX_PRECISION_FP64)
-            return ref ? f.template operator()<double, KerrAdaptive, 0>()
-                       : f.template operator()<double, KerrAdaptive, FL_FAST>();
+            return ref ? f.template operator()<double, KerrAdaptive, XF>()
+                       : f.template operator()<double, KerrAdaptive, FL_FAST | XF>();
         // the error-controlled form evaluates no sine or cosine per stage, so
         // forms 0 and 2 are the same kernel
         if (precision == SGX_PRECISION_MIXED)
-            return ref ? f.template operator()<float, KerrAdaptive, FL_MIXED>()
-                       : f.template operator()<float, KerrAdaptive, FL_FAST | FL_MIXED>();
-        return ref ? f.template operator()<float, KerrAdaptive, 0>()
-                   : f.template operator()<float, KerrAdaptive, FL_FAST>();
+            return ref ? f.template operator()<float, KerrAdaptive, FL_MIXED | XF>()
+                       : f.template operator()<float, KerrAdaptive, FL_FAST | FL_MIXED | XF>();
+        return ref ? f.template operator()<float, KerrAdaptive, XF>()
+                   : f.template operator()<float, KerrAdaptive, FL_FAST | XF>();
     }
     if (metric == SGX_METRIC_KERR) {
         if (precision == SGX_PRECISION_FP64)
@@ -902,7 +912,7 @@ cudaError_t launch_probe(const void* d_view, int metric, int precision, int inte
     pass.h_max_frac = opts.h_max_frac;
     pass.zone = opts.zone;
     pass.project = opts.project;
-    return dispatch(metric, precision, integrator, rhs_form,
+    return dispatch<FL_RTPROJ>(metric, precision, integrator, rhs_form,
                     [&]<class T, template <class, int> class Policy, int FL>() {
                         return run_probe<T, Policy, FL>(d_view, n, gx, gy, s, hdr3, steps, term, pass, st);
                     });
@@ -916,18 +926,21 @@ cudaError_t launch_invariants(const void* d_view, int precision, int rhs_form, s
     if (blocks == 0) return cudaSuccess;
     const bool ref = rhs_form == 1;
     const unsigned b = unsigned(blocks);
+    constexpr int R = FL_RTPROJ;
     if (precision == SGX_PRECISION_FP64) {
         const auto* vw = static_cast<const View<double>*>(d_view);
-        if (ref) trace_invariants<double, 0><<<b, threads, 0, st>>>(vw, n, gx, gy, s, inv5, term, pass);
-        else trace_invariants<double, FL_FAST><<<b, threads, 0, st>>>(vw, n, gx, gy, s, inv5, term, pass);
+        if (ref) trace_invariants<double, R><<<b, threads, 0, st>>>(vw, n, gx, gy, s, inv5, term, pass);
+        else trace_invariants<double, FL_FAST | R><<<b, threads, 0, st>>>(vw, n, gx, gy, s, inv5, term, pass);
     } else {
         const auto* vw = static_cast<const View<float>*>(d_view);
         if (precision == SGX_PRECISION_MIXED) {
-            if (ref) trace_invariants<float, FL_MIXED><<<b, threads, 0, st>>>(vw, n, gx, gy, s, inv5, term, pass);
-            else trace_invariants<float, FL_FAST | FL_MIXED><<<b, threads, 0, st>>>(vw, n, gx, gy, s, inv5, term, pass);
+            if (ref) trace_invariants<float, FL_MIXED | R><<<b, threads, 0, st>>>(vw, n, gx, gy, s, inv5, term, pass);
+            else
+                trace_invariants<float, FL_FAST | FL_MIXED | R><<<b, threads, 0, st>>>(vw, n, gx, gy, s, inv5, term,
+                                                                                        pass);
         } else {
-            if (ref) trace_invariants<float, 0><<<b, threads, 0, st>>>(vw, n, gx, gy, s, inv5, term, pass);
-            else trace_invariants<float, FL_FAST><<<b, threads, 0, st>>>(vw, n, gx, gy, s, inv5, term, pass);
+            if (ref) trace_invariants<float, R><<<b, threads, 0, st>>>(vw, n, gx, gy, s, inv5, term, pass);
+            else trace_invariants<float, FL_FAST | R><<<b, threads, 0, st>>>(vw, n, gx, gy, s, inv5, term, pass);
         }
     }
     return cudaGetLastError();
