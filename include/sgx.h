@@ -44,7 +44,7 @@ typedef enum sgx_status {
 typedef enum sgx_format {
     SGX_FORMAT_RGBA8_SRGB = 0, /* reference output: ACES per sample, mean, sRGB, u8 */
     SGX_FORMAT_RGBA32F = 1,    /* the same mean before sRGB/quantisation, float, alpha 1 */
-    SGX_FORMAT_RGBA16F_HDR = 2 /* mean scene-referred HDR (x exposure), half, alpha 1 */
+    SGX_FORMAT_RGBA16F_HDR = 2 /* mean scene-referred HDR (before exposure), half, alpha 1 */
 } sgx_format;
 
 /* Arithmetic of the integration. */
@@ -255,7 +255,11 @@ sgx_status sgx_trace_invariants(sgx_context* ctx, const sgx_uniforms* u, const s
  * half-resolution Karis-weighted extract with a soft-knee threshold, a
  * separable blur, and the compose hdr + bloom * strength, times exposure,
  * ACES, then sRGB (RGBA8) or linear (RGBA32F).  Capture the result with
- * sgx_capture in that format. */
+ * sgx_capture in that format.  The extract at the uniforms' threshold is made
+ * by the render itself (sgx_render in SGX_FORMAT_RGBA16F_HDR fuses it into
+ * its last accumulation pass), so with threshold < 0 the first call after a
+ * render blurs and composes only; a threshold of the caller's own, or a
+ * later call on the same frame, extracts again from the HDR frame. */
 typedef struct sgx_bloom_opts {
     uint32_t struct_size;
     float sigma_px;  /* blur sigma in full-resolution pixels; <= 0: the reference's 7-tap kernel */

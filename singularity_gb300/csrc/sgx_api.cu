@@ -39,6 +39,7 @@ void free_image(sgx_context* c) {
     c->d_bloom = nullptr;
     c->d_post = nullptr;
     c->bloom_cap = 0;
+    c->bloom_ext_valid = false;
     c->post_valid = false;
     if (c->d_acc) cudaFree(c->d_acc);
     if (c->d_results) cudaFree(c->d_results);
@@ -187,6 +188,15 @@ sgx_status render_impl(sgx_context* c, const sgx_uniforms* u, const sgx_render_o
     }
     const std::uint32_t tw = o.tile_w;
     const std::uint32_t th = o.tile_h;
+    // An HDR frame into the context's image fuses the bloom extract into its
+    // last accumulation pass (sgx_bloom then blurs and composes only).
+    c->bloom_ext_valid = false;
+    const bool fuse_ext = format == SGX_FORMAT_RGBA16F_HDR && out == c->d_image && slice.count <= 1u &&
+                          u->width >= 2u && u->height >= 2u;
+    if (fuse_ext) {
+        const sgx_status bs = sgx_internal::ensure_bloom_targets(c, u->width, u->height);
+        if (bs != SGX_OK) return bs;
+    }
 
     sgx_render_stats acc{};
     for (std::uint32_t done = 0; done < count;) {
@@ -215,8 +225,13 @@ sgx_status render_impl(sgx_context* c, const sgx_uniforms* u, const sgx_render_o
         SGX_CUDA(c, cudaEventRecord(c->ev_trace1, st));
         const bool first = (s0 == 0);
         const bool finalize = (s0 + n == spp);
-        SGX_CUDA(c, sgxk::launch_accumulate(int(o.precision), pass.vs, c->d_results, c->d_acc, first, finalize,
-                                            format, out, st));
+        if (finalize && fuse_ext)
+            SGX_CUDA(c, sgxk::launch_accumulate_hdr_extract(int(o.precision), pass.vs, c->d_results, c->d_acc, first,
+                                                            out, c->d_bloom, u->width, u->height,
+                                                            u->bloom_threshold, st));
+        else
+            SGX_CUDA(c, sgxk::launch_accumulate(int(o.precision), pass.vs, c->d_results, c->d_acc, first, finalize,
+                                                format, out, st));
         SGX_CUDA(c, cudaMemcpyAsync(c->h_counters, c->d_counters, sizeof(sgxk::PassCounters),
                                     cudaMemcpyDeviceToHost, st));
         SGX_CUDA(c, cudaEventRecord(c->ev_end, st));
@@ -231,6 +246,10 @@ sgx_status render_impl(sgx_context* c, const sgx_uniforms* u, const sgx_render_o
         done += n;
         c->next_sample = s0 + n;
         c->frame_valid = finalize;
+        if (finalize && fuse_ext) {
+            c->bloom_ext_valid = true;
+            c->bloom_ext_threshold = u->bloom_threshold;
+        }
     }
     c->frame_spp = spp;
     c->frame_format = format;

@@ -42,6 +42,8 @@ struct sgx_context {
     sgx_uniforms last_u{};        // uniforms of the last render (bloom reads exposure, threshold, strength)
     void* d_bloom = nullptr;      // two half-resolution half4 targets
     std::size_t bloom_cap = 0;    // bytes of one target
+    bool bloom_ext_valid = false; // the first target holds the extract the last HDR render fused in ...
+    float bloom_ext_threshold = 0.0f;  // ... at this threshold
     void* d_post = nullptr;       // composed frame after sgx_bloom (16 B / pixel)
     bool post_valid = false;
     std::uint32_t post_format = SGX_FORMAT_RGBA8_SRGB;
@@ -53,6 +55,8 @@ void sgx_internal_free_diff(sgx_context* ctx);
 
 
 namespace sgx_internal {
+// The two half-resolution bloom targets of a W x H frame (sgx_post.cu).
+sgx_status ensure_bloom_targets(sgx_context* ctx, std::uint32_t W, std::uint32_t H);
 inline sgx_status fail(sgx_context* ctx, sgx_status s, const std::string& msg) {
     if (ctx != nullptr) ctx->err = msg;
     return s;

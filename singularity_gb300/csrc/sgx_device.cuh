@@ -1061,4 +1061,34 @@ __device__ __forceinline__ double error_norm_fp64_1div(const KSC<T>& y, const KA
     return e;
 }
 
+// ---------------------------------------------------------------------------
+// Bloom extract (render/vulkan/shaders/bloom.hlsl:13-40): one half-resolution
+// texel from a 2x2 block of the HDR frame (the values as the half-precision
+// frame holds them): the Karis-weighted average (weights 1 / (1 + luma)),
+// scaled by the soft knee luma^2 / max(luma + threshold, 1e-4) / luma.  One
+// definition for the separate extract kernel and for the extract fused into
+// the last accumulation pass, so the two give the same texel.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float bloom_luma(float r, float g, float b) {
+    return r * 0.2126f + g * 0.7152f + b * 0.0722f;
+}
+
+__device__ __forceinline__ void karis_extract(float4 a, float4 b, float4 c, float4 d, float threshold, float& r,
+                                              float& g, float& bl) {
+    const float la = 1.0f / (1.0f + bloom_luma(a.x, a.y, a.z));
+    const float lb = 1.0f / (1.0f + bloom_luma(b.x, b.y, b.z));
+    const float lc = 1.0f / (1.0f + bloom_luma(c.x, c.y, c.z));
+    const float ld = 1.0f / (1.0f + bloom_luma(d.x, d.y, d.z));
+    const float wden = fmaxf(la + lb + lc + ld, 1e-6f);
+    const float ar = (a.x * la + b.x * lb + c.x * lc + d.x * ld) / wden;
+    const float ag = (a.y * la + b.y * lb + c.y * lc + d.y * ld) / wden;
+    const float ab = (a.z * la + b.z * lb + c.z * lc + d.z * ld) / wden;
+    const float l = bloom_luma(ar, ag, ab);
+    const float knee = (l * l) / fmaxf(l + threshold, 1e-4f);
+    const float k = (l > 1e-4f) ? (knee / l) : 0.0f;
+    r = ar * k;
+    g = ag * k;
+    bl = ab * k;
+}
+
 }  // namespace sgxd

@@ -139,6 +139,14 @@ cudaError_t launch_invariants(const void* d_view, int precision, int rhs_form, s
 cudaError_t launch_accumulate(int precision, const ViewSet& vs, const void* results, float4* acc, bool first,
                               bool finalize, std::uint32_t format, void* out, cudaStream_t st);
 
+// The last pass of a single-view, unsliced SGX_FORMAT_RGBA16F_HDR frame (W x
+// H, W and H >= 2) with the bloom extract fused in: as launch_accumulate with
+// finalize, plus ext (W/2 x H/2 half4 texels) = the Karis-weighted, soft-knee
+// extract of each 2x2 block of the half-precision frame at `threshold`.
+cudaError_t launch_accumulate_hdr_extract(int precision, const ViewSet& vs, const void* results, float4* acc,
+                                          bool first, void* out, void* ext, std::uint32_t W, std::uint32_t H,
+                                          float threshold, cudaStream_t st);
+
 // Re-encodes an accumulated single-view frame (acc, float4 mean-sum) in another format.
 cudaError_t launch_encode(const float4* acc, std::uint32_t npix, float scale, std::uint32_t format, void* out,
                           cudaStream_t st);

@@ -49,8 +49,9 @@ __device__ __forceinline__ void store_h4(__half2* p, std::uint64_t i, float x, f
     p[2 * i + 1] = __floats2half2_rn(z, 1.0f);
 }
 
-__device__ __forceinline__ float luma(float r, float g, float b) { return r * 0.2126f + g * 0.7152f + b * 0.0722f; }
-
+// Separate extract from the stored HDR frame: used when sgx_bloom is given a
+// threshold of its own, or on a second post-process of the same frame (the
+// last accumulation pass fuses the extract at the uniforms' threshold).
 __global__ void extract_kernel(const __half2* __restrict__ hdr, int W, __half2* __restrict__ dst, int bw, int bh,
                                float threshold) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -61,18 +62,9 @@ __global__ void extract_kernel(const __half2* __restrict__ hdr, int W, __half2* 
     const float4 b = load_h4(hdr, std::uint64_t(sy) * W + sx + 1);
     const float4 c = load_h4(hdr, std::uint64_t(sy + 1) * W + sx);
     const float4 d = load_h4(hdr, std::uint64_t(sy + 1) * W + sx + 1);
-    const float la = 1.0f / (1.0f + luma(a.x, a.y, a.z));
-    const float lb = 1.0f / (1.0f + luma(b.x, b.y, b.z));
-    const float lc = 1.0f / (1.0f + luma(c.x, c.y, c.z));
-    const float ld = 1.0f / (1.0f + luma(d.x, d.y, d.z));
-    const float wden = fmaxf(la + lb + lc + ld, 1e-6f);
-    const float r = (a.x * la + b.x * lb + c.x * lc + d.x * ld) / wden;
-    const float g = (a.y * la + b.y * lb + c.y * lc + d.y * ld) / wden;
-    const float bl = (a.z * la + b.z * lb + c.z * lc + d.z * ld) / wden;
-    const float l = luma(r, g, bl);
-    const float knee = (l * l) / fmaxf(l + threshold, 1e-4f);
-    const float k = (l > 1e-4f) ? (knee / l) : 0.0f;
-    store_h4(dst, std::uint64_t(y) * bw + x, r * k, g * k, bl * k);
+    float r, g, bl;
+    sgxd::karis_extract(a, b, c, d, threshold, r, g, bl);
+    store_h4(dst, std::uint64_t(y) * bw + x, r, g, bl);
 }
 
 __global__ void blur_kernel(const __half2* __restrict__ src, __half2* __restrict__ dst, int bw, int bh, int vertical,
@@ -157,6 +149,20 @@ Kernel1D make_kernel(float sigma_px) {
 
 }  // namespace
 
+sgx_status sgx_internal::ensure_bloom_targets(sgx_context* c, std::uint32_t W, std::uint32_t H) {
+    const std::uint32_t bw = W / 2 > 1 ? W / 2 : 1, bh = H / 2 > 1 ? H / 2 : 1;
+    const std::size_t half_bytes = std::size_t(bw) * bh * 8;
+    if (c->bloom_cap >= half_bytes) return SGX_OK;
+    if (c->d_bloom) cudaFree(c->d_bloom);
+    c->d_bloom = nullptr;
+    c->bloom_cap = 0;
+    c->bloom_ext_valid = false;
+    cudaError_t e = cudaMalloc(&c->d_bloom, 2 * half_bytes);
+    if (e != cudaSuccess) return cuda_fail(c, e, "bloom targets: cudaMalloc");
+    c->bloom_cap = half_bytes;
+    return SGX_OK;
+}
+
 extern "C" sgx_status sgx_bloom(sgx_context* c, const sgx_bloom_opts* opts) {
     if (c == nullptr) return SGX_ERR_INVALID_ARGUMENT;
     if (!c->frame_valid || c->frame_format != SGX_FORMAT_RGBA16F_HDR)
@@ -177,14 +183,8 @@ extern "C" sgx_status sgx_bloom(sgx_context* c, const sgx_bloom_opts* opts) {
     if (W < 2 || H < 2) return fail(c, SGX_ERR_INVALID_ARGUMENT, "bloom needs at least 2x2 pixels");
     cudaSetDevice(c->device);
     const std::size_t half_bytes = std::size_t(bw) * bh * 8;
-    if (c->bloom_cap < half_bytes) {
-        if (c->d_bloom) cudaFree(c->d_bloom);
-        c->d_bloom = nullptr;
-        c->bloom_cap = 0;
-        cudaError_t e = cudaMalloc(&c->d_bloom, 2 * half_bytes);
-        if (e != cudaSuccess) return cuda_fail(c, e, "sgx_bloom: cudaMalloc");
-        c->bloom_cap = half_bytes;
-    }
+    const sgx_status st = sgx_internal::ensure_bloom_targets(c, std::uint32_t(W), std::uint32_t(H));
+    if (st != SGX_OK) return st;
     if (c->d_post == nullptr) {
         cudaError_t e = cudaMalloc(&c->d_post, std::size_t(W) * H * 16);
         if (e != cudaSuccess) return cuda_fail(c, e, "sgx_bloom: cudaMalloc");
@@ -195,7 +195,12 @@ extern "C" sgx_status sgx_bloom(sgx_context* c, const sgx_bloom_opts* opts) {
     const dim3 blk(16, 16);
     const dim3 gh((bw + 15) / 16, (bh + 15) / 16), gf((W + 15) / 16, (H + 15) / 16);
     const Kernel1D kw = make_kernel(o.sigma_px);
-    extract_kernel<<<gh, blk, 0, c->stream>>>(hdr, W, a, bw, bh, threshold);
+    // the render's last accumulation pass already wrote the extract at the
+    // uniforms' threshold into the first target; a threshold of the caller's
+    // own, or a second post-process of the frame, extracts again
+    const bool fused = o.threshold < 0.0f && c->bloom_ext_valid && c->bloom_ext_threshold == threshold;
+    if (!fused) extract_kernel<<<gh, blk, 0, c->stream>>>(hdr, W, a, bw, bh, threshold);
+    c->bloom_ext_valid = false;  // the blur below overwrites the first target
     blur_kernel<<<gh, blk, 0, c->stream>>>(a, b, bw, bh, 0, kw);
     blur_kernel<<<gh, blk, 0, c->stream>>>(b, a, bw, bh, 1, kw);
     compose_kernel<<<gf, blk, 0, c->stream>>>(hdr, a, W, H, bw, bh, strength, c->last_u.exposure, o.format, c->d_post);

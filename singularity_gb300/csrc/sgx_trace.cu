@@ -674,24 +674,18 @@ __device__ __forceinline__ void encode_pixel(float4 sum, float scale, std::uint3
 // geodesic_kernel.cu:492-501); the last pass scales by 1/spp and encodes.
 // For the HDR format the sum is of the raw HDR colour (no exposure, no tone
 // map), the input of the bloom/blit pipeline.
+// The pass's samples of packed pixel p of view vid added to its running sum
+// in sample order; the sum is stored back to acc and returned.
 template <class T>
-__global__ void __launch_bounds__(256) accumulate_kernel(ViewSet vs, const Rec<T>* __restrict__ results,
-                                                         float4* __restrict__ acc, bool first, bool finalize,
-                                                         std::uint32_t format, void* out) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const SmemSet<T> m = carve<T>(smem_raw, vs.n, 0);
-    load_set(m, vs, false);
-    __syncthreads();
-    const std::uint64_t p = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (p >= vs.total_pix) return;
-    const std::uint32_t vid = vs.n == 1u ? 0u : find_view(m.pix_off, vs.n, p);
+__device__ __forceinline__ float4 accum_pixel(const SmemSet<T>& m, const ViewSet& vs, std::uint32_t vid,
+                                              std::uint64_t p, const Rec<T>* __restrict__ results,
+                                              float4* __restrict__ acc, bool first, bool raw) {
     const View<T>& v = m.views[vid];
     const std::uint64_t pix = p - m.pix_off[vid];
     const std::uint64_t npix = std::uint64_t(v.width) * (vs.slice_count > 1u ? vs.slice_h : v.height);
     const std::uint64_t base = m.rec_off[vid] + pix;
     const std::uint32_t S = m.S[vid];
     float4 sum = first ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : acc[p];
-    const bool raw = format == SGX_FORMAT_RGBA16F_HDR;
     for (std::uint32_t s = 0; s < S; ++s) {
         const Rec<T> rec = results[base + std::uint64_t(s) * npix];
         const V3<T> hdr = shade_record(v, rec);
@@ -706,7 +700,90 @@ __global__ void __launch_bounds__(256) accumulate_kernel(ViewSet vs, const Rec<T
         }
     }
     acc[p] = sum;
-    if (finalize) encode_pixel(sum, 1.0f / float(v.spp), format, out, p);
+    return sum;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) accumulate_kernel(ViewSet vs, const Rec<T>* __restrict__ results,
+                                                         float4* __restrict__ acc, bool first, bool finalize,
+                                                         std::uint32_t format, void* out) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const SmemSet<T> m = carve<T>(smem_raw, vs.n, 0);
+    load_set(m, vs, false);
+    __syncthreads();
+    const std::uint64_t p = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (p >= vs.total_pix) return;
+    const std::uint32_t vid = vs.n == 1u ? 0u : find_view(m.pix_off, vs.n, p);
+    const float4 sum = accum_pixel(m, vs, vid, p, results, acc, first, format == SGX_FORMAT_RGBA16F_HDR);
+    if (finalize) encode_pixel(sum, 1.0f / float(m.views[vid].spp), format, out, p);
+}
+
+// The last pass of a single-view HDR frame with the bloom extract fused in:
+// one lane per pixel as in accumulate_kernel, the four lanes of a 2x2 block of
+// the frame (bw x bh = W/2 x H/2 blocks) adjacent in the warp.  Each adds its
+// pixel's samples and writes the half-precision HDR mean; the block's first
+// lane gathers the four half values by warp shuffles and writes the block's
+// half-resolution extract texel (karis_extract, as the separate extract
+// kernel computes it from the stored frame).  Lanes past the blocks take the
+// pixels outside them (the last column when W is odd, then the last row when
+// H is odd).  Every lane of a warp reaches the shuffles.
+template <class T>
+__global__ void __launch_bounds__(256)
+    accumulate_hdr_extract_kernel(ViewSet vs, const Rec<T>* __restrict__ results, float4* __restrict__ acc,
+                                  bool first, void* out, __half2* __restrict__ ext, std::uint32_t bw,
+                                  std::uint32_t bh, float threshold) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const SmemSet<T> m = carve<T>(smem_raw, vs.n, 0);
+    load_set(m, vs, false);
+    __syncthreads();
+    const View<T>& v = m.views[0];
+    const std::uint32_t W = v.width, H = v.height;
+    const float scale = 1.0f / float(v.spp);
+    const std::uint64_t t = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const std::uint64_t nq = std::uint64_t(bw) * bh;
+    const bool in_block = t < 4ull * nq;
+    bool valid = true;
+    std::uint64_t p = 0;
+    if (in_block) {
+        const std::uint64_t q = t >> 2;
+        const std::uint32_t k = std::uint32_t(t & 3ull);
+        const std::uint32_t qy = std::uint32_t(q / bw), qx = std::uint32_t(q - std::uint64_t(qy) * bw);
+        p = std::uint64_t(2u * qy + (k >> 1)) * W + 2u * qx + (k & 1u);
+    } else {
+        std::uint64_t e = t - 4ull * nq;
+        if (W > 2u * bw && e < 2ull * bh) {
+            p = e * W + (W - 1u);
+        } else {
+            if (W > 2u * bw) e -= 2ull * bh;
+            valid = H > 2u * bh && e < W;
+            p = std::uint64_t(H - 1u) * W + e;
+        }
+    }
+    float4 h = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (valid) {
+        const float4 sum = accum_pixel(m, vs, 0u, p, results, acc, first, true);
+        encode_pixel(sum, scale, SGX_FORMAT_RGBA16F_HDR, out, p);
+        // the pixel as the half-precision frame holds it
+        const float2 lo = __half22float2(__floats2half2_rn(sum.x * scale, sum.y * scale));
+        const float2 hi = __half22float2(__floats2half2_rn(sum.z * scale, 1.0f));
+        h = make_float4(lo.x, lo.y, hi.x, hi.y);
+    }
+    const unsigned lane = threadIdx.x & 31u, lead = lane & ~3u;
+    float4 qv[4];
+#pragma unroll
+    for (unsigned k = 0; k < 4u; ++k) {
+        qv[k].x = __shfl_sync(kFull, h.x, lead + k);
+        qv[k].y = __shfl_sync(kFull, h.y, lead + k);
+        qv[k].z = __shfl_sync(kFull, h.z, lead + k);
+        qv[k].w = 1.0f;
+    }
+    if (in_block && (lane & 3u) == 0u) {
+        float r, g, b;
+        karis_extract(qv[0], qv[1], qv[2], qv[3], threshold, r, g, b);
+        const std::uint64_t q = t >> 2;
+        ext[2 * q] = __floats2half2_rn(r, g);
+        ext[2 * q + 1] = __floats2half2_rn(b, 1.0f);
+    }
 }
 
 __global__ void encode_kernel(const float4* __restrict__ acc, std::uint32_t npix, float scale, std::uint32_t format,
@@ -965,6 +1042,27 @@ cudaError_t launch_accumulate(int precision, const ViewSet& vs, const void* resu
         if (e != cudaSuccess) return e;
         accumulate_kernel<float><<<unsigned(blocks), threads, smem, st>>>(
             vs, static_cast<const Rec<float>*>(results), acc, first, finalize, format, out);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_accumulate_hdr_extract(int precision, const ViewSet& vs, const void* results, float4* acc,
+                                          bool first, void* out, void* ext, std::uint32_t W, std::uint32_t H,
+                                          float threshold, cudaStream_t st) {
+    if (vs.n != 1u || vs.slice_count > 1u || W < 2u || H < 2u) return cudaErrorInvalidValue;
+    const std::uint32_t bw = W / 2u, bh = H / 2u;
+    const std::uint64_t n = 4ull * bw * bh + (W > 2u * bw ? 2ull * bh : 0ull) + (H > 2u * bh ? W : 0u);
+    const unsigned threads = 256;
+    const unsigned blocks = unsigned((n + threads - 1) / threads);
+    __half2* e = static_cast<__half2*>(ext);
+    if (precision == SGX_PRECISION_FP64) {
+        const std::size_t smem = set_smem_bytes<double>(vs.n, 0);
+        accumulate_hdr_extract_kernel<double><<<blocks, threads, smem, st>>>(
+            vs, static_cast<const Rec<double>*>(results), acc, first, out, e, bw, bh, threshold);
+    } else {
+        const std::size_t smem = set_smem_bytes<float>(vs.n, 0);
+        accumulate_hdr_extract_kernel<float><<<blocks, threads, smem, st>>>(
+            vs, static_cast<const Rec<float>*>(results), acc, first, out, e, bw, bh, threshold);
     }
     return cudaGetLastError();
 }

@@ -80,3 +80,38 @@ def test_bloom_errors(renderer, sgx):
         renderer.capture(N.FORMAT_RGBA8_SRGB)
     with pytest.raises(sgx.SgxError):
         renderer.bloom(fmt=N.FORMAT_RGBA16F_HDR)
+
+
+@pytest.mark.parametrize("w,h,precision", [(128, 70, 0), (97, 55, 0), (64, 37, 2)])
+def test_fused_extract_equals_the_separate_pass(renderer, sgx, w, h, precision):
+    """An HDR render into the context's image writes the bloom extract in its
+    last accumulation pass, so the first sgx_bloom after it blurs and
+    composes only; a threshold of the caller's own makes sgx_bloom extract
+    again from the stored frame.  Both composites are the same, the fused
+    pass's HDR frame equals the plain accumulation's (sgx_render_device into a
+    caller buffer, which does not fuse), and progressive passes fuse on their
+    last pass.  Odd sizes exercise the pixels outside the 2x2 blocks."""
+    import ctypes as C
+    import torch
+    N = sgx._native
+    u = _scene(sgx, w, h, spp=4)
+    opts = sgx.default_opts(format=N.FORMAT_RGBA16F_HDR, precision=precision)
+    hdr = renderer.render_image(u, opts, fmt=N.FORMAT_RGBA16F_HDR)
+    fused = renderer.bloom(sigma_px=8.0, fmt=N.FORMAT_RGBA32F)
+    separate = renderer.bloom(sigma_px=8.0, threshold=u.bloom_threshold, fmt=N.FORMAT_RGBA32F)
+    np.testing.assert_array_equal(fused, separate)
+    again = renderer.bloom(sigma_px=8.0, fmt=N.FORMAT_RGBA32F)  # a second call extracts again
+    np.testing.assert_array_equal(again, fused)
+    dev = torch.zeros(w * h * 8, dtype=torch.uint8, device="cuda")
+    lib = N.load()
+    st = lib.sgx_render_device(renderer.handle, C.byref(u), C.byref(opts), C.c_void_p(dev.data_ptr()),
+                               N.FORMAT_RGBA16F_HDR, None)
+    assert st == 0, lib.sgx_last_error(renderer.handle).decode()
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(dev.cpu().numpy().view(np.float16).reshape(h, w, 4), hdr)
+    for b in (0, 3):
+        o = sgx.default_opts(format=N.FORMAT_RGBA16F_HDR, precision=precision, sample_begin=b,
+                             sample_count=3 if b == 0 else 1)
+        renderer.render(u, o)
+    np.testing.assert_array_equal(renderer.capture(N.FORMAT_RGBA16F_HDR), hdr)
+    np.testing.assert_array_equal(renderer.bloom(sigma_px=8.0, fmt=N.FORMAT_RGBA32F), fused)
