@@ -119,3 +119,23 @@ def test_png_reader_handles_every_row_filter(tmp_path):
     path.write_bytes(b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", 7, 5, 8, 6, 0, 0, 0))
                      + chunk(b"IDAT", zlib.compress(raw)) + chunk(b"IEND", b""))
     np.testing.assert_array_equal(read_png(path), img)
+
+
+@pytest.mark.gpu
+def test_relinked_cli_multi_frame_orbit_equals_ours(relinked, tmp_path):
+    """The reference's multi-frame mode (`--frames 4 --output-pattern`, the
+    camera orbiting 2 pi and the disc clock advancing 1/30 s a frame,
+    cuda_cli/main.cpp:251-338) through the relinked reference CLI and
+    through singularity_cuda_cli: the same four frames."""
+    ours = ROOT / "singularity_gb300" / "_build" / "singularity_cuda_cli"
+    scene = tmp_path / "k.scene"
+    scene.write_text(GOLDEN_SCENES["kerr_a094"])
+    for exe, name in ((relinked, "ref"), (ours, "ours")):
+        r = run(exe, "--frames", "4", "--output-pattern", tmp_path / f"{name}_%02d.png", "--res", "96x64",
+                "--samples-per-pixel", "2", "--scene", scene)
+        assert r.returncode == 0, r.stderr
+        assert r.stdout.count("wrote") == 4
+    for k in range(4):
+        a, b = read_png(tmp_path / f"ref_{k:02d}.png"), read_png(tmp_path / f"ours_{k:02d}.png")
+        np.testing.assert_array_equal(a, b)
+    assert not np.array_equal(read_png(tmp_path / "ours_00.png"), read_png(tmp_path / "ours_02.png"))
