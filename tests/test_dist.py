@@ -145,3 +145,15 @@ def test_split_frame_gathers_to_the_whole_frame_two_gloo_ranks(sgx, oracle):
     assert out[1] is None
     whole, _ = oracle.render(u)
     np.testing.assert_array_equal(out[0], whole)
+
+
+def test_assemble_slices_with_torch_tensors():
+    """dist.assemble_slices puts the rows of torch slices (the gathered NCCL
+    buffers) back in frame order, as it does for numpy arrays."""
+    import torch
+    from singularity_gb300 import dist as D
+    H, W, band, count = 37, 5, 4, 3
+    frame = torch.arange(H * W * 4, dtype=torch.int32).reshape(H, W, 4)
+    parts = [frame[torch.as_tensor(D.slice_row_indices(H, band, count, i))] for i in range(count)]
+    assert torch.equal(D.assemble_slices(parts, H, band), frame)
+    assert np.array_equal(D.assemble_slices([p.numpy() for p in parts], H, band), frame.numpy())

@@ -207,3 +207,28 @@ def test_projection_keeps_the_image(renderer, oracle, sgx):
     assert np.abs(img - ldr64).mean() <= 1e-3
     with pytest.raises(sgx.SgxError):
         renderer.render(u, o)
+
+
+def test_invariants_and_projection_options_are_checked(renderer, sgx):
+    """sgx_trace_invariants reports the error-controlled Kerr form only (the
+    fixed step or Schwarzschild uniforms are refused); an empty sample list
+    is a no-op; a batch refuses projection = 0 like a render."""
+    N = sgx._native
+    u = _scene(sgx, 16, 16, spp=1)
+    gx = np.zeros(4, np.uint32)
+    with pytest.raises(sgx.SgxError):
+        renderer.trace_invariants(u, gx, gx, gx, sgx.default_opts())  # fixed step
+    sc = sgx.Scene(metric=sgx.MetricType.Schwarzschild, spin_a_over_M=0.0, disc_inner_M=6.0, disc_outer_M=20.0)
+    us = sgx.pack_uniforms(sc, sgx.build_orbital_camera(30.0, 0.2, 0.0, 40.0), 16, 16)
+    with pytest.raises(sgx.SgxError):
+        renderer.trace_invariants(us, gx, gx, gx, _opts(sgx, "f32"))
+    inv, term = renderer.trace_invariants(u, gx[:0], gx[:0], gx[:0], _opts(sgx, "f32"))
+    assert inv.shape == (0, 5) and term.shape == (0,)
+    o = _opts(sgx, "f32")
+    o.projection = 0
+    with pytest.raises(sgx.SgxError):
+        sgx.Batch(renderer, [u, u], o)
+    o.projection = 1
+    o.slice_count, o.slice_index = 2, 0
+    with pytest.raises(sgx.SgxError):
+        sgx.Batch(renderer, [u, u], o)
