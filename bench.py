@@ -689,7 +689,7 @@ def main() -> None:
     if single and not args.no_precision_study and adaptive_main:
         study = precision_study(S, N, O, lib, r, u, d_out, stream, torch)
     same = None
-    if single and not args.no_same_algorithm and args.workload == "4k":
+    if single and not args.no_same_algorithm:
         same = same_algorithm_study(S, N, lib, r, u, d_out, stream, torch)
         if study is not None:
             same["adaptive_steps_per_ray"] = study["mixed_steps_per_ray"]
@@ -724,7 +724,7 @@ def main() -> None:
         "hdr_bloom_1080p": sig(hdr),
         "adjoint_512x512x4": sig(diff, 3),
         "cli_4k_256spp": sig(cli),
-        "same_algorithm_4k_16spp": sig(same),
+        ("same_algorithm_4k_16spp" if args.workload == "4k" else "same_algorithm_16spp"): sig(same),
         "precision_study": sig(study, 3),
     }
     print(json.dumps(line, separators=(",", ":")), flush=True)
