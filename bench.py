@@ -706,7 +706,7 @@ def main() -> None:
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "strong",
-        "vs_baseline": value / 13.1, "dtype": "f32" if args.precision != "fp64" else "f64", "data": "synthetic",
+        "vs_baseline": None, "dtype": "f32" if args.precision != "fp64" else "f64", "data": "synthetic",
         "config": {"workload": f"{scene_name()}_{algo}_{args.precision}", "spp_per_step": SPP_PER_STEP,
                    "rays_per_step": npix * SPP_PER_STEP,
                    "integrator": ("error-controlled RK4, FSAL 3rd-order estimate, tol 1e-6, p_theta projected "
@@ -715,8 +715,10 @@ def main() -> None:
                    "precision": args.precision, "rhs_form": args.rhs_form,
                    "parallelism": f"frame split in {world} slices of 8-row bands" if world > 1 else "1 GPU",
                    "l2": "each step writes a 2.1 GB per-sample buffer (> 129 MB L2); no extra flush",
-                   "vs_baseline_basis": "13.1 Mrays/s: 4K Kerr a/M=0.94 256 spp in 162 s on an RTX 3090 "
-                                        "(README.md:39,130), wall clock incl. PNG, fixed step h=0.4"},
+                   "vs_published_rtx3090_basis": "13.1 Mrays/s derived from the reference's 4K Kerr a/M=0.94 256 "
+                                                 "spp in 162 s on an RTX 3090 (README.md:39,130): wall clock incl. "
+                                                 "PNG, fixed step h=0.4, its default camera (not this config)"},
+        "vs_published_rtx3090": value / 13.1,
         "roofline": sig(roof, 5), "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
         "gpu_launches": 3 * args.steps,
         "budget_exhausted_rays": stats_acc["budget"],
