@@ -102,3 +102,8 @@ def test_noalloc_rejects_frames_beyond_its_scratch(sgx):
     opts = sgx.default_opts(sample_begin=2)
     st, msg = _noalloc(lib, N, u, N.FORMAT_RGBA8_SRGB, out, 0, opts)
     assert st == 1 and "whole frames" in msg
+    # nor frame slices, and a tile needs both of its sides
+    st, msg = _noalloc(lib, N, u, N.FORMAT_RGBA8_SRGB, out, 0, sgx.default_opts(slice_count=2))
+    assert st == 1 and "slices" in msg
+    st, msg = _noalloc(lib, N, u, N.FORMAT_RGBA8_SRGB, out, 0, sgx.default_opts(tile_w=8))
+    assert st == 1 and "tile" in msg
