@@ -164,7 +164,7 @@ def reference_cpu_rate(O, u_ref, seconds: float = 12.0, seed: int = 0) -> dict:
     def run(n):
         gx, gy, s = _sample_rays(rng, npix, u_ref.width, n, 0)
         t0 = time.perf_counter()
-        O.ref_trace(u_ref, gx, gy, s, threads=threads)
+        O.ref_trace(u_ref, gx, gy, s, threads=threads, release=True)
         return gx.size, time.perf_counter() - t0
 
     _, dt = run(256)
@@ -172,7 +172,8 @@ def reference_cpu_rate(O, u_ref, seconds: float = 12.0, seed: int = 0) -> dict:
     rays, dt = run(n)
     return {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "reference",
             "sample": f"{n} random pixels x {SPP_PER_STEP} Halton samples ({rays} rays, {dt:.1f} s) through the "
-                      "reference's geodesic_kernel.cu compiled for the host, fixed step h=0.4"}
+                      "reference's geodesic_kernel.cu compiled for the host with its Release flags (-O3 "
+                      "-ffast-math), fixed step h=0.4"}
 
 
 def ops_per_step(O, u, n: int = 1024, seed: int = 1, adaptive=None) -> tuple[float, float]:
@@ -196,7 +197,7 @@ def run_reference(args, rank: int) -> None:
     except Exception as e:  # noqa: BLE001
         print(json.dumps({"impl": "reference", "unavailable": f"building the reference for this host failed: {e}"}))
         return
-    if not O.ref_available():
+    if not (O.ref_available() and O.REF_RELEASE_LIB.exists()):
         print(json.dumps({"impl": "reference", "unavailable": "no reference sources (checkout or the "
                                                               "oracle/_ref/src snapshot) on this machine"}))
         return
@@ -211,7 +212,7 @@ def run_reference(args, rank: int) -> None:
     def step():
         gx, gy, s = _sample_rays(rng, npix, u.width, n_pix, k[0] % passes)
         k[0] += 1
-        O.ref_trace(u, gx, gy, s, threads=threads)
+        O.ref_trace(u, gx, gy, s, threads=threads, release=True)
         return gx.size
 
     for _ in range(args.warmup):
@@ -228,8 +229,9 @@ def run_reference(args, rank: int) -> None:
             "config": {"workload": scene_name() + "_fixed_h0.4_max2500_f32",
                        "integrator": "the reference's fixed-step RK4, h = 0.4, at most 2500 steps "
                                      "(render/cuda/cuda_backend.cu:35-36)",
-                       "code": "render/cuda/kernels/geodesic_kernel.cu compiled for the host (oracle/_ref), "
-                               "uniforms by the reference's camera and Scene defaults",
+                       "code": "render/cuda/kernels/geodesic_kernel.cu compiled for the host (oracle/_ref) with the "
+                               "reference's Release flags -O3 -ffast-math (CMakeLists.txt:121-122), uniforms by "
+                               "the reference's camera and Scene defaults",
                        "sample_per_step": sample},
             "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": threads, "kind": "reference", "sample": sample},
             "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

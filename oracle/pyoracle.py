@@ -231,7 +231,8 @@ def build_relink() -> Path | None:
 
 
 _lib = None
-_ref = None
+_ref = {}
+REF_RELEASE_LIB = HERE / "_ref" / "libref_host_release.so"
 
 
 def lib() -> C.CDLL:
@@ -247,11 +248,14 @@ def ref_available() -> bool:
     return REF_LIB.exists()
 
 
-def ref_lib() -> C.CDLL:
-    global _ref
-    if _ref is None:
-        _ref = C.CDLL(str(REF_LIB))
-    return _ref
+def ref_lib(release: bool = False) -> C.CDLL:
+    """The reference's kernel source compiled for the host: the exact-flag
+    build (parity pins), or with release=True the reference's own Release
+    flags, -O3 -ffast-math (CMakeLists.txt:121-122; timing)."""
+    key = bool(release)
+    if key not in _ref:
+        _ref[key] = C.CDLL(str(REF_RELEASE_LIB if release else REF_LIB))
+    return _ref[key]
 
 
 def _p(a: np.ndarray | None):
@@ -342,13 +346,13 @@ def ref_render(u, threads: int | None = None) -> np.ndarray:
     return out
 
 
-def ref_trace(u, gx, gy, s, threads: int | None = None) -> np.ndarray:
+def ref_trace(u, gx, gy, s, threads: int | None = None, release: bool = False) -> np.ndarray:
     threads = threads or default_threads()
     gx = np.ascontiguousarray(gx, dtype=np.uint32)
     gy = np.ascontiguousarray(gy, dtype=np.uint32)
     s = np.ascontiguousarray(s, dtype=np.uint32)
     hdr = np.zeros((gx.size, 3), dtype=np.float32)
-    ref_lib().ref_trace_hdr(_u(u), C.c_int64(gx.size), _p(gx), _p(gy), _p(s), _p(hdr), C.c_int(threads))
+    ref_lib(release).ref_trace_hdr(_u(u), C.c_int64(gx.size), _p(gx), _p(gy), _p(s), _p(hdr), C.c_int(threads))
     return hdr
 
 
