@@ -211,8 +211,10 @@ sgx_status sgx_resize(sgx_context* ctx, uint32_t width, uint32_t height);
  * call renders one progressive pass [sample_begin, sample_begin+count); the
  * image is final after the pass that reaches u->supersample. */
 sgx_status sgx_render(sgx_context* ctx, const sgx_uniforms* u, const sgx_render_opts* opts);
-/* capture_frame (cuda_backend.cu:154-166): copies the last image to host
- * memory in `format`; bytes must be width*height*(4 | 16 | 8). */
+/* capture_frame (cuda_backend.cu:154-166): copies the last image sgx_render
+ * made to host memory in `format`; bytes must be width*height*(4 | 16 | 8).
+ * Renders into a caller's buffer (sgx_render_device) leave the context's
+ * image, and what sgx_capture and sgx_bloom see, unchanged. */
 sgx_status sgx_capture(sgx_context* ctx, void* host_out, size_t bytes, uint32_t format);
 /* Counters of the last sgx_render. */
 sgx_status sgx_get_stats(const sgx_context* ctx, sgx_render_stats* out);

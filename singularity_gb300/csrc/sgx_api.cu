@@ -191,7 +191,14 @@ sgx_status render_impl(sgx_context* c, const sgx_uniforms* u, const sgx_render_o
     // An HDR frame into the context's image fuses the bloom extract into its
     // last accumulation pass (sgx_bloom then blurs and composes only).
     c->bloom_ext_valid = false;
-    const bool fuse_ext = format == SGX_FORMAT_RGBA16F_HDR && out == c->d_image && slice.count <= 1u &&
+    // Only a render into the context's own image changes what sgx_capture and
+    // sgx_bloom see; a render into a caller's buffer leaves that state alone.
+    const bool own = out == c->d_image;
+    if (own) {
+        c->frame_valid = false;
+        c->post_valid = false;
+    }
+    const bool fuse_ext = format == SGX_FORMAT_RGBA16F_HDR && own && slice.count <= 1u &&
                           u->width >= 2u && u->height >= 2u;
     if (fuse_ext) {
         const sgx_status bs = sgx_internal::ensure_bloom_targets(c, u->width, u->height);
@@ -245,17 +252,19 @@ sgx_status render_impl(sgx_context* c, const sgx_uniforms* u, const sgx_render_o
         cudaEventElapsedTime(&acc.total_ms, c->ev_begin, c->ev_end);
         done += n;
         c->next_sample = s0 + n;
-        c->frame_valid = finalize;
+        if (own) c->frame_valid = finalize;
         if (finalize && fuse_ext) {
             c->bloom_ext_valid = true;
             c->bloom_ext_threshold = u->bloom_threshold;
         }
     }
-    c->frame_spp = spp;
-    c->frame_format = format;
     c->stats = acc;
-    c->last_u = *u;
-    c->post_valid = false;
+    if (own) {
+        c->frame_spp = spp;
+        c->frame_format = format;
+        c->last_u = *u;
+        c->post_valid = false;
+    }
     return SGX_OK;
 }
 

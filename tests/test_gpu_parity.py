@@ -183,6 +183,37 @@ def test_errors_are_status_codes(renderer, sgx):
     assert img.shape == (8, 8, 4)
 
 
+def test_device_render_leaves_the_context_image_alone(sgx):
+    """sgx_capture and sgx_bloom see only what sgx_render put in the context's
+    image: a render into a caller's buffer through sgx_render_device neither
+    makes a frame capturable nor replaces the frame already there."""
+    import ctypes as C
+    import torch
+    N = sgx._native
+    lib = N.load()
+    cam = sgx.build_orbital_camera(30.0, 0.15, 0.0, 60.0)
+    u = sgx.pack_uniforms(sgx.Scene(render_supersample=2), cam, 24, 16)
+    other = sgx.pack_uniforms(sgx.Scene(render_supersample=2, spin_a_over_M=0.5),
+                              sgx.build_orbital_camera(25.0, 0.4, 1.0, 50.0), 24, 16)
+    dev = torch.zeros(16 * 24 * 4, dtype=torch.uint8, device="cuda")
+    with sgx.Renderer() as r:
+        st = lib.sgx_render_device(r.handle, C.byref(other), C.byref(sgx.default_opts()),
+                                   C.c_void_p(dev.data_ptr()), N.FORMAT_RGBA8_SRGB, None)
+        torch.cuda.synchronize()
+        assert st == N.SGX_OK
+        host = np.empty((16, 24, 4), np.uint8)
+        st = lib.sgx_capture(r.handle, host.ctypes.data_as(C.c_void_p), host.nbytes, N.FORMAT_RGBA8_SRGB)
+        assert st == 4  # SGX_ERR_NOT_RENDERED: no sgx_render yet
+        # a frame of the context, then a device render of another scene of the same size
+        want = r.render_image(u)
+        st = lib.sgx_render_device(r.handle, C.byref(other), C.byref(sgx.default_opts()),
+                                   C.c_void_p(dev.data_ptr()), N.FORMAT_RGBA8_SRGB, None)
+        torch.cuda.synchronize()
+        assert st == N.SGX_OK
+        np.testing.assert_array_equal(r.capture(), want)
+        assert not np.array_equal(dev.cpu().numpy().reshape(16, 24, 4), want)
+
+
 def test_cuda_backend_mirror(sgx):
     """CudaBackend lifecycle and its 1/30 s frame clock (cuda_backend.cu:105-166)."""
     be = sgx.CudaBackend()
