@@ -412,21 +412,23 @@ def hdr_bloom_study(S, N, r, torch, reps: int = 3) -> dict:
             "mrays_s_incl_post": rays / (ms / 1e3) / 1e6}
 
 
-def diff_study(S, N, r, torch, adam_steps: int = 200, fd_eps: float = 1e-3) -> dict:
+def diff_study(S, N, r, torch, adam_steps: int = 200, fd_eps: float = 1e-3, fp32_ck: int = 0) -> dict:
     """Parameter recovery: the differentiable form (emitting-slab disc, soft edges,
     winding fade) at 512x512x4 = 1,048,576 rays; target a = 0.7, i = 60 deg,
     r_in = ISCO(0.7), T-scale 1; guess a = 0.5, i = 50 deg, r_in = 1.2 ISCO(0.5),
     T-scale 0.8; loss = mean squared image error to the FP64 target image.
     grad/s = forward + adjoint per second (synchronous calls, wall clock);
     the adjoints against central differences (eps 1e-3) of the FP64 forward at
-    full size; FP32 against FP64 adjoint; 200 Adam steps from the guess."""
+    full size; FP32 against FP64 adjoint; 200 Adam steps from the guess.
+    fp32_ck: steps between the FP32 form's checkpoints (0: the library's choice)."""
     from singularity_gb300 import diff as D
     W = S.workloads
     base = W.differentiation_base(512, 512, 4)
     tgt = W.differentiation_params(W.differentiation_target())
     guess = W.differentiation_params(W.differentiation_guess())
     dr = D.DiffRenderer(r)
-    o32, o64 = D.DiffOptions(precision=N.PRECISION_FP32), D.DiffOptions(precision=N.PRECISION_FP64)
+    o32 = D.DiffOptions(precision=N.PRECISION_FP32, checkpoint_interval=fp32_ck)
+    o64 = D.DiffOptions(precision=N.PRECISION_FP64)
     target = dr.forward(base, tgt, o64).clone()
     out = {"model": "slab"}
 
@@ -448,6 +450,7 @@ def diff_study(S, N, r, torch, adam_steps: int = 200, fd_eps: float = 1e-3) -> d
             tf.append(t1 - t0)
             tb.append(t2 - t1)
         grads[name] = g
+        out[f"{name}_checkpoint_steps"] = dr.stats()["checkpoint_steps"]
         if name == "fp32":
             out["fp32_forward_ms"] = 1e3 * float(np.median(tf))
             out["fp32_backward_ms"] = 1e3 * float(np.median(tb))
@@ -521,6 +524,8 @@ def main() -> None:
     ap.add_argument("--no-cli-study", action="store_true")
     ap.add_argument("--no-same-algorithm", action="store_true")
     ap.add_argument("--adam-steps", type=int, default=200)
+    ap.add_argument("--diff-checkpoint-interval", type=int, default=0, choices=[0, 10, 64],
+                    help="steps between the FP32 adjoint study's checkpoints (0: the library's choice)")
     ap.add_argument("--rhs-form", type=int, default=0)
     ap.add_argument("--integrator", choices=["adaptive", "fixed"], default="adaptive")
     # the precision form: FP32 bulk with FP64 constants of motion and FP64 step
@@ -696,7 +701,7 @@ def main() -> None:
         if study is not None:
             same["adaptive_steps_per_ray"] = study["mixed_steps_per_ray"]
     hdr = hdr_bloom_study(S, N, r, torch) if single and not args.no_batch_study and adaptive_main else None
-    diff = (diff_study(S, N, r, torch, adam_steps=args.adam_steps)
+    diff = (diff_study(S, N, r, torch, adam_steps=args.adam_steps, fp32_ck=args.diff_checkpoint_interval)
             if single and not args.no_diff_study and adaptive_main else None)
     cli = cli_study() if single and not args.no_cli_study and args.workload == "4k" else None
     cpu = None

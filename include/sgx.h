@@ -381,7 +381,10 @@ typedef struct sgx_diff_opts {
     float half_thickness;  /* slab half-thickness, units of M (0.3) */
     float tau_perp;        /* slab optical depth across (4) */
     uint32_t adjoint_form; /* SGX_DIFF_ADJOINT_REVERSE (default) or SGX_DIFF_ADJOINT_DUAL */
-    uint32_t reserved;
+    uint32_t checkpoint_interval; /* steps between the forward's checkpoints: 0 (default) = 10 for FP32
+                                     with the reverse-pass adjoint when its records fit the form's 16 GiB
+                                     budget (the adjoint keeps its recomputed segment in shared
+                                     memory), else 64 (segment in thread-local memory); or 10 or 64 */
 } sgx_diff_opts;
 void sgx_diff_opts_default(sgx_diff_opts* opts);
 /* Forward pass: renders the form for `params` with size, samples, distance
@@ -389,8 +392,8 @@ void sgx_diff_opts_default(sgx_diff_opts* opts);
  * escape radius, exposure, turbulence, time and the Doppler/redshift flags
  * from `base` (a Kerr uniform block), into d_image (device, W*H*3 floats; NULL:
  * an internal buffer) and keeps what the backward pass needs (a state and
- * transmittance checkpoint every 64 steps, (max_steps/64 + 1) * 7 values per
- * ray).  Synchronous. */
+ * transmittance checkpoint every C = opts->checkpoint_interval steps,
+ * (max_steps/C + 1) * 9 values per ray).  Synchronous. */
 sgx_status sgx_diff_forward(sgx_context* ctx, const sgx_uniforms* base, const sgx_diff_params* params,
                             const sgx_diff_opts* opts, float* d_image, void* stream);
 /* Backward pass of the last forward: d_grad_image (device, W*H*3 floats) is
@@ -400,6 +403,8 @@ sgx_status sgx_diff_backward(sgx_context* ctx, const float* d_grad_image, double
 /* Rays and RK4 steps of the last forward, and (crossing model) how many
  * crossings beyond the 8 recorded per ray were left out of the backward pass. */
 sgx_status sgx_diff_stats(sgx_context* ctx, uint64_t* rays, uint64_t* steps, uint64_t* crossing_overflow);
+/* Steps between the checkpoints of the last forward (10 or 64; 0 before one). */
+uint32_t sgx_diff_checkpoint_steps(const sgx_context* ctx);
 
 /* ---- measurement --------------------------------------------------------- */
 /* No counterpart in the reference: the device's FP32 FMA issue ceiling in

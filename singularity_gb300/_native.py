@@ -135,7 +135,7 @@ class DiffOpts(C.Structure):
     _fields_ = [("struct_size", C.c_uint32), ("precision", C.c_uint32), ("edge_width", C.c_float),
                 ("fade_start", C.c_float), ("fade_width", C.c_float), ("model", C.c_uint32),
                 ("half_thickness", C.c_float), ("tau_perp", C.c_float), ("adjoint_form", C.c_uint32),
-                ("reserved", C.c_uint32)]
+                ("checkpoint_interval", C.c_uint32)]
 
 
 DIFF_MODEL_CROSSING, DIFF_MODEL_SLAB = 0, 1
@@ -186,6 +186,7 @@ SIGNATURES = [
     ("sgx_diff_forward", C.c_int, [_P, C.POINTER(Uniforms), C.POINTER(DiffParams), C.POINTER(DiffOpts), _P, _P]),
     ("sgx_diff_backward", C.c_int, [_P, _P, C.POINTER(C.c_double), _P]),
     ("sgx_diff_stats", C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    ("sgx_diff_checkpoint_steps", C.c_uint32, [_P]),
     ("sgx_measure_fp32_peak", C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
     ("sgx_trace_samples", C.c_int, [_P, C.POINTER(Uniforms), C.POINTER(RenderOpts), C.c_uint64, _U32P, _U32P,
                                     _U32P, _F32P, _U32P, _U32P]),

@@ -12,15 +12,15 @@
 // Parameters: spin a/M, inclination, disc inner radius, temperature scale.
 //
 // Forward: one thread per (pixel, sample) ray.  Each ray stores its state and
-// transmittance every 64 steps (structure-of-arrays checkpoints in HBM,
+// transmittance every 10 or 64 steps (structure-of-arrays checkpoints in HBM,
 // component-major so neighbouring rays write neighbouring words), its last
 // emitting step (slab) or its crossings (crossing model), and its HDR colour;
 // an image kernel averages ACES(hdr * exposure) per pixel.
 //
 // Adjoint: given dLoss/dImage, each ray seeds dLoss/dhdr and sweeps the steps
 // backwards from its last emitting step, one checkpoint segment at a time
-// (the segment's states recomputed from its checkpoint into thread-local
-// memory).  Emission terms go through the transmittance chain with their
+// (the segment's states recomputed from its checkpoint into shared memory
+// for 10-step segments, thread-local memory for 64-step ones).  Emission terms go through the transmittance chain with their
 // local derivatives from dual numbers (sgx_dual.cuh); the adjoint vector is
 // carried through each RK4 step by the hand-derived reverse pass of
 // sgx_adjoint.cuh (or, as a cross-check, by the step's Jacobian built with
@@ -78,6 +78,12 @@ sgx_status sgx_diff_forward(sgx_context* c, const sgx_uniforms* base, const sgx_
         return fail(c, SGX_ERR_INVALID_ARGUMENT, "edge_width and fade_width must be positive");
     if (o.adjoint_form != SGX_DIFF_ADJOINT_REVERSE && o.adjoint_form != SGX_DIFF_ADJOINT_DUAL)
         return fail(c, SGX_ERR_INVALID_ARGUMENT, "unknown adjoint_form");
+    if (o.checkpoint_interval != 0u && o.checkpoint_interval != std::uint32_t(kCkDense) &&
+        o.checkpoint_interval != std::uint32_t(kCkSparse))
+        return fail(c, SGX_ERR_INVALID_ARGUMENT, "checkpoint_interval must be 0 (automatic), 10 or 64");
+    const bool dense_ok = o.precision == SGX_PRECISION_FP32 && o.adjoint_form == SGX_DIFF_ADJOINT_REVERSE;
+    if (o.checkpoint_interval == std::uint32_t(kCkDense) && !dense_ok)
+        return fail(c, SGX_ERR_UNSUPPORTED, "10-step checkpoints apply to FP32 with the reverse-pass adjoint");
     if (o.model == SGX_DIFF_MODEL_SLAB && !(o.half_thickness > 0.0f && o.tau_perp > 0.0f))
         return fail(c, SGX_ERR_INVALID_ARGUMENT, "half_thickness and tau_perp must be positive");
     if (!(params->spin >= 0.0 && params->spin < 1.0) || !(params->incl > 0.0 && params->incl < 3.14159265) ||
@@ -90,12 +96,22 @@ sgx_status sgx_diff_forward(sgx_context* c, const sgx_uniforms* base, const sgx_
     st.valid = false;
     const std::uint32_t spp = base->supersample < 1u ? 1u : (base->supersample > 1024u ? 1024u : base->supersample);
     st.n = std::uint64_t(base->width) * base->height * spp;
-    st.slots = base->max_steps / kCk + 1;
     st.precision = o.precision;
     st.nx = o.model == SGX_DIFF_MODEL_SLAB ? 1u : std::uint32_t(kMaxCross);
-    const std::size_t need = o.precision == SGX_PRECISION_FP64 ? state_bytes<double>(st.n, st.slots, spp, st.nx)
-                                                               : state_bytes<float>(st.n, st.slots, spp, st.nx);
-    if (need > c->workspace_budget * 4)
+    auto bytes_for = [&](std::uint32_t ck) {
+        const std::uint32_t slots = base->max_steps / ck + 1;
+        return o.precision == SGX_PRECISION_FP64 ? state_bytes<double>(st.n, slots, spp, st.nx)
+                                                 : state_bytes<float>(st.n, slots, spp, st.nx);
+    };
+    const std::size_t limit = c->workspace_budget * 4;
+    std::uint32_t ck = o.checkpoint_interval;
+    if (ck == 0u)
+        ck = dense_ok && bytes_for(std::uint32_t(kCkDense)) <= limit ? std::uint32_t(kCkDense)
+                                                                      : std::uint32_t(kCkSparse);
+    st.ck = ck;
+    st.slots = base->max_steps / ck + 1;
+    const std::size_t need = bytes_for(ck);
+    if (need > limit)
         return fail(c, SGX_ERR_INVALID_ARGUMENT, "differentiable render needs " + std::to_string(need >> 20) +
                                                      " MiB of records: fewer rays or max_steps");
     if (st.cap < need) {
@@ -165,6 +181,10 @@ sgx_status sgx_diff_stats(sgx_context* c, uint64_t* rays, uint64_t* steps, uint6
     if (steps != nullptr) *steps = h[1];
     if (crossing_overflow != nullptr) *crossing_overflow = h[0];
     return SGX_OK;
+}
+
+uint32_t sgx_diff_checkpoint_steps(const sgx_context* c) {
+    return c != nullptr && c->diff != nullptr && c->diff->valid ? c->diff->ck : 0u;
 }
 
 }  // extern "C"

@@ -25,7 +25,16 @@ namespace {
 
 using namespace sgxd;
 
-constexpr int kCk = 64;       // steps between checkpoints
+// Steps between checkpoints.  Sparse (64): the adjoint recomputes each
+// segment into thread-local memory (65 states, 2.3 KB a thread, which streams
+// through L2 and DRAM).  Dense (10): the 11 states of a segment fit in shared
+// memory for 16 resident warps per SM (11 x 9 values x 4 B x 128 threads =
+// 50.7 KB a block, four blocks), at 6.4x the checkpoint bytes.  FP32 with the
+// hand-derived reverse pass takes the dense form when its records fit the
+// form's memory budget, everything else the sparse one.
+constexpr int kCkSparse = 64;
+constexpr int kCkDense = 10;
+constexpr int kBackwardThreads = 128;
 constexpr int kMaxCross = 8;  // crossings recorded per ray (crossing model)
 constexpr int NS = 8;         // state: r, theta, phi, p_r, p_theta, psi (swept angle), sin(theta), cos(theta)
 constexpr int NC = NS + 1;    // checkpoint: state and transmittance
@@ -380,9 +389,9 @@ __device__ __forceinline__ void ray_pixel(const DiffConst<T>& k, std::uint64_t i
     gx = std::uint32_t(pix - std::uint64_t(gy) * k.width);
 }
 
-template <class T>
+template <class T, int CK>
 __device__ __forceinline__ void store_ckpt(const DiffBufs<T>& b, std::uint64_t id, std::uint32_t n, const T* y, T tau) {
-    const std::uint64_t base = std::uint64_t(n / kCk) * NC * b.n + id;
+    const std::uint64_t base = std::uint64_t(n / CK) * NC * b.n + id;
 #pragma unroll
     for (int i = 0; i < NS; ++i) b.ckpt[base + std::uint64_t(i) * b.n] = y[i];
     b.ckpt[base + std::uint64_t(NS) * b.n] = tau;
@@ -390,7 +399,7 @@ __device__ __forceinline__ void store_ckpt(const DiffBufs<T>& b, std::uint64_t i
 
 // Forward: one thread per ray.  SLAB: emission and absorption every step in
 // the layer; otherwise soft crossings of the equatorial plane.
-template <class T, bool SLAB>
+template <class T, bool SLAB, int CK>
 __global__ void __launch_bounds__(128) diff_forward_kernel(DiffConst<T> k, DiffParamsT<T> p, DiffBufs<T> b) {
     const std::uint64_t id = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     std::uint32_t n = 0;
@@ -409,7 +418,7 @@ __global__ void __launch_bounds__(128) diff_forward_kernel(DiffConst<T> k, DiffP
 #pragma unroll
             for (int i = 0; i < NS; ++i) prev[i] = y[i];
             for (; n < k.max_steps; ++n) {
-                if (!SLAB && n % kCk == 0) store_ckpt(b, id, n, y, tau);
+                if (!SLAB && n % CK == 0) store_ckpt<T, CK>(b, id, n, y, tau);
                 if (!isfinite(y[0]) || y[0] < hcut) break;
                 if (y[0] > k.escape_r) break;
                 if constexpr (SLAB) {
@@ -423,7 +432,7 @@ __global__ void __launch_bounds__(128) diff_forward_kernel(DiffConst<T> k, DiffP
                         ++nc;
                         last = n;
                     }
-                    if (n % kCk == 0) store_ckpt(b, id, n, y, tau);
+                    if (n % CK == 0) store_ckpt<T, CK>(b, id, n, y, tau);
                 } else {
                     const T mid = T(1.5707963267948966);
                     if (disc && n > 0 && ((prev[1] - mid) * (y[1] - mid) < T(0))) {
@@ -539,10 +548,19 @@ __device__ __forceinline__ void step_adjoint(const T* yp, T E, T L, T a, const D
 }
 
 // Adjoint: one thread per ray, a reverse sweep from the ray's last emitting
-// step to the camera, one checkpoint segment at a time.
-template <class T, bool SLAB, bool DUALJ>
-__global__ void __launch_bounds__(128, 4) diff_backward_kernel(DiffConst<T> k, DiffParamsT<T> p, DiffBufs<T> b,
-                                                            const float* __restrict__ gimg) {
+// step to the camera, one checkpoint segment at a time.  CK = kCkDense keeps
+// the recomputed segment in dynamic shared memory, (CK + 1) * NC values a
+// thread laid out [slot][value][thread] (consecutive threads, consecutive
+// words); CK = kCkSparse in a thread-local array.  Launched with
+// kBackwardThreads threads a block.
+template <class T, bool SLAB, bool DUALJ, int CK>
+__global__ void __launch_bounds__(kBackwardThreads, 4)
+    diff_backward_kernel(DiffConst<T> k, DiffParamsT<T> p, DiffBufs<T> b, const float* __restrict__ gimg) {
+    constexpr bool SHARED = CK == kCkDense;
+    extern __shared__ __align__(16) unsigned char diff_seg_raw[];
+    // value v of slot j of this thread's segment (shared form)
+    T* const seg = reinterpret_cast<T*>(diff_seg_raw) + threadIdx.x;
+    auto at = [](int j, int v) { return (j * NC + v) * kBackwardThreads; };
     const std::uint64_t id = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (id >= b.n) return;
     double* gout = b.grads;
@@ -572,7 +590,7 @@ __global__ void __launch_bounds__(128, 4) diff_backward_kernel(DiffConst<T> k, D
     T lam[NS] = {};
     T muE = T(0), muL = T(0), mua = T(0), g_a = T(0), g_rin = T(0), g_ts = T(0);
     const bool fade = k.fade != 0u;
-    T Y[kCk + 1][NS];
+    [[maybe_unused]] T Y[SHARED ? 1 : CK + 1][NS];
 
     // Crossing model: seeds of the transmittance chain
     //   colour = sum_j tau_j w_j c_j,  tau_{j+1} = tau_j (1 - w_j):
@@ -601,31 +619,72 @@ __global__ void __launch_bounds__(128, 4) diff_backward_kernel(DiffConst<T> k, D
     }
     // Slab model: the same chain over every emitting step, R carried through the sweep.
     T R[3] = {T(0), T(0), T(0)};
-    T tb[kCk + 1];
+    [[maybe_unused]] T tb[SHARED ? 1 : CK + 1];
 
-    const int mlast = int((klast - 1) / kCk);
+    const int mlast = int((klast - 1) / CK);
     for (int m = mlast; m >= 0; --m) {
-        const std::uint32_t kbeg = std::uint32_t(m) * kCk;
-        const std::uint32_t kend = (kbeg + kCk < klast) ? kbeg + kCk : klast;
+        const std::uint32_t kbeg = std::uint32_t(m) * CK;
+        const std::uint32_t kend = (kbeg + CK < klast) ? kbeg + CK : klast;
         const std::uint64_t cb = std::uint64_t(m) * NC * b.n + id;
-#pragma unroll
-        for (int i = 0; i < NS; ++i) Y[0][i] = b.ckpt[cb + std::uint64_t(i) * b.n];
         T tau = b.ckpt[cb + std::uint64_t(NS) * b.n];
-        for (std::uint32_t kk = kbeg + 1; kk <= kend; ++kk) {
-            const T* yp = Y[kk - 1 - kbeg];
-            T* yc = Y[kk - kbeg];
-            step_g<T, T>(yp, E, L, a, k.M, k.h, fade, yc);
-            if constexpr (SLAB) {
-                tb[kk - kbeg] = tau;  // transmittance before step kk's emission
-                T col[3], alpha;
-                if (slab_g<T, T>(yp[0], yp[1], yp[2], yc[0], yc[1], yc[2], yc[5], yc[6], yc[7], L, a, r_in,
-                                 p.t_scale, k, col, alpha))
-                    tau = tau * (T(1) - alpha);
+        if constexpr (SHARED) {
+            // the running state in registers, each state stored once
+            T yc[NS];
+#pragma unroll
+            for (int i = 0; i < NS; ++i) {
+                yc[i] = b.ckpt[cb + std::uint64_t(i) * b.n];
+                seg[at(0, i)] = yc[i];
+            }
+            for (std::uint32_t kk = kbeg + 1; kk <= kend; ++kk) {
+                const int j = int(kk - kbeg);
+                T yn[NS];
+                step_g<T, T>(yc, E, L, a, k.M, k.h, fade, yn);
+                if constexpr (SLAB) {
+                    seg[at(j, NS)] = tau;  // transmittance before step kk's emission
+                    T col[3], alpha;
+                    if (slab_g<T, T>(yc[0], yc[1], yc[2], yn[0], yn[1], yn[2], yn[5], yn[6], yn[7], L, a, r_in,
+                                     p.t_scale, k, col, alpha))
+                        tau = tau * (T(1) - alpha);
+                }
+#pragma unroll
+                for (int i = 0; i < NS; ++i) {
+                    seg[at(j, i)] = yn[i];
+                    yc[i] = yn[i];
+                }
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < NS; ++i) Y[0][i] = b.ckpt[cb + std::uint64_t(i) * b.n];
+            for (std::uint32_t kk = kbeg + 1; kk <= kend; ++kk) {
+                const T* yp = Y[kk - 1 - kbeg];
+                T* yc = Y[kk - kbeg];
+                step_g<T, T>(yp, E, L, a, k.M, k.h, fade, yc);
+                if constexpr (SLAB) {
+                    tb[kk - kbeg] = tau;  // transmittance before step kk's emission
+                    T col[3], alpha;
+                    if (slab_g<T, T>(yp[0], yp[1], yp[2], yc[0], yc[1], yc[2], yc[5], yc[6], yc[7], L, a, r_in,
+                                     p.t_scale, k, col, alpha))
+                        tau = tau * (T(1) - alpha);
+                }
             }
         }
         for (std::uint32_t kk = kend; kk > kbeg; --kk) {
-            const T* yp = Y[kk - 1 - kbeg];
-            const T* yc = Y[kk - kbeg];
+            const int j = int(kk - kbeg);
+            [[maybe_unused]] T ypr[NS], ycr[NS];
+            const T* yp;
+            const T* yc;
+            if constexpr (SHARED) {
+#pragma unroll
+                for (int i = 0; i < NS; ++i) {
+                    ypr[i] = seg[at(j - 1, i)];
+                    ycr[i] = seg[at(j, i)];
+                }
+                yp = ypr;
+                yc = ycr;
+            } else {
+                yp = Y[j - 1];
+                yc = Y[j];
+            }
             T pend[NS] = {};
             using D = Dual<T, 11>;
             using DA = Dual<T, 10>;
@@ -644,7 +703,9 @@ __global__ void __launch_bounds__(128, 4) diff_backward_kernel(DiffConst<T> k, D
                     DC col[3];
                     slab_colour_g<DC, T>(DC::var(yc[0], 0), DC::var(yc[2], 1), DC::var(L, 2), DC::var(a, 3),
                                          DC::var(r_in, 4), DC::var(p.t_scale, 5), k, col);
-                    const T tj = tb[kk - kbeg];
+                    T tj;
+                    if constexpr (SHARED) tj = seg[at(j, NS)];
+                    else tj = tb[j];
                     const T gcs = tj * alv;
                     const T gal = tj * (g[0] * (colv[0] - R[0]) + g[1] * (colv[1] - R[1]) + g[2] * (colv[2] - R[2]));
 #pragma unroll
@@ -797,6 +858,7 @@ struct sgx_diff_state {
     std::size_t cap = 0;
     std::uint64_t n = 0;
     std::uint32_t slots = 0;
+    std::uint32_t ck = kCkSparse;  // steps between checkpoints (kCkSparse or kCkDense)
     std::uint32_t precision = SGX_PRECISION_FP32;
     std::uint32_t nx = kMaxCross;  // crossing records per ray (1 for the slab model)
     sgx_uniforms u{};
@@ -855,10 +917,16 @@ cudaError_t run_forward(sgx_diff_state& st, float* img, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(b.overflow, 0, 16, s);
     if (e != cudaSuccess) return e;
     offsets_kernel<T><<<(k.spp + 127) / 128, 128, 0, s>>>(k.spp, const_cast<T*>(b.ox), const_cast<T*>(b.oy));
-    if (st.o.model == SGX_DIFF_MODEL_SLAB)
-        diff_forward_kernel<T, true><<<unsigned((st.n + 127) / 128), 128, 0, s>>>(k, p, b);
-    else
-        diff_forward_kernel<T, false><<<unsigned((st.n + 127) / 128), 128, 0, s>>>(k, p, b);
+    const unsigned grid = unsigned((st.n + 127) / 128);
+    const bool slab = st.o.model == SGX_DIFF_MODEL_SLAB;
+    bool dense = false;
+    if constexpr (sizeof(T) == 4) dense = st.ck == std::uint32_t(kCkDense);
+    if constexpr (sizeof(T) == 4) {
+        if (dense && slab) diff_forward_kernel<T, true, kCkDense><<<grid, 128, 0, s>>>(k, p, b);
+        else if (dense) diff_forward_kernel<T, false, kCkDense><<<grid, 128, 0, s>>>(k, p, b);
+    }
+    if (!dense && slab) diff_forward_kernel<T, true, kCkSparse><<<grid, 128, 0, s>>>(k, p, b);
+    else if (!dense) diff_forward_kernel<T, false, kCkSparse><<<grid, 128, 0, s>>>(k, p, b);
     const std::uint64_t npix = std::uint64_t(k.width) * k.height;
     diff_image_kernel<T><<<unsigned((npix + 255) / 256), 256, 0, s>>>(k, b, img);
     return cudaGetLastError();
@@ -869,12 +937,27 @@ cudaError_t run_backward(sgx_diff_state& st, const float* gimg, double* d_out4, 
     const DiffConst<T> k = make_const<T>(st.u, st.o);
     const DiffParamsT<T> p{T(st.p.spin), T(st.p.incl), T(st.p.r_in), T(st.p.t_scale)};
     DiffBufs<T> b = carve_bufs<T>(st, k.spp);
-    const unsigned grid = unsigned((st.n + 127) / 128);
+    const unsigned grid = unsigned((st.n + kBackwardThreads - 1) / kBackwardThreads);
     const bool slab = st.o.model == SGX_DIFF_MODEL_SLAB, dual = st.o.adjoint_form == SGX_DIFF_ADJOINT_DUAL;
-    if (slab && !dual) diff_backward_kernel<T, true, false><<<grid, 128, 0, s>>>(k, p, b, gimg);
-    else if (slab) diff_backward_kernel<T, true, true><<<grid, 128, 0, s>>>(k, p, b, gimg);
-    else if (!dual) diff_backward_kernel<T, false, false><<<grid, 128, 0, s>>>(k, p, b, gimg);
-    else diff_backward_kernel<T, false, true><<<grid, 128, 0, s>>>(k, p, b, gimg);
+    bool dense = false;
+    if constexpr (sizeof(T) == 4) {
+        // the dense checkpoints pair with the hand-derived reverse pass only
+        dense = st.ck == std::uint32_t(kCkDense);
+        if (dense) {
+            const int smem = (kCkDense + 1) * NC * kBackwardThreads * int(sizeof(T));
+            auto* kern = slab ? diff_backward_kernel<T, true, false, kCkDense>
+                              : diff_backward_kernel<T, false, false, kCkDense>;
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e != cudaSuccess) return e;
+            kern<<<grid, kBackwardThreads, smem, s>>>(k, p, b, gimg);
+        }
+    }
+    if (!dense) {
+        if (slab && !dual) diff_backward_kernel<T, true, false, kCkSparse><<<grid, kBackwardThreads, 0, s>>>(k, p, b, gimg);
+        else if (slab) diff_backward_kernel<T, true, true, kCkSparse><<<grid, kBackwardThreads, 0, s>>>(k, p, b, gimg);
+        else if (!dual) diff_backward_kernel<T, false, false, kCkSparse><<<grid, kBackwardThreads, 0, s>>>(k, p, b, gimg);
+        else diff_backward_kernel<T, false, true, kCkSparse><<<grid, kBackwardThreads, 0, s>>>(k, p, b, gimg);
+    }
     const std::uint32_t nchunks = std::uint32_t((st.n + 1023) / 1024);
     double* part = reinterpret_cast<double*>(reinterpret_cast<unsigned char*>(b.overflow) + 256);
     reduce_chunks<<<dim3(nchunks, 4), 256, 0, s>>>(b.grads, st.n, part, nchunks);

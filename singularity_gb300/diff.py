@@ -32,7 +32,8 @@ PARAM_NAMES = ("spin", "incl", "r_in", "t_scale")
 class DiffOptions:
     """Options of the form (sgx_diff_opts): FP32 or FP64, disc model (emitting
     slab or equatorial crossings), soft edge width (M), winding fade (rad),
-    slab half-thickness (M) and optical depth across."""
+    slab half-thickness (M) and optical depth across, adjoint form, steps
+    between the forward's checkpoints."""
     precision: int = N.PRECISION_FP32
     edge_width: float = 0.1
     fade_start: float = 0.625 * math.pi
@@ -41,6 +42,7 @@ class DiffOptions:
     half_thickness: float = 0.3
     tau_perp: float = 4.0
     adjoint_form: int = N.DIFF_ADJOINT_REVERSE
+    checkpoint_interval: int = 0  # 0: automatic (10 for FP32 reverse-pass adjoints that fit, else 64)
 
     def to_c(self) -> N.DiffOpts:
         o = N.DiffOpts()
@@ -53,6 +55,7 @@ class DiffOptions:
         o.half_thickness = self.half_thickness
         o.tau_perp = self.tau_perp
         o.adjoint_form = self.adjoint_form
+        o.checkpoint_interval = self.checkpoint_interval
         return o
 
     def oracle_form(self) -> dict:
@@ -110,7 +113,8 @@ class DiffRenderer:
     def stats(self):
         rays, steps, over = C.c_uint64(), C.c_uint64(), C.c_uint64()
         self._r._check(self._lib.sgx_diff_stats(self._r.handle, C.byref(rays), C.byref(steps), C.byref(over)))
-        return {"rays": rays.value, "steps": steps.value, "crossing_overflow": over.value}
+        return {"rays": rays.value, "steps": steps.value, "crossing_overflow": over.value,
+                "checkpoint_steps": int(self._lib.sgx_diff_checkpoint_steps(self._r.handle))}
 
 
 def _autograd_fn():

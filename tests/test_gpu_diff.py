@@ -141,6 +141,41 @@ def test_reverse_pass_matches_dual_jacobians(diff, sgx, prec, model):
     assert np.all(rel <= (1e-9 if prec == 2 else 1e-4)), rel
 
 
+@pytest.mark.parametrize("model", [1, 0])
+def test_dense_and_sparse_checkpoints_agree(diff, sgx, model):
+    """FP32 adjoint from 10-step checkpoints (segment recomputed into shared
+    memory) against 64-step checkpoints (thread-local segment): the same
+    recomputed states and reverse pass, so the same gradient to rounding."""
+    from singularity_gb300 import diff as D
+    base, tgt, guess = _setup(sgx, 48, 32, 2)
+    target = diff.forward(base, tgt, D.DiffOptions(model=model)).clone()
+    out = []
+    for ck in (10, 64):
+        img = diff.forward(base, guess, D.DiffOptions(model=model, checkpoint_interval=ck))
+        assert diff.stats()["checkpoint_steps"] == ck
+        out.append(diff.backward(_loss_grad_image(img, target)))
+    rel = np.abs(out[0] - out[1]) / np.abs(out[1])
+    print(f"model {model}: 10-step {out[0]} 64-step {out[1]} rel {rel} identical {np.array_equal(out[0], out[1])}")
+    assert np.all(rel <= 1e-6), rel
+
+
+def test_checkpoint_interval_options(diff, sgx):
+    from singularity_gb300 import diff as D
+    N = sgx._native
+    base, tgt, guess = _setup(sgx, 16, 16, 1)
+    for bad in (D.DiffOptions(checkpoint_interval=7),
+                D.DiffOptions(checkpoint_interval=10, precision=N.PRECISION_FP64),
+                D.DiffOptions(checkpoint_interval=10, adjoint_form=N.DIFF_ADJOINT_DUAL)):
+        with pytest.raises(sgx.SgxError):
+            diff.forward(base, guess, bad)
+    # automatic: 10 for FP32 with the reverse pass (records fit the budget), else 64
+    for ok, want in ((D.DiffOptions(), 10), (D.DiffOptions(precision=N.PRECISION_FP64), 64),
+                     (D.DiffOptions(checkpoint_interval=64, precision=N.PRECISION_FP64), 64),
+                     (D.DiffOptions(adjoint_form=N.DIFF_ADJOINT_DUAL), 64)):
+        diff.forward(base, guess, ok)
+        assert diff.stats()["checkpoint_steps"] == want
+
+
 def test_backward_is_deterministic(diff, sgx):
     import torch
     base, tgt, guess = _setup(sgx, 40, 30, 2)
