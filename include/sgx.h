@@ -74,9 +74,9 @@ typedef struct sgx_render_opts {
     uint32_t sample_begin;   /* first Halton sample of this pass (default 0) */
     uint32_t sample_count;   /* samples in this pass; 0 = all remaining (default 0) */
     uint32_t block_threads;  /* launch shape: threads per block, a multiple of 32 up to 256;
-                                0 = tuned default */
+                                0 = tuned default (64) */
     uint32_t blocks_per_sm;  /* launch shape: resident blocks per SM; 0 = occupancy limit */
-    uint32_t refill_interval;/* steps between warp refills of finished rays; 0 = 32 */
+    uint32_t refill_interval;/* steps between warp refills of finished rays; 0 = 128 */
     uint32_t rhs_form;       /* Kerr right-hand side: 0 = the same Hamiltonian in Carter's
                                     separated form, three reciprocals (default),
                                 1 = the reference's division-for-division form,
@@ -298,7 +298,7 @@ sgx_status sgx_batch_output(const sgx_batch* b, const void** d_frames, uint64_t*
 sgx_status sgx_batch_capture(sgx_batch* b, uint32_t view, void* host_out, size_t bytes);
 void sgx_batch_destroy(sgx_batch* b);
 /* Launch-shape autotuner: times every combination of threads per block
- * {128, 256}, refill interval {4, 8, 16, 32} and ray-order tile {rows, 8x4,
+ * {64, 128, 256}, refill interval {16, 32, 64, 128} and ray-order tile {rows, 8x4,
  * 16x8, 32x2} on the views with samples capped at sample_cap (0: 4) and writes
  * the fastest into *best (other fields from base); *best_ms gets its time. */
 sgx_status sgx_autotune(sgx_context* ctx, const sgx_uniforms* views, uint32_t n, const sgx_render_opts* base,

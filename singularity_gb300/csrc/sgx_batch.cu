@@ -305,8 +305,8 @@ sgx_status sgx_autotune(sgx_context* c, const sgx_uniforms* views, uint32_t n, c
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(tb.d_u, capped.data(), n * sizeof(sgx_uniforms), cudaMemcpyHostToDevice, c->stream);
 
-    static const std::uint32_t kThreads[] = {128, 256};
-    static const std::uint32_t kRefill[] = {4, 8, 16, 32};
+    static const std::uint32_t kThreads[] = {64, 128, 256};
+    static const std::uint32_t kRefill[] = {16, 32, 64, 128};
     static const std::uint32_t kTiles[][2] = {{0, 0}, {8, 4}, {16, 8}, {32, 2}};
     float best_t = 1e30f;
     sgx_render_opts best_o = o;

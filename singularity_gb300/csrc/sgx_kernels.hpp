@@ -65,9 +65,16 @@ __host__ __device__ inline std::uint32_t slice_row(std::uint32_t band, std::uint
     return (b * count + index) * band + (l - b * band);
 }
 
-// Steps between warp refills when the caller leaves it to the library: the
-// 4K Kerr pass runs 1.6 % faster at 32 than at 16 (64: within 1 %; 8: 4 % slower).
-constexpr std::uint32_t kDefaultRefill = 32;
+// Launch shape when the caller leaves it to the library.  A refill runs the
+// per-ray set-up (camera ray, constants of motion, photon-orbit radius, first
+// right-hand side) once per warp for however many lanes are idle, so refilling
+// every 128 steps instead of every 32 amortises it over more lanes: on the 4K
+// Kerr pass (error-controlled, mixed) the trace kernel takes 47.7 ms at
+// 64-thread blocks and refill 128 against 49.7 ms at 256 and 32 (96 and 192:
+// within 0.1 ms of 128; 1080p: 12.59 against 13.10 ms; the fixed step 188.6
+// against 192.4 ms); 64-thread blocks are 0.3-1 % faster than 128 or 256.
+constexpr std::uint32_t kDefaultRefill = 128;
+constexpr int kDefaultBlockThreads = 64;
 constexpr std::uint32_t kMaxLaunchViews = 128;
 constexpr std::uint32_t kMaxPassSamplesHost = 1024;
 

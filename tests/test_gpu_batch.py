@@ -107,7 +107,7 @@ def test_autotune_picks_a_valid_shape(renderer, sgx):
     views = _views(sgx, seed=11, n=8, small=False)
     base = sgx.default_opts(integrator=1)
     best, ms = sgx.autotune(renderer, views, base, sample_cap=2)
-    assert ms > 0 and best.block_threads in (128, 256) and best.refill_interval in (4, 8, 16, 32)
+    assert ms > 0 and best.block_threads in (64, 128, 256) and best.refill_interval in (16, 32, 64, 128)
     assert (best.tile_w, best.tile_h) in ((0, 0), (8, 4), (16, 8), (32, 2))
     assert best.integrator == 1
     b = sgx.Batch(renderer, views[:3], best)
