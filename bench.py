@@ -671,12 +671,12 @@ def main() -> None:
     lib.sgx_measure_fp32_peak(local, 20000, C.byref(peak))
     # DRAM bytes of the trace kernel per launch from one ncu capture of a full
     # 4K 16-spp launch of the adaptive precision form (dram__bytes_read.sum +
-    # dram__bytes_write.sum = 2,089,191,680 B for 132,710,400 rays: the 16-byte
+    # dram__bytes_write.sum = 2,089,134,848 B for 132,710,400 rays: the 16-byte
     # hit record per ray, part of it still in L2 when the kernel ends), scaled
     # by this rank's rays; other workloads: null
     traffic = None
     if args.integrator == "adaptive" and args.workload == "4k" and args.precision == "mixed":
-        traffic = 2089191680 / 132710400 * u.width * rows * SPP_PER_STEP
+        traffic = 2089134848 / 132710400 * u.width * rows * SPP_PER_STEP
     roof = {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
             "frac": achieved / peak.value if peak.value else None, "traffic": traffic,
             "peak_source": "of measured: register-resident FMA ceiling (sgx_measure_fp32_peak) on this GPU; "
