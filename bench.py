@@ -455,6 +455,17 @@ def diff_study(S, N, r, torch, adam_steps: int = 200, fd_eps: float = 1e-3, fp32
             out["fp32_forward_ms"] = 1e3 * float(np.median(tf))
             out["fp32_backward_ms"] = 1e3 * float(np.median(tb))
         out[f"{name}_grad_per_s"] = 1.0 / (float(np.median(tf)) + float(np.median(tb)))
+    if out["fp32_checkpoint_steps"] != 64:
+        # config 5 names checkpoints every 64 steps: that form's rate beside the default's
+        o64ck = D.DiffOptions(precision=N.PRECISION_FP32, checkpoint_interval=64)
+        dr.backward(loss_grad(dr.forward(base, guess, o64ck)))  # warm
+        ts = []
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            dr.backward(loss_grad(dr.forward(base, guess, o64ck)))
+            ts.append(time.perf_counter() - t0)
+        out["fp32_ck64_grad_per_s"] = 1.0 / float(np.median(ts))
     fd = np.zeros(4)
     for k in range(4):
         lp, lm = [], []
