@@ -74,7 +74,7 @@ typedef struct sgx_render_opts {
     uint32_t sample_begin;   /* first Halton sample of this pass (default 0) */
     uint32_t sample_count;   /* samples in this pass; 0 = all remaining (default 0) */
     uint32_t block_threads;  /* launch shape: threads per block, a multiple of 32 up to 256;
-                                0 = tuned default (64) */
+                                0 = tuned default (64 for one view, 128 for a batch) */
     uint32_t blocks_per_sm;  /* launch shape: resident blocks per SM; 0 = occupancy limit */
     uint32_t refill_interval;/* steps between warp refills of finished rays; 0 = 128 */
     uint32_t rhs_form;       /* Kerr right-hand side: 0 = the same Hamiltonian in Carter's

@@ -852,7 +852,8 @@ cudaError_t run_kernel(const PassDesc& pass, LaunchShape shape, const void* h_vi
     cudaGetDevice(&dev);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int threads = shape.block_threads > 0 ? shape.block_threads : kDefaultBlockThreads;
+    const int threads = shape.block_threads > 0 ? shape.block_threads
+                                                : (ONE ? kDefaultBlockThreads : kDefaultBlockThreadsMulti);
     int per_sm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
     if (e != cudaSuccess) return e;
