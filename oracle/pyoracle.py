@@ -9,9 +9,8 @@ this module, and only as the checker.  It loads:
   for the host CPU (``make -C oracle ref``), present only where the reference
   sources are.
 
-Where the reference sources are: ``reference_root()`` — the directory named by
-the environment variable SGX_REFERENCE_ROOT; else the reference checkout of
-this build environment, /root/reference; else the snapshot
+Where the reference sources are: ``reference_root()`` — the checkout named by
+the environment variable SGX_REFERENCE_ROOT; else the snapshot
 ``oracle/_ref/src`` that ``make -C oracle snapshot`` leaves beside the
 builds (the reference files the recipes compile, so that a machine without the
 checkout, such as the GPU host, can build them).
@@ -31,7 +30,6 @@ HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libref_host.so"
 SNAPSHOT = HERE / "_ref" / "src"
-_CHECKOUT = Path("/root/reference")  # the reference checkout of this build environment
 
 
 def _has_sources(root: Path) -> bool:
@@ -39,11 +37,10 @@ def _has_sources(root: Path) -> bool:
 
 
 def reference_checkout() -> Path | None:
-    """A full checkout of the reference, if this machine has one."""
+    """The full checkout of the reference named by SGX_REFERENCE_ROOT, if any."""
     env = os.environ.get("SGX_REFERENCE_ROOT")
-    for root in ([Path(env)] if env else []) + [_CHECKOUT]:
-        if _has_sources(root):
-            return root
+    if env and _has_sources(Path(env)):
+        return Path(env)
     return None
 
 

@@ -1,7 +1,7 @@
 """Generate the committed golden fixtures from the reference tree.
 
-Run where a full reference checkout is (oracle.pyoracle.reference_checkout():
-$SGX_REFERENCE_ROOT, else the build environment's checkout).  Nothing at test
+Run where a full reference checkout is, named by $SGX_REFERENCE_ROOT
+(oracle.pyoracle.reference_checkout()).  Nothing at test
 time reads the reference tree; the tests read only the files this script
 writes:
 
