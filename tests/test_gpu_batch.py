@@ -164,3 +164,27 @@ def test_batch_near_field_cameras_match_single_views(renderer, sgx, precision):
         assert (got[..., :3].max(axis=-1) > 3).mean() > 0.1  # not a black frame
         _assert_parity(got, renderer.render_image(v, opts), f"near view {i}")
     b.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batch_launch_shape_does_not_change_the_frames(renderer, sgx, precision):
+    """Threads per block, refill interval and ray-order tiles decide only which
+    warp traces which ray of which view: every view's frame is bit-identical
+    across launch shapes (the autotuner's choice changes speed, not pixels)."""
+    N = sgx._native
+    views = _views(sgx, seed=13, n=5)
+    frames = None
+    for shape in (dict(), dict(block_threads=256, refill_interval=32), dict(block_threads=64, refill_interval=16,
+                                                                           tile_w=8, tile_h=4),
+                  dict(block_threads=128, refill_interval=1000, tile_w=32, tile_h=2), dict(block_threads=96)):
+        b = sgx.Batch(renderer, views, sgx.default_opts(integrator=1, precision=precision, **shape),
+                      fmt=N.FORMAT_RGBA32F)
+        b.launch()
+        b.wait()
+        got = [b.capture(i) for i in range(len(views))]
+        b.close()
+        if frames is None:
+            frames = got
+        else:
+            for i in range(len(views)):
+                np.testing.assert_array_equal(got[i], frames[i], err_msg=f"{shape} view {i}")
