@@ -641,6 +641,8 @@ def main() -> None:
                                        N.FORMAT_RGBA8_SRGB, C.c_void_p(stream.cuda_stream))
             if st != 0:
                 raise RuntimeError(lib.sgx_last_error(r.handle).decode())
+            # the collective runs behind torch's current stream: order it after the render
+            torch.cuda.current_stream().wait_stream(stream)
             frame = D.gather_frame(d_slice.view(rows, u.width, 4), u.height, SLICE_BAND)
             if rank == 0:
                 host.copy_(frame.reshape(-1))

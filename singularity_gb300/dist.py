@@ -117,7 +117,10 @@ def gather_frame(local_slice, height: int, band: int):
     """Gathers every rank's slice of one frame to rank 0 and assembles it.
 
     local_slice: this rank's [rows, width, ...] tensor (a CUDA tensor under
-    NCCL, a CPU tensor under gloo).  Slices differ in rows by at most one
+    NCCL, a CPU tensor under gloo).  The collective is ordered after the
+    work queued on torch's current stream: a slice rendered on another stream
+    must be waited for first (`torch.cuda.current_stream().wait_stream(s)`).
+    Slices differ in rows by at most one
     band, so each is padded to the largest for the collective.  Returns the
     [height, width, ...] frame on rank 0 and None on the other ranks; with
     no initialised group (one process), the slice itself."""
