@@ -154,7 +154,7 @@ def _sample_rays(rng, npix: int, width: int, n_pix: int, pass_index: int):
     return gx, gy, s
 
 
-def reference_cpu_rate(O, u_ref, seconds: float = 12.0, seed: int = 0) -> dict:
+def reference_cpu_rate(O, u_ref, seconds: float = 15.0, seed: int = 0) -> dict:
     """The reference's kernel source compiled for the host (oracle/_ref) on all
     host cores: random pixels x 16 samples of the workload, sized to ~`seconds`."""
     threads = os.cpu_count() or 1
