@@ -68,7 +68,7 @@ typedef struct sgx_render_opts {
     uint32_t integrator;     /* sgx_integrator */
     uint32_t format;         /* sgx_format kept by sgx_capture's default */
     float tolerance;         /* adaptive: error tolerance (default 1e-6) */
-    float h_init_frac;       /* adaptive: first step = h_init_frac * r_camera (default 0.02) */
+    float h_init_frac;       /* adaptive: first step = h_init_frac * r_camera (default 0.1) */
     float h_max_frac;        /* adaptive: step ceiling = h_max_frac * r (default 0.1) */
     float fp64_zone;         /* mixed: FP64 control band half-width in M (default 0.05) */
     uint32_t sample_begin;   /* first Halton sample of this pass (default 0) */

@@ -58,7 +58,7 @@ class AdaptiveOpts(C.Structure):
                 ("no_projection", C.c_uint32)]
 
 
-def adaptive_opts(tol=1e-6, h_init_frac=0.02, h_max_frac=0.1, zone=0.05, max_steps=0, mixed=False,
+def adaptive_opts(tol=1e-6, h_init_frac=0.1, h_max_frac=0.1, zone=0.05, max_steps=0, mixed=False,
                   early_capture=True, projection=True) -> "AdaptiveOpts":
     """The adaptive integrator's options (defaults = the library's defaults)."""
     return AdaptiveOpts(tol, h_init_frac, h_max_frac, zone, max_steps, int(bool(mixed)), int(not early_capture),

@@ -300,7 +300,7 @@ void sgx_render_opts_default(sgx_render_opts* o) {
     o->integrator = SGX_INTEGRATOR_FIXED;
     o->format = SGX_FORMAT_RGBA8_SRGB;
     o->tolerance = 1e-6f;
-    o->h_init_frac = 0.02f;
+    o->h_init_frac = 0.1f;
     o->h_max_frac = 0.1f;
     o->fp64_zone = 0.05f;
     o->projection = 1u;
